@@ -1,0 +1,172 @@
+"""Acoustic solve: native plan wrapper and the autograd Function around the CUDA library.
+
+``AcousticSolve.apply(alpha1, alpha2, damp, wavelet, plan)`` replaces the reference's
+``forward_kernel`` time loop (ADFWI/propagator/acoustic_kernels.py:179-301) and its
+autograd backward through ``torch.utils.checkpoint`` (268-278): the forward runs the CUDA
+time loop, the backward runs the hand-written adjoint and returns dL/d alpha1 and
+dL/d alpha2; PyTorch autograd then carries them through alpha = f(pad(vp), pad(rho)).
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _native as N
+
+_SNAP = {"native": N.SNAP_NATIVE, "f32": N.SNAP_NATIVE, "fp32": N.SNAP_NATIVE, "float32": N.SNAP_NATIVE,
+         "bf16": N.SNAP_BF16, "bfloat16": N.SNAP_BF16, "fp16": N.SNAP_FP16, "float16": N.SNAP_FP16}
+
+
+def snapshot_code(precision):
+    if isinstance(precision, int):
+        return precision
+    try:
+        return _SNAP[str(precision).lower()]
+    except KeyError:
+        raise ValueError("snapshot precision must be one of native, bf16, fp16") from None
+
+
+def dtype_code(dtype):
+    if dtype == torch.float32:
+        return N.F32
+    if dtype == torch.float64:
+        return N.F64
+    raise ValueError("adfwi_gb300 propagators support float32 and float64, got %s" % dtype)
+
+
+def _i32(a):
+    return np.ascontiguousarray(np.asarray(a, dtype=np.int64).astype(np.int32))
+
+
+class AcousticPlan(object):
+    """Geometry tables and launch configuration of one acoustic solve shape (host object)."""
+
+    def __init__(self, *, nz, nx, nabc, free_surface, src_z, src_x, rcv_z, rcv_x, nt, dt, dtype,
+                 checkpoint_segments=1, snapshot_every=0, snapshot_precision="native",
+                 shots_per_block=0, memory_budget=0):
+        self.lib = N.lib()
+        self.src_z, self.src_x = _i32(src_z), _i32(src_x)
+        self.rcv_z, self.rcv_x = _i32(rcv_z), _i32(rcv_x)
+        self.ns, self.nr, self.nt = len(self.src_z), len(self.rcv_z), int(nt)
+        self.nz, self.nx, self.nabc = int(nz), int(nx), int(nabc)
+        self.dtype = dtype
+        d = N.AcousticDesc()
+        d.nz, d.nx, d.nabc, d.free_surface = self.nz, self.nx, self.nabc, int(bool(free_surface))
+        d.ns, d.nt, d.nr, d.dtype = self.ns, self.nt, self.nr, dtype_code(dtype)
+        d.checkpoint_segments = int(checkpoint_segments)
+        d.snapshot_every = int(snapshot_every or 0)
+        d.snapshot_precision = snapshot_code(snapshot_precision)
+        d.shots_per_block = int(shots_per_block or 0)
+        d.dt = float(dt)
+        d.memory_budget = int(memory_budget or 0)
+        self.desc = d
+        h = ctypes.c_void_p()
+        rc = self.lib.adfwi_acoustic_plan_create(
+            ctypes.byref(d), self.src_z.ctypes.data_as(ctypes.c_void_p),
+            self.src_x.ctypes.data_as(ctypes.c_void_p), self.rcv_z.ctypes.data_as(ctypes.c_void_p),
+            self.rcv_x.ctypes.data_as(ctypes.c_void_p), ctypes.byref(h))
+        N.check(rc, "adfwi_acoustic_plan_create")
+        self.handle = h
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h is not None and h.value:
+            try:
+                self.lib.adfwi_acoustic_plan_destroy(h)
+            except Exception:
+                pass
+            self.handle = None
+
+    def workspace_bytes(self, with_gradient):
+        b = ctypes.c_int64()
+        N.check(self.lib.adfwi_acoustic_workspace_bytes(self.handle, int(bool(with_gradient)), ctypes.byref(b)),
+                "adfwi_acoustic_workspace_bytes")
+        return b.value
+
+    @property
+    def snapshot_every(self):
+        k = ctypes.c_int32()
+        N.check(self.lib.adfwi_acoustic_snapshot_every(self.handle, ctypes.byref(k)), "adfwi_acoustic_snapshot_every")
+        return k.value
+
+    def _check(self, t, shape, name):
+        if not t.is_cuda:
+            raise RuntimeError("%s must be a CUDA tensor (adfwi_gb300 runs on the GPU only)" % name)
+        if t.dtype != self.dtype:
+            raise TypeError("%s has dtype %s, the plan uses %s" % (name, t.dtype, self.dtype))
+        if tuple(t.shape) != tuple(shape):
+            raise ValueError("%s has shape %s, expected %s" % (name, tuple(t.shape), tuple(shape)))
+        if not t.is_contiguous():
+            raise ValueError("%s must be contiguous" % name)
+
+    def grid_shape(self):
+        return (self.nz + 2 * self.nabc, self.nx + 2 * self.nabc)
+
+    def run_forward(self, alpha1, alpha2, damp, wavelet, with_gradient, workspace=None, records=None,
+                    fw=None, stream=None):
+        """Run the forward solve; returns (rec_p, rec_u, rec_w, fw_p, fw_u, fw_w, workspace)."""
+        g = self.grid_shape()
+        for t, n in ((alpha1, "alpha1"), (alpha2, "alpha2"), (damp, "damp")):
+            self._check(t, g, n)
+        self._check(wavelet, (self.ns, self.nt), "wavelet")
+        dev = alpha1.device
+        need = self.workspace_bytes(with_gradient)
+        if workspace is None:
+            workspace = torch.empty(need, dtype=torch.uint8, device=dev)
+        if records is None:
+            shp = (self.ns, self.nt, self.nr)
+            records = tuple(torch.empty(shp, dtype=self.dtype, device=dev) for _ in range(3)) if self.nr else (None,) * 3
+        if fw is None:
+            fw = tuple(torch.empty((self.nz, self.nx), dtype=self.dtype, device=dev) for _ in range(3))
+        st = ctypes.c_void_p(stream) if stream is not None else N.stream_handle(dev)
+        rc = self.lib.adfwi_acoustic_forward(
+            self.handle, N.ptr(alpha1), N.ptr(alpha2), N.ptr(damp), N.ptr(wavelet),
+            N.ptr(records[0]), N.ptr(records[1]), N.ptr(records[2]), N.ptr(fw[0]), N.ptr(fw[1]), N.ptr(fw[2]),
+            int(bool(with_gradient)), N.ptr(workspace), workspace.numel(), st)
+        N.check(rc, "adfwi_acoustic_forward")
+        return records + fw + (workspace,)
+
+    def run_backward(self, alpha1, alpha2, damp, wavelet, grads, workspace, stream=None):
+        """Adjoint solve after run_forward(with_gradient=True); returns (dL/d alpha1, dL/d alpha2)."""
+        shp = (self.ns, self.nt, self.nr)
+        gs = []
+        for gr, n in zip(grads, ("grad_rec_p", "grad_rec_u", "grad_rec_w")):
+            if gr is not None:
+                gr = gr.to(dtype=self.dtype).contiguous()
+                self._check(gr, shp, n)
+            gs.append(gr)
+        ga1 = torch.empty_like(alpha1)
+        ga2 = torch.empty_like(alpha2)
+        st = ctypes.c_void_p(stream) if stream is not None else N.stream_handle(alpha1.device)
+        rc = self.lib.adfwi_acoustic_backward(
+            self.handle, N.ptr(alpha1), N.ptr(alpha2), N.ptr(damp), N.ptr(wavelet),
+            N.ptr(gs[0]), N.ptr(gs[1]), N.ptr(gs[2]), N.ptr(ga1), N.ptr(ga2), N.ptr(workspace),
+            workspace.numel(), st)
+        N.check(rc, "adfwi_acoustic_backward")
+        return ga1, ga2
+
+
+class AcousticSolve(torch.autograd.Function):
+    """records, forward wavefields = solve(alpha1, alpha2); backward = hand-written adjoint."""
+
+    @staticmethod
+    def forward(ctx, alpha1, alpha2, damp, wavelet, plan):
+        alpha1 = alpha1.contiguous()
+        alpha2 = alpha2.contiguous()
+        damp = damp.contiguous()
+        wavelet = wavelet.contiguous()
+        need_grad = bool(ctx.needs_input_grad[0] or ctx.needs_input_grad[1])
+        rp, ru, rw, fp, fu, fw, ws = plan.run_forward(alpha1, alpha2, damp, wavelet, need_grad)
+        ctx.plan = plan
+        ctx.ws = ws if need_grad else None
+        ctx.save_for_backward(alpha1, alpha2, damp, wavelet)
+        ctx.mark_non_differentiable(fp, fu, fw)
+        return rp, ru, rw, fp, fu, fw
+
+    @staticmethod
+    def backward(ctx, grp, gru, grw, _gfp, _gfu, _gfw):
+        alpha1, alpha2, damp, wavelet = ctx.saved_tensors
+        if ctx.ws is None:
+            raise RuntimeError("AcousticSolve.backward called without a gradient-mode forward")
+        ga1, ga2 = ctx.plan.run_backward(alpha1, alpha2, damp, wavelet, (grp, gru, grw), ctx.ws)
+        return ga1, ga2, None, None, None

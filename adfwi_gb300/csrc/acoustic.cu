@@ -1,0 +1,981 @@
+// Acoustic (p, u, w) 4th-order staggered-grid propagator for sm_103a: forward step,
+// exact discrete adjoint step, checkpoint / recompute driver and the C ABI.
+//
+// Reference algorithm (paths inside liufeng2317/ADFWI):
+//   ADFWI/propagator/acoustic_kernels.py:113-174  one time step (p update, source, free-surface
+//                                                 mirror, u and w updates, w mirror, receivers,
+//                                                 illumination sums)
+//   ADFWI/propagator/acoustic_kernels.py:252-265  alpha / kappa coefficient definitions
+//   ADFWI/propagator/acoustic_kernels.py:268-301  chunked time loop and the record dict
+//
+// One launch advances one time step of all shots. A thread block owns a TZ x TX tile of one
+// grid and loops over a group of shots, so that the coefficient tiles it stages in shared
+// memory are reused by every shot of the group. Within a shot the block computes the new
+// pressure on the tile plus a halo (1 row/column before, 2 after) from u and w staged in
+// shared memory, and then the new u and w on the tile from that pressure: p, u and w each
+// cross HBM once per step (ping-pong buffers keep the Jacobi semantics of the reference's
+// slice assignments). The forward arithmetic uses explicitly rounded operations (no FMA
+// contraction) in the reference's evaluation order, so float32 records reproduce the
+// reference's PyTorch CPU results bit for bit.
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string.h>
+
+#include <algorithm>
+#include <cmath>
+#include <new>
+#include <vector>
+
+#include "../../include/adfwi_gb300.h"
+#include "common.cuh"
+#include "snapshot.cuh"
+
+namespace adfwi {
+namespace ac {
+
+constexpr int TX = 32;        // tile columns = threads in x
+constexpr int TZ = 16;        // tile rows
+constexpr int BY = 8;         // thread rows
+constexpr int RPT = TZ / BY;  // tile rows per thread
+constexpr int NT = TX * BY;   // threads per block
+constexpr int EZ = TZ + 3, EX = TX + 3;  // p halo region: rows i0-1..i0+TZ+1, cols j0-1..j0+TX+1
+constexpr int UZ = TZ + 3, UX = TX + 6;  // u region: rows i0-1..i0+TZ+1, cols j0-3..j0+TX+2
+constexpr int WZ = TZ + 6, WX = TX + 3;  // w region: rows i0-3..i0+TZ+2, cols j0-1..j0+TX+1
+constexpr int AZ = TZ + 6, AX = TX + 6;  // union of the u and w regions (adjoint alpha2)
+
+// Explicitly rounded arithmetic (keeps the reference's operation order; no FMA contraction).
+__device__ __forceinline__ float radd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float rsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float rmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double radd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double rsub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double rmul(double a, double b) { return __dmul_rn(a, b); }
+
+template <typename T>
+struct Geo {
+  Layout L;
+  int ns, nt, nr;
+  int fs;     // first stencil row of u/w (nabc with a free surface, else 1)
+  int fsurf;  // free surface on / off
+  int zbeg;   // first tiled row (fs-1 with a free surface: rows above never change)
+  int tiles_x;
+  int nabc, nz, nx;
+  T dt;
+  T c1, c2;
+  const int* src_z;          // padded source rows (ns)
+  const int* src_x;          // padded source columns (ns)
+  const int* tile_rcv_beg;   // ntiles+1 offsets into trcv_*
+  const int* trcv_cell;      // (local row << 16) | local column
+  const int* trcv_id;        // receiver index
+  const int* tile_cell_beg;  // ntiles+1 offsets into tcell_*
+  const int* tcell_cell;     // unique receiver cells of a tile, packed like trcv_cell
+  const int* tcell_rbeg;     // ncells+1 offsets into cell_rcv
+  const int* cell_rcv;       // receiver indices grouped by unique cell
+};
+
+// Update regions of acoustic_kernels.py:115, 139, 151.
+template <typename T>
+__device__ __forceinline__ bool in_p(const Geo<T>& g, int i, int j) {
+  return i >= g.fs + 1 && i <= g.L.nzp - 3 && j >= 2 && j <= g.L.nxp - 3;
+}
+template <typename T>
+__device__ __forceinline__ bool in_u(const Geo<T>& g, int i, int j) {
+  return i >= g.fs && i <= g.L.nzp - 2 && j >= 1 && j <= g.L.nxp - 3;
+}
+template <typename T>
+__device__ __forceinline__ bool in_w(const Geo<T>& g, int i, int j) {
+  return i >= g.fs && i <= g.L.nzp - 3 && j >= 1 && j <= g.L.nxp - 2;
+}
+template <typename T>
+__device__ __forceinline__ bool in_window(const Geo<T>& g, int i, int j) {
+  return i >= g.nabc && i < g.nabc + g.nz && j >= g.nabc && j < g.nabc + g.nx;
+}
+
+template <typename T>
+struct FwdSmem {
+  T su[UZ][UX];
+  T sw[WZ][WX];
+  T sp[EZ][EX];
+  T sa1[EZ][EX];
+  T sd[EZ][EX];
+  T sa2[TZ][TX];
+  T sou[TZ][TX];
+  T sow[TZ][TX];
+};
+
+// Divergence c1*(u[j]-u[j-1]+w[i]-w[i-1]) + c2*(u[j+1]-u[j-2]+w[i+1]-w[i-2]) in the
+// reference's left-to-right order; (r, c) are p-halo coordinates of (i, j).
+template <typename T>
+__device__ __forceinline__ T divergence(const FwdSmem<T>& s, const Geo<T>& g, int r, int c) {
+  T t1 = rsub(radd(rsub(s.su[r][c + 2], s.su[r][c + 1]), s.sw[r + 2][c]), s.sw[r + 1][c]);
+  T t2 = rsub(radd(rsub(s.su[r][c + 3], s.su[r][c]), s.sw[r + 3][c]), s.sw[r][c]);
+  return radd(rmul(g.c1, t1), rmul(g.c2, t2));
+}
+
+// New pressure at grid cell (i, j) with p-halo coordinates (r, c), before the mirror.
+template <typename T>
+__device__ __forceinline__ T eval_p(const FwdSmem<T>& s, const Geo<T>& g, const T* __restrict__ P0,
+                                    int i, int j, int r, int c, int sz, int sx, T sval) {
+  T v = P0[g.L.off(i, j)];
+  if (in_p(g, i, j)) {
+    T k1 = rmul(s.sd[r][c], g.dt);
+    v = rsub(rmul(rsub(T(1), k1), v), rmul(s.sa1[r][c], divergence(s, g, r, c)));
+  }
+  if (i == sz && j == sx) v = radd(v, sval);
+  return v;
+}
+
+// One forward time step of shots [blockIdx.z*G, ...). Optional outputs may be null.
+template <typename T>
+__global__ void __launch_bounds__(NT) fwd_step(
+    Geo<T> g, int it, int G, int accum_u, const T* __restrict__ a1, const T* __restrict__ a2,
+    const T* __restrict__ damp, const T* __restrict__ wav, const T* __restrict__ p0,
+    const T* __restrict__ u0, const T* __restrict__ w0, T* __restrict__ p1, T* __restrict__ u1,
+    T* __restrict__ w1, T* __restrict__ d1, T* __restrict__ rec_p, T* __restrict__ rec_u,
+    T* __restrict__ rec_w, T* __restrict__ ill_p, T* __restrict__ ill_u) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  FwdSmem<T>& s = *reinterpret_cast<FwdSmem<T>*>(smem_raw);
+  const Layout L = g.L;
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
+  const int tile = blockIdx.y * g.tiles_x + blockIdx.x;
+  const int i0 = g.zbeg + blockIdx.y * TZ, j0 = blockIdx.x * TX;
+
+  for (int e = tid; e < EZ * EX; e += NT) {
+    int r = e / EX, c = e - r * EX;
+    int64_t o = L.off(i0 - 1 + r, j0 - 1 + c);
+    s.sa1[r][c] = a1[o];
+    s.sd[r][c] = damp[o];
+  }
+#pragma unroll
+  for (int k = 0; k < RPT; ++k) s.sa2[ty + BY * k][tx] = a2[L.off(i0 + ty + BY * k, j0 + tx)];
+
+  T acc_p[RPT], acc_u[RPT];
+#pragma unroll
+  for (int k = 0; k < RPT; ++k) acc_p[k] = acc_u[k] = T(0);
+
+  const int s_beg = blockIdx.z * G, s_end = min(g.ns, s_beg + G);
+  const int rb = g.tile_rcv_beg[tile], re = g.tile_rcv_beg[tile + 1];
+  for (int sh = s_beg; sh < s_end; ++sh) {
+    const int64_t so = (int64_t)sh * L.plane;
+    const T* P0 = p0 + so;
+    const T* U0 = u0 + so;
+    const T* W0 = w0 + so;
+    for (int e = tid; e < UZ * UX; e += NT) {
+      int r = e / UX, c = e - r * UX;
+      s.su[r][c] = U0[L.off(i0 - 1 + r, j0 - 3 + c)];
+    }
+    for (int e = tid; e < WZ * WX; e += NT) {
+      int r = e / WX, c = e - r * WX;
+      s.sw[r][c] = W0[L.off(i0 - 3 + r, j0 - 1 + c)];
+    }
+    __syncthreads();
+    const int sz = g.src_z[sh], sx = g.src_x[sh];
+    const T sval = rmul(g.dt, wav[(int64_t)sh * g.nt + it]);
+    for (int e = tid; e < EZ * EX; e += NT) {
+      int r = e / EX, c = e - r * EX;
+      int i = i0 - 1 + r, j = j0 - 1 + c;
+      T v = T(0);
+      if (i >= g.zbeg && i < L.nzp && j >= 0 && j < L.nxp) {
+        if (g.fsurf && i == g.fs - 1)  // p[fs-1] = -p[fs+1]  (acoustic_kernels.py:135-136)
+          v = -eval_p(s, g, P0, i + 2, j, r + 2, c, sz, sx, sval);
+        else
+          v = eval_p(s, g, P0, i, j, r, c, sz, sx, sval);
+      }
+      s.sp[r][c] = v;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < RPT; ++k) {
+      const int li = ty + BY * k;
+      const int i = i0 + li, j = j0 + tx;
+      const int r = li + 1, c = tx + 1;
+      T pv = s.sp[r][c];
+      // u update (acoustic_kernels.py:139-148)
+      T uo = s.su[r][c + 2];
+      T un = uo;
+      if (in_u(g, i, j)) {
+        T k2 = rmul(rmul(T(0.5), radd(s.sd[r][c], s.sd[r][c + 1])), g.dt);
+        T dpx = radd(rmul(g.c1, rsub(s.sp[r][c + 1], s.sp[r][c])),
+                     rmul(g.c2, rsub(s.sp[r][c + 2], s.sp[r][c - 1])));
+        un = rsub(rmul(rsub(T(1), k2), uo), rmul(s.sa2[li][tx], dpx));
+      }
+      // w update (acoustic_kernels.py:151-160); w[fs-1] = w[fs] mirror (163-164)
+      const int ie = (g.fsurf && i == g.fs - 1) ? g.fs : i;
+      const int rr = r + (ie - i);
+      T wo = s.sw[rr + 2][c];
+      T wn = wo;
+      if (in_w(g, ie, j)) {
+        T k3 = rmul(rmul(T(0.5), radd(s.sd[rr][c], s.sd[rr + 1][c])), g.dt);
+        T dpz = radd(rmul(g.c1, rsub(s.sp[rr + 1][c], s.sp[rr][c])),
+                     rmul(g.c2, rsub(s.sp[rr + 2][c], s.sp[rr - 1][c])));
+        wn = rsub(rmul(rsub(T(1), k3), wo), rmul(s.sa2[rr - 1][tx], dpz));
+      }
+      s.sou[li][tx] = un;
+      s.sow[li][tx] = wn;
+      if (i < L.nzp && j < L.nxp) {
+        const int64_t o = so + L.off(i, j);
+        p1[o] = pv;
+        u1[o] = un;
+        w1[o] = wn;
+        if (d1 != nullptr) d1[o] = in_p(g, i, j) ? divergence(s, g, r, c) : T(0);
+        if (in_window(g, i, j)) {
+          acc_p[k] += pv * pv;
+          acc_u[k] += un * un;
+        }
+      }
+    }
+    __syncthreads();
+    if (rec_p != nullptr && ty == 0) {
+      const int64_t rowbase = ((int64_t)sh * g.nt + it) * g.nr;
+      for (int q = rb + tx; q < re; q += TX) {
+        int cell = g.trcv_cell[q];
+        int li = cell >> 16, lj = cell & 0xffff;
+        int64_t o = rowbase + g.trcv_id[q];
+        rec_p[o] = s.sp[li + 1][lj + 1];
+        rec_u[o] = s.sou[li][lj];
+        rec_w[o] = s.sow[li][lj];
+      }
+    }
+  }
+  if (ill_p != nullptr) {
+    const int64_t go = (int64_t)blockIdx.z * L.plane;
+#pragma unroll
+    for (int k = 0; k < RPT; ++k) {
+      const int i = i0 + ty + BY * k, j = j0 + tx;
+      if (i < L.nzp && j < L.nxp && in_window(g, i, j)) {
+        ill_p[go + L.off(i, j)] += acc_p[k];
+        if (accum_u) ill_u[go + L.off(i, j)] += acc_u[k];
+      }
+    }
+  }
+}
+
+template <typename T>
+struct AdjSmem {
+  T qu[UZ][UX];  // -alpha2 * lambda_u on the u region (zero outside the u update region)
+  T qw[WZ][WX];  // -alpha2 * lambda_w on the w region
+  T lp[EZ][EX];  // lambda_p after the u/w transposes and the free-surface fold
+  T ph[EZ][EX];  // forward pressure after this step (history)
+  T sa1[EZ][EX];
+  T sd[EZ][EX];
+  T sa2[AZ][AX];
+  T op[TZ][TX];
+  T ou[TZ][TX];
+  T ow[TZ][TX];
+};
+
+template <typename T>
+__device__ __forceinline__ T adj_lp(const AdjSmem<T>& s, const Geo<T>& g, const T* __restrict__ LP0,
+                                    int i, int j, int r, int c) {
+  // lambda_p + D_x^T(q_u) + D_z^T(q_w): transposes of the forward differences of p used by
+  // the u and w updates (acoustic_kernels.py:143-146, 155-158).
+  T v = LP0[g.L.off(i, j)];
+  v += g.c1 * (s.qu[r][c + 1] - s.qu[r][c + 2]) + g.c2 * (s.qu[r][c] - s.qu[r][c + 3]);
+  v += g.c1 * (s.qw[r + 1][c] - s.qw[r + 2][c]) + g.c2 * (s.qw[r][c] - s.qw[r + 3][c]);
+  return v;
+}
+
+template <typename T>
+__device__ __forceinline__ T qp_at(const AdjSmem<T>& s, const Geo<T>& g, int i, int j, int r, int c) {
+  return in_p(g, i, j) ? -s.sa1[r][c] * s.lp[r][c] : T(0);
+}
+
+// Reverse of forward step `it`. Input lambda = dL/d(state after step it) including the
+// receiver injection of step it and the w-mirror fold; output = the same for step it-1.
+// Accumulates dL/d alpha1 and dL/d alpha2 of this step into per-group partial planes.
+template <typename T>
+__global__ void __launch_bounds__(NT) adj_step(
+    Geo<T> g, int it, int G, const T* __restrict__ a1, const T* __restrict__ a2,
+    const T* __restrict__ damp, const T* __restrict__ lp0, const T* __restrict__ lu0,
+    const T* __restrict__ lw0, T* __restrict__ lp1, T* __restrict__ lu1, T* __restrict__ lw1,
+    const T* __restrict__ phist, const T* __restrict__ dhist, const T* __restrict__ gr_p,
+    const T* __restrict__ gr_u, const T* __restrict__ gr_w, T* __restrict__ g1,
+    T* __restrict__ g2) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  AdjSmem<T>& s = *reinterpret_cast<AdjSmem<T>*>(smem_raw);
+  const Layout L = g.L;
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
+  const int tile = blockIdx.y * g.tiles_x + blockIdx.x;
+  const int i0 = g.zbeg + blockIdx.y * TZ, j0 = blockIdx.x * TX;
+
+  for (int e = tid; e < EZ * EX; e += NT) {
+    int r = e / EX, c = e - r * EX;
+    int64_t o = L.off(i0 - 1 + r, j0 - 1 + c);
+    s.sa1[r][c] = a1[o];
+    s.sd[r][c] = damp[o];
+  }
+  for (int e = tid; e < AZ * AX; e += NT) {
+    int r = e / AX, c = e - r * AX;
+    s.sa2[r][c] = a2[L.off(i0 - 3 + r, j0 - 3 + c)];
+  }
+  __syncthreads();
+
+  T ag1[RPT], ag2[RPT];
+#pragma unroll
+  for (int k = 0; k < RPT; ++k) ag1[k] = ag2[k] = T(0);
+
+  const int s_beg = blockIdx.z * G, s_end = min(g.ns, s_beg + G);
+  const int cb = g.tile_cell_beg[tile], ce = g.tile_cell_beg[tile + 1];
+  const bool inject = (it >= 1) && (gr_p != nullptr || gr_u != nullptr || gr_w != nullptr);
+  for (int sh = s_beg; sh < s_end; ++sh) {
+    const int64_t so = (int64_t)sh * L.plane;
+    const T* LP0 = lp0 + so;
+    const T* LU0 = lu0 + so;
+    const T* LW0 = lw0 + so;
+    const T* PH = phist + so;
+    for (int e = tid; e < UZ * UX; e += NT) {
+      int r = e / UX, c = e - r * UX;
+      int i = i0 - 1 + r, j = j0 - 3 + c;
+      s.qu[r][c] = in_u(g, i, j) ? -s.sa2[r + 2][c] * LU0[L.off(i, j)] : T(0);
+    }
+    for (int e = tid; e < WZ * WX; e += NT) {
+      int r = e / WX, c = e - r * WX;
+      int i = i0 - 3 + r, j = j0 - 1 + c;
+      s.qw[r][c] = in_w(g, i, j) ? -s.sa2[r][c + 2] * LW0[L.off(i, j)] : T(0);
+    }
+    for (int e = tid; e < EZ * EX; e += NT) {
+      int r = e / EX, c = e - r * EX;
+      s.ph[r][c] = PH[L.off(i0 - 1 + r, j0 - 1 + c)];
+    }
+    __syncthreads();
+    for (int e = tid; e < EZ * EX; e += NT) {
+      int r = e / EX, c = e - r * EX;
+      int i = i0 - 1 + r, j = j0 - 1 + c;
+      T v = T(0);
+      if (i >= 0 && i < L.nzp && j >= 0 && j < L.nxp) {
+        if (g.fsurf && i == g.fs - 1) {
+          v = T(0);  // adjoint of p[fs-1] = -p[fs+1]: the mirrored row carries no sensitivity
+        } else {
+          v = adj_lp(s, g, LP0, i, j, r, c);
+          if (g.fsurf && i == g.fs + 1 && r >= 2) v -= adj_lp(s, g, LP0, i - 2, j, r - 2, c);
+        }
+      }
+      s.lp[r][c] = v;
+    }
+    __syncthreads();
+    const T* DH = dhist + so;
+#pragma unroll
+    for (int k = 0; k < RPT; ++k) {
+      const int li = ty + BY * k;
+      const int i = i0 + li, j = j0 + tx;
+      const int r = li + 1, c = tx + 1;
+      T lpm = s.lp[r][c];
+      T lpo = lpm;
+      T qc = qp_at(s, g, i, j, r, c);
+      if (in_p(g, i, j)) {
+        lpo = (T(1) - s.sd[r][c] * g.dt) * lpm;
+        ag1[k] -= lpm * DH[L.off(i, j)];
+      }
+      const int64_t oo = L.off(i, j);
+      T luin = (i < L.nzp && j < L.nxp) ? LU0[oo] : T(0);
+      T lwin = (i < L.nzp && j < L.nxp) ? LW0[oo] : T(0);
+      T luo = luin, lwo = lwin;
+      if (in_u(g, i, j)) {
+        T k2 = T(0.5) * (s.sd[r][c] + s.sd[r][c + 1]) * g.dt;
+        luo = (T(1) - k2) * luin;
+        T dpx = g.c1 * (s.ph[r][c + 1] - s.ph[r][c]) + g.c2 * (s.ph[r][c + 2] - s.ph[r][c - 1]);
+        ag2[k] -= luin * dpx;
+      }
+      if (in_w(g, i, j)) {
+        T k3 = T(0.5) * (s.sd[r][c] + s.sd[r + 1][c]) * g.dt;
+        lwo = (T(1) - k3) * lwin;
+        T dpz = g.c1 * (s.ph[r + 1][c] - s.ph[r][c]) + g.c2 * (s.ph[r + 2][c] - s.ph[r - 1][c]);
+        ag2[k] -= lwin * dpz;
+      }
+      // transposes of the p update's differences of u and w (acoustic_kernels.py:119-126)
+      luo += g.c1 * (qc - qp_at(s, g, i, j + 1, r, c + 1)) +
+             g.c2 * (qp_at(s, g, i, j - 1, r, c - 1) - qp_at(s, g, i, j + 2, r, c + 2));
+      lwo += g.c1 * (qc - qp_at(s, g, i + 1, j, r + 1, c)) +
+             g.c2 * (qp_at(s, g, i - 1, j, r - 1, c) - qp_at(s, g, i + 2, j, r + 2, c));
+      s.op[li][tx] = lpo;
+      s.ou[li][tx] = luo;
+      s.ow[li][tx] = lwo;
+    }
+    __syncthreads();
+    if (inject && ty == 0) {
+      // dL/d records of step it-1 enter the state after step it-1 (acoustic_kernels.py:167-169)
+      const int64_t rowbase = ((int64_t)sh * g.nt + (it - 1)) * g.nr;
+      for (int q = cb + tx; q < ce; q += TX) {
+        int cell = g.tcell_cell[q];
+        int li = cell >> 16, lj = cell & 0xffff;
+        T ap = T(0), au = T(0), aw = T(0);
+        for (int m = g.tcell_rbeg[q]; m < g.tcell_rbeg[q + 1]; ++m) {
+          int64_t o = rowbase + g.cell_rcv[m];
+          if (gr_p) ap += gr_p[o];
+          if (gr_u) au += gr_u[o];
+          if (gr_w) aw += gr_w[o];
+        }
+        s.op[li][lj] += ap;
+        s.ou[li][lj] += au;
+        s.ow[li][lj] += aw;
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < RPT; ++k) {
+      const int li = ty + BY * k;
+      const int i = i0 + li, j = j0 + tx;
+      if (i < L.nzp && j < L.nxp) {
+        const int64_t o = so + L.off(i, j);
+        T wv = s.ow[li][tx];
+        if (g.fsurf && i == g.fs - 1) wv = T(0);                    // adjoint of w[fs-1] = w[fs]
+        if (g.fsurf && i == g.fs && li >= 1) wv += s.ow[li - 1][tx];
+        lp1[o] = s.op[li][tx];
+        lu1[o] = s.ou[li][tx];
+        lw1[o] = wv;
+      }
+    }
+    __syncthreads();
+  }
+  const int64_t go = (int64_t)blockIdx.z * L.plane;
+#pragma unroll
+  for (int k = 0; k < RPT; ++k) {
+    const int i = i0 + ty + BY * k, j = j0 + tx;
+    if (i < L.nzp && j < L.nxp) {
+      g1[go + L.off(i, j)] += ag1[k];
+      g2[go + L.off(i, j)] += ag2[k];
+    }
+  }
+}
+
+// Seed of the reverse pass: lambda = injection of the records of the last step.
+template <typename T>
+__global__ void adj_seed(Geo<T> g, int ntiles, const T* __restrict__ gr_p, const T* __restrict__ gr_u,
+                         const T* __restrict__ gr_w, T* lp, T* lu, T* lw) {
+  const int sh = blockIdx.y;
+  const int64_t rowbase = ((int64_t)sh * g.nt + (g.nt - 1)) * g.nr;
+  const int ncell = g.tile_cell_beg[ntiles];
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < ncell; q += gridDim.x * blockDim.x) {
+    int tile = 0;
+    {  // locate the tile of unique cell q (binary search on tile_cell_beg)
+      int lo = 0, hi = ntiles;
+      while (hi - lo > 1) {
+        int mid = (lo + hi) >> 1;
+        if (g.tile_cell_beg[mid] <= q) lo = mid; else hi = mid;
+      }
+      tile = lo;
+    }
+    int cell = g.tcell_cell[q];
+    int i = g.zbeg + (tile / g.tiles_x) * TZ + (cell >> 16);
+    int j = (tile % g.tiles_x) * TX + (cell & 0xffff);
+    T ap = T(0), au = T(0), aw = T(0);
+    for (int m = g.tcell_rbeg[q]; m < g.tcell_rbeg[q + 1]; ++m) {
+      int64_t o = rowbase + g.cell_rcv[m];
+      if (gr_p) ap += gr_p[o];
+      if (gr_u) au += gr_u[o];
+      if (gr_w) aw += gr_w[o];
+    }
+    int64_t o = (int64_t)sh * g.L.plane + g.L.off(i, j);
+    lp[o] += ap;
+    lu[o] += au;
+    lw[o] += aw;
+  }
+}
+
+// Copy a dense (h, w) array into a pitched plane at cell (0, 0) (ghosts untouched).
+template <typename T>
+__global__ void pack_plane(Layout L, int h, int w, const T* __restrict__ src, T* __restrict__ dst) {
+  int64_t n = (int64_t)h * w;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+    int i = (int)(e / w), j = (int)(e - (int64_t)i * w);
+    dst[L.off(i, j)] = src[e];
+  }
+}
+
+// dst(h, w) = sum over `groups` partial planes of the window starting at (oi, oj).
+template <typename T>
+__global__ void reduce_planes(Layout L, int groups, int oi, int oj, int h, int w, const T* __restrict__ src,
+                              T* __restrict__ dst) {
+  int64_t n = (int64_t)h * w;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+    int i = (int)(e / w), j = (int)(e - (int64_t)i * w);
+    T acc = T(0);
+    for (int q = 0; q < groups; ++q) acc += src[(int64_t)q * L.plane + L.off(oi + i, oj + j)];
+    dst[e] = acc;
+  }
+}
+
+// forward_wavefield_{p,u,w} of the reference (acoustic_kernels.py:172-174, 285-288):
+// fw_p = P, fw_u = P + U(last chunk), fw_w = fw_p + (U(last chunk) + sum_s w(last step)^2).
+template <typename T>
+__global__ void illum_finalize(Layout L, int groups, int ns, int nabc, int nz, int nx, const T* __restrict__ ip,
+                               const T* __restrict__ iu, const T* __restrict__ wlast, T* fw_p, T* fw_u,
+                               T* fw_w) {
+  int64_t n = (int64_t)nz * nx;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+    int i = (int)(e / nx) + nabc, j = (int)(e % nx) + nabc;
+    T P = T(0), U = T(0), W = T(0);
+    for (int q = 0; q < groups; ++q) {
+      P += ip[(int64_t)q * L.plane + L.off(i, j)];
+      U += iu[(int64_t)q * L.plane + L.off(i, j)];
+    }
+    for (int s = 0; s < ns; ++s) {
+      T v = wlast[(int64_t)s * L.plane + L.off(i, j)];
+      W += v * v;
+    }
+    if (fw_p) fw_p[e] = P;
+    if (fw_u) fw_u[e] = P + U;
+    if (fw_w) fw_w[e] = P + (U + W);
+  }
+}
+
+}  // namespace ac
+}  // namespace adfwi
+
+// ----------------------------------------------------------------------------------------
+// Plan, workspace and drivers.
+// ----------------------------------------------------------------------------------------
+using namespace adfwi;
+
+struct adfwi_acoustic_plan {
+  adfwi_acoustic_desc d;
+  int nzp, nxp, fs, zbeg;
+  int tiles_x, tiles_z, ntiles;
+  int G, ngroups;
+  int K, nseg;           // snapshot interval and number of segments (gradient mode)
+  int last_chunk_start;  // first step of the reference's last checkpoint chunk
+  int elem;              // bytes per element
+  Layout L;
+  std::vector<int32_t> tab;  // geometry tables, uploaded into the workspace
+  int64_t o_srcz, o_srcx, o_trb, o_trc, o_tri, o_tcb, o_tcc, o_tcr, o_cr;
+  int ncells;
+};
+
+namespace {
+
+struct Carve {
+  int64_t coef, fa, fb, ilp, ilu, tab;  // forward
+  int64_t snap, snap_scale, hp, hd, la, lb, g1, g2;  // gradient extras
+  int64_t total;
+};
+
+int64_t align256(int64_t x) { return (x + 255) / 256 * 256; }
+
+Carve carve(const adfwi_acoustic_plan* p, bool grad, int K) {
+  Carve c{};
+  const int64_t pl = p->L.plane * p->elem;
+  const int64_t ns = p->d.ns;
+  int64_t o = 0;
+  auto take = [&](int64_t bytes) { int64_t at = o; o += align256(bytes); return at; };
+  c.coef = take(3 * pl);
+  c.fa = take(3 * ns * pl);
+  c.fb = take(3 * ns * pl);
+  c.ilp = take((int64_t)p->ngroups * pl);
+  c.ilu = take((int64_t)p->ngroups * pl);
+  c.tab = take((int64_t)p->tab.size() * 4);
+  if (grad) {
+    const int nseg = (p->d.nt + K - 1) / K;
+    const bool full = K >= p->d.nt;
+    const int64_t snap_elem = p->d.snapshot_precision == ADFWI_SNAP_NATIVE ? p->elem : 2;
+    c.snap = take(full ? 0 : (int64_t)nseg * 3 * ns * p->L.plane * snap_elem);
+    c.snap_scale = take(full ? 0 : (int64_t)nseg * 3 * ns * 4);
+    c.hp = take((int64_t)K * ns * pl);
+    c.hd = take((int64_t)K * ns * pl);
+    c.la = take(3 * ns * pl);
+    c.lb = take(3 * ns * pl);
+    c.g1 = take((int64_t)p->ngroups * pl);
+    c.g2 = take((int64_t)p->ngroups * pl);
+  }
+  c.total = o;
+  return c;
+}
+
+int choose_K(const adfwi_acoustic_plan* p) {
+  const int nt = p->d.nt;
+  const int64_t budget = p->d.memory_budget;
+  if (p->d.snapshot_every > 0) return std::min(p->d.snapshot_every, nt);
+  if (budget <= 0) return std::min(nt, std::max(1, (int)std::ceil(std::sqrt(1.5 * nt))));
+  // The whole history fits: the forward pass keeps it and no step is recomputed.
+  if (carve(p, true, nt).total <= budget) return nt;
+  // Otherwise: memory(K) = snapshots (falling with K) + segment history (rising with K) is
+  // smallest near K* = sqrt(1.5 nt); take the longest segment beyond K* that still fits
+  // (one recomputation pass either way, fewer snapshots).
+  int kstar = std::min(nt - 1, std::max(1, (int)std::lround(std::sqrt(1.5 * nt))));
+  while (kstar > 1 && carve(p, true, kstar - 1).total < carve(p, true, kstar).total) --kstar;
+  while (kstar < nt - 1 && carve(p, true, kstar + 1).total < carve(p, true, kstar).total) ++kstar;
+  if (carve(p, true, kstar).total > budget) return kstar;  // does not fit at all: the call reports it
+  int lo = kstar, hi = nt - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) / 2;
+    if (carve(p, true, mid).total <= budget) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+template <typename T>
+ac::Geo<T> make_geo(const adfwi_acoustic_plan* p, const unsigned char* ws, const Carve& c) {
+  ac::Geo<T> g;
+  g.L = p->L;
+  g.ns = p->d.ns;
+  g.nt = p->d.nt;
+  g.nr = p->d.nr;
+  g.fs = p->fs;
+  g.fsurf = p->d.free_surface;
+  g.zbeg = p->zbeg;
+  g.tiles_x = p->tiles_x;
+  g.nabc = p->d.nabc;
+  g.nz = p->d.nz;
+  g.nx = p->d.nx;
+  g.dt = (T)p->d.dt;
+  g.c1 = (T)(9.0 / 8.0);
+  g.c2 = (T)(-1.0 / 24.0);
+  const int32_t* tb = reinterpret_cast<const int32_t*>(ws + c.tab);
+  g.src_z = tb + p->o_srcz;
+  g.src_x = tb + p->o_srcx;
+  g.tile_rcv_beg = tb + p->o_trb;
+  g.trcv_cell = tb + p->o_trc;
+  g.trcv_id = tb + p->o_tri;
+  g.tile_cell_beg = tb + p->o_tcb;
+  g.tcell_cell = tb + p->o_tcc;
+  g.tcell_rbeg = tb + p->o_tcr;
+  g.cell_rcv = tb + p->o_cr;
+  return g;
+}
+
+int grid_blocks(int64_t n) { return (int)std::min<int64_t>(std::max<int64_t>((n + 255) / 256, 1), 152 * 16); }
+
+template <typename T>
+int setup_common(const adfwi_acoustic_plan* p, unsigned char* ws, const Carve& c, const void* alpha1,
+                 const void* alpha2, const void* damp, cudaStream_t st) {
+  const int64_t pl = p->L.plane * p->elem;
+  // Zero coefficient planes (ghosts), field buffers and illumination partials.
+  ADFWI_CUDA_TRY(cudaMemsetAsync(ws + c.coef, 0, c.tab - c.coef, st));
+  ADFWI_CUDA_TRY(cudaMemcpyAsync(ws + c.tab, p->tab.data(), p->tab.size() * 4, cudaMemcpyHostToDevice, st));
+  const int64_t n = (int64_t)p->nzp * p->nxp;
+  T* cf = reinterpret_cast<T*>(ws + c.coef);
+  const void* src[3] = {alpha1, alpha2, damp};
+  for (int q = 0; q < 3; ++q) {
+    ac::pack_plane<T><<<grid_blocks(n), 256, 0, st>>>(p->L, p->nzp, p->nxp, static_cast<const T*>(src[q]),
+                                                      reinterpret_cast<T*>(reinterpret_cast<unsigned char*>(cf) + q * pl));
+  }
+  ADFWI_CUDA_TRY(cudaGetLastError());
+  return kOk;
+}
+
+template <typename T>
+void launch_fwd(const adfwi_acoustic_plan* p, const ac::Geo<T>& g, int it, int accum_u, const T* cf,
+                const T* wav, const T* p0, const T* u0, const T* w0, T* p1, T* u1, T* w1, T* d1,
+                T* rp, T* ru, T* rw, T* ilp, T* ilu, cudaStream_t st) {
+  const int64_t pl = p->L.plane;
+  dim3 grid(p->tiles_x, p->tiles_z, p->ngroups);
+  dim3 block(ac::TX, ac::BY);
+  ac::fwd_step<T><<<grid, block, sizeof(ac::FwdSmem<T>), st>>>(
+      g, it, p->G, accum_u, cf, cf + pl, cf + 2 * pl, wav, p0, u0, w0, p1, u1, w1, d1, rp, ru, rw, ilp, ilu);
+}
+
+template <typename T>
+int set_smem_limits() {
+  static bool done = false;
+  if (!done) {
+    ADFWI_CUDA_TRY(cudaFuncSetAttribute(ac::fwd_step<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)sizeof(ac::FwdSmem<T>)));
+    ADFWI_CUDA_TRY(cudaFuncSetAttribute(ac::adj_step<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)sizeof(ac::AdjSmem<T>)));
+    done = true;
+  }
+  return kOk;
+}
+
+template <typename T>
+int forward_impl(const adfwi_acoustic_plan* p, const void* alpha1, const void* alpha2, const void* damp,
+                 const void* wavelet, void* rec_p, void* rec_u, void* rec_w, void* fw_p, void* fw_u,
+                 void* fw_w, bool grad, unsigned char* ws, int64_t ws_bytes, cudaStream_t st) {
+  int rc = set_smem_limits<T>();
+  if (rc) return rc;
+  const int K = grad ? p->K : 1;
+  Carve c = carve(p, grad, K);
+  if (ws_bytes < c.total) {
+    set_error("workspace too small: %lld bytes given, %lld needed", (long long)ws_bytes, (long long)c.total);
+    return kWorkspaceTooSmall;
+  }
+  rc = setup_common<T>(p, ws, c, alpha1, alpha2, damp, st);
+  if (rc) return rc;
+  ac::Geo<T> g = make_geo<T>(p, ws, c);
+  const int64_t pl = p->L.plane;
+  const int64_t ns = p->d.ns;
+  const T* cf = reinterpret_cast<const T*>(ws + c.coef);
+  T* fa = reinterpret_cast<T*>(ws + c.fa);
+  T* fb = reinterpret_cast<T*>(ws + c.fb);
+  T* ilp = reinterpret_cast<T*>(ws + c.ilp);
+  T* ilu = reinterpret_cast<T*>(ws + c.ilu);
+  const T* wav = static_cast<const T*>(wavelet);
+  const bool full = grad && K >= p->d.nt;
+  T* hp = grad ? reinterpret_cast<T*>(ws + c.hp) : nullptr;
+  T* hd = grad ? reinterpret_cast<T*>(ws + c.hd) : nullptr;
+  T* cur = fa;
+  T* nxt = fb;
+  for (int it = 0; it < p->d.nt; ++it) {
+    if (grad && !full && it % K == 0) {
+      int rc2 = snapshot_store<T>(p->d.snapshot_precision, cur, 3 * ns, pl, ws + c.snap, ws + c.snap_scale,
+                                  (int64_t)(it / K) * 3 * ns, st);
+      if (rc2) return rc2;
+    }
+    const T* p0 = cur;
+    T* p1 = nxt;
+    T* d1 = nullptr;
+    if (full) {
+      p0 = it == 0 ? cur : hp + (int64_t)(it - 1) * ns * pl;
+      p1 = hp + (int64_t)it * ns * pl;
+      d1 = hd + (int64_t)it * ns * pl;
+    }
+    launch_fwd<T>(p, g, it, it >= p->last_chunk_start ? 1 : 0, cf, wav, p0, cur + ns * pl, cur + 2 * ns * pl, p1,
+                  nxt + ns * pl, nxt + 2 * ns * pl, d1, static_cast<T*>(rec_p), static_cast<T*>(rec_u),
+                  static_cast<T*>(rec_w), ilp, ilu, st);
+    std::swap(cur, nxt);
+  }
+  ADFWI_CUDA_TRY(cudaGetLastError());
+  if (fw_p || fw_u || fw_w) {
+    const int64_t n = (int64_t)p->d.nz * p->d.nx;
+    ac::illum_finalize<T><<<grid_blocks(n), 256, 0, st>>>(p->L, p->ngroups, p->d.ns, p->d.nabc, p->d.nz, p->d.nx,
+                                                          ilp, ilu, cur + 2 * ns * pl, static_cast<T*>(fw_p),
+                                                          static_cast<T*>(fw_u), static_cast<T*>(fw_w));
+    ADFWI_CUDA_TRY(cudaGetLastError());
+  }
+  return kOk;
+}
+
+template <typename T>
+int backward_impl(const adfwi_acoustic_plan* p, const void* wavelet, const void* grp, const void* gru,
+                  const void* grw, void* ga1, void* ga2, unsigned char* ws, int64_t ws_bytes, cudaStream_t st) {
+  int rc = set_smem_limits<T>();
+  if (rc) return rc;
+  const int K = p->K;
+  Carve c = carve(p, true, K);
+  if (ws_bytes < c.total) {
+    set_error("workspace too small: %lld bytes given, %lld needed", (long long)ws_bytes, (long long)c.total);
+    return kWorkspaceTooSmall;
+  }
+  ac::Geo<T> g = make_geo<T>(p, ws, c);
+  const int64_t pl = p->L.plane;
+  const int64_t ns = p->d.ns;
+  const int nt = p->d.nt;
+  const bool full = K >= nt;
+  const T* cf = reinterpret_cast<const T*>(ws + c.coef);
+  T* fa = reinterpret_cast<T*>(ws + c.fa);
+  T* fb = reinterpret_cast<T*>(ws + c.fb);
+  T* hp = reinterpret_cast<T*>(ws + c.hp);
+  T* hd = reinterpret_cast<T*>(ws + c.hd);
+  T* la = reinterpret_cast<T*>(ws + c.la);
+  T* lb = reinterpret_cast<T*>(ws + c.lb);
+  T* g1 = reinterpret_cast<T*>(ws + c.g1);
+  T* g2 = reinterpret_cast<T*>(ws + c.g2);
+  const T* wav = static_cast<const T*>(wavelet);
+  const T* gp = static_cast<const T*>(grp);
+  const T* gu = static_cast<const T*>(gru);
+  const T* gw = static_cast<const T*>(grw);
+
+  ADFWI_CUDA_TRY(cudaMemsetAsync(la, 0, 3 * ns * pl * sizeof(T), st));
+  ADFWI_CUDA_TRY(cudaMemsetAsync(lb, 0, 3 * ns * pl * sizeof(T), st));
+  ADFWI_CUDA_TRY(cudaMemsetAsync(g1, 0, (size_t)p->ngroups * pl * sizeof(T), st));
+  ADFWI_CUDA_TRY(cudaMemsetAsync(g2, 0, (size_t)p->ngroups * pl * sizeof(T), st));
+  if (gp || gu || gw) {
+    dim3 sg(std::max(1, std::min(64, (p->ncells + 127) / 128)), p->d.ns);
+    ac::adj_seed<T><<<sg, 128, 0, st>>>(g, p->ntiles, gp, gu, gw, la, la + ns * pl, la + 2 * ns * pl);
+  }
+  T* lcur = la;
+  T* lnxt = lb;
+  const int nseg = full ? 1 : (nt + K - 1) / K;
+  dim3 grid(p->tiles_x, p->tiles_z, p->ngroups);
+  dim3 block(ac::TX, ac::BY);
+  for (int seg = nseg - 1; seg >= 0; --seg) {
+    const int t0 = full ? 0 : seg * K;
+    const int t1 = full ? nt : std::min(nt, t0 + K);
+    if (!full) {
+      // Recompute the segment from its snapshot, keeping p and the divergence of every step.
+      int rc2 = snapshot_load<T>(p->d.snapshot_precision, fa, 3 * ns, pl, ws + c.snap, ws + c.snap_scale,
+                                 (int64_t)seg * 3 * ns, st);
+      if (rc2) return rc2;
+      T* cur = fa;
+      T* nxt = fb;
+      for (int it = t0; it < t1; ++it) {
+        const T* p0 = it == t0 ? fa : hp + (int64_t)(it - 1 - t0) * ns * pl;
+        launch_fwd<T>(p, g, it, 0, cf, wav, p0, cur + ns * pl, cur + 2 * ns * pl, hp + (int64_t)(it - t0) * ns * pl,
+                      nxt + ns * pl, nxt + 2 * ns * pl, hd + (int64_t)(it - t0) * ns * pl, nullptr, nullptr,
+                      nullptr, nullptr, nullptr, st);
+        std::swap(cur, nxt);
+      }
+    }
+    for (int it = t1 - 1; it >= t0; --it) {
+      ac::adj_step<T><<<grid, block, sizeof(ac::AdjSmem<T>), st>>>(
+          g, it, p->G, cf, cf + pl, cf + 2 * pl, lcur, lcur + ns * pl, lcur + 2 * ns * pl, lnxt, lnxt + ns * pl,
+          lnxt + 2 * ns * pl, hp + (int64_t)(it - t0) * ns * pl, hd + (int64_t)(it - t0) * ns * pl, gp, gu, gw, g1,
+          g2);
+      std::swap(lcur, lnxt);
+    }
+    ADFWI_CUDA_TRY(cudaGetLastError());
+  }
+  const int64_t n = (int64_t)p->nzp * p->nxp;
+  ac::reduce_planes<T><<<grid_blocks(n), 256, 0, st>>>(p->L, p->ngroups, 0, 0, p->nzp, p->nxp, g1,
+                                                       static_cast<T*>(ga1));
+  ac::reduce_planes<T><<<grid_blocks(n), 256, 0, st>>>(p->L, p->ngroups, 0, 0, p->nzp, p->nxp, g2,
+                                                       static_cast<T*>(ga2));
+  ADFWI_CUDA_TRY(cudaGetLastError());
+  return kOk;
+}
+
+}  // namespace
+
+extern "C" {
+
+int adfwi_acoustic_plan_create(const adfwi_acoustic_desc* desc, const int32_t* src_z, const int32_t* src_x,
+                               const int32_t* rcv_z, const int32_t* rcv_x, adfwi_acoustic_plan** out) {
+  ADFWI_CHECK_ARG(desc && out, "null descriptor or output pointer");
+  *out = nullptr;
+  const adfwi_acoustic_desc& d = *desc;
+  ADFWI_CHECK_ARG(d.nz >= 1 && d.nx >= 1 && d.nabc >= 2, "need nz, nx >= 1 and nabc >= 2");
+  ADFWI_CHECK_ARG(d.ns >= 1 && d.nt >= 1 && d.nr >= 0, "need ns >= 1, nt >= 1, nr >= 0");
+  ADFWI_CHECK_ARG(d.dtype == ADFWI_F32 || d.dtype == ADFWI_F64, "dtype must be ADFWI_F32 or ADFWI_F64");
+  ADFWI_CHECK_ARG(d.snapshot_precision >= 0 && d.snapshot_precision <= 2, "bad snapshot_precision");
+  ADFWI_CHECK_ARG(d.checkpoint_segments >= 1, "checkpoint_segments must be >= 1");
+  ADFWI_CHECK_ARG(src_z && src_x && (d.nr == 0 || (rcv_z && rcv_x)), "null geometry array");
+  adfwi_acoustic_plan* p = new (std::nothrow) adfwi_acoustic_plan();
+  if (!p) {
+    set_error("host allocation failed");
+    return kBadArgument;
+  }
+  p->d = d;
+  p->nzp = d.nz + 2 * d.nabc;
+  p->nxp = d.nx + 2 * d.nabc;
+  p->fs = d.free_surface ? d.nabc : 1;
+  p->zbeg = d.free_surface ? p->fs - 1 : 0;
+  p->elem = d.dtype == ADFWI_F64 ? 8 : 4;
+  p->L = make_layout(p->nzp, p->nxp, ac::TZ, ac::TX, p->elem);
+  p->tiles_x = (p->nxp + ac::TX - 1) / ac::TX;
+  p->tiles_z = (p->nzp - p->zbeg + ac::TZ - 1) / ac::TZ;
+  p->ntiles = p->tiles_x * p->tiles_z;
+  // torch.chunk(wavelet, checkpoint_segments): chunks of ceil(nt / segments) steps.
+  const int chunk = (d.nt + d.checkpoint_segments - 1) / d.checkpoint_segments;
+  const int nchunks = (d.nt + chunk - 1) / chunk;
+  p->last_chunk_start = (nchunks - 1) * chunk;
+  // Shots per block: enough blocks to fill the GPU (about 8 resident per SM).
+  int G = d.shots_per_block;
+  if (G <= 0) {
+    const int want_groups = std::max(1, (152 * 8 + p->ntiles - 1) / p->ntiles);
+    const int groups = std::min(d.ns, want_groups);
+    G = (d.ns + groups - 1) / groups;
+  }
+  p->G = std::max(1, std::min(G, d.ns));
+  p->ngroups = (d.ns + p->G - 1) / p->G;
+
+  // Geometry tables.
+  std::vector<int32_t>& t = p->tab;
+  p->o_srcz = t.size();
+  for (int s = 0; s < d.ns; ++s) {
+    int z = src_z[s] + d.nabc, x = src_x[s] + d.nabc;
+    if (z < p->zbeg || z >= p->nzp || x < 0 || x >= p->nxp) {
+      set_error("source %d at (z=%d, x=%d) lies outside the model", s, src_z[s], src_x[s]);
+      delete p;
+      return kBadGeometry;
+    }
+    t.push_back(z);
+  }
+  p->o_srcx = t.size();
+  for (int s = 0; s < d.ns; ++s) t.push_back(src_x[s] + d.nabc);
+  struct R { int tile, cell, id; };
+  std::vector<R> rs(d.nr);
+  for (int r = 0; r < d.nr; ++r) {
+    int z = rcv_z[r] + d.nabc, x = rcv_x[r] + d.nabc;
+    // u has nxp-1 columns and w has nzp-1 rows (acoustic_kernels.py:241-242, 167-169)
+    if (z < p->zbeg || z > p->nzp - 2 || x < 0 || x > p->nxp - 2) {
+      set_error("receiver %d at (z=%d, x=%d) lies outside the recordable model", r, rcv_z[r], rcv_x[r]);
+      delete p;
+      return kBadGeometry;
+    }
+    int lz = z - p->zbeg;
+    rs[r].tile = (lz / ac::TZ) * p->tiles_x + x / ac::TX;
+    rs[r].cell = ((lz % ac::TZ) << 16) | (x % ac::TX);
+    rs[r].id = r;
+  }
+  std::stable_sort(rs.begin(), rs.end(), [](const R& a, const R& b) {
+    return a.tile != b.tile ? a.tile < b.tile : a.cell < b.cell;
+  });
+  p->o_trb = t.size();
+  {
+    std::vector<int32_t> beg(p->ntiles + 1, 0);
+    for (const R& r : rs) beg[r.tile + 1]++;
+    for (int q = 0; q < p->ntiles; ++q) beg[q + 1] += beg[q];
+    t.insert(t.end(), beg.begin(), beg.end());
+  }
+  p->o_trc = t.size();
+  for (const R& r : rs) t.push_back(r.cell);
+  p->o_tri = t.size();
+  for (const R& r : rs) t.push_back(r.id);
+  // unique cells per tile
+  std::vector<int32_t> tcb(p->ntiles + 1, 0), tcc, tcr, cr;
+  for (size_t q = 0; q < rs.size(); ++q) {
+    bool fresh = q == 0 || rs[q].tile != rs[q - 1].tile || rs[q].cell != rs[q - 1].cell;
+    if (fresh) {
+      tcb[rs[q].tile + 1]++;
+      tcc.push_back(rs[q].cell);
+      tcr.push_back((int32_t)cr.size());
+    }
+    cr.push_back(rs[q].id);
+  }
+  tcr.push_back((int32_t)cr.size());
+  for (int q = 0; q < p->ntiles; ++q) tcb[q + 1] += tcb[q];
+  p->ncells = (int)tcc.size();
+  p->o_tcb = t.size();
+  t.insert(t.end(), tcb.begin(), tcb.end());
+  p->o_tcc = t.size();
+  t.insert(t.end(), tcc.begin(), tcc.end());
+  p->o_tcr = t.size();
+  t.insert(t.end(), tcr.begin(), tcr.end());
+  p->o_cr = t.size();
+  t.insert(t.end(), cr.begin(), cr.end());
+  if (t.empty()) t.push_back(0);
+
+  p->K = choose_K(p);
+  p->nseg = (d.nt + p->K - 1) / p->K;
+  *out = p;
+  return kOk;
+}
+
+void adfwi_acoustic_plan_destroy(adfwi_acoustic_plan* plan) { delete plan; }
+
+int adfwi_acoustic_workspace_bytes(const adfwi_acoustic_plan* p, int32_t with_gradient, int64_t* bytes) {
+  ADFWI_CHECK_ARG(p && bytes, "null plan or output pointer");
+  *bytes = carve(p, with_gradient != 0, with_gradient ? p->K : 1).total;
+  return kOk;
+}
+
+int adfwi_acoustic_snapshot_every(const adfwi_acoustic_plan* p, int32_t* steps) {
+  ADFWI_CHECK_ARG(p && steps, "null plan or output pointer");
+  *steps = p->K;
+  return kOk;
+}
+
+int adfwi_acoustic_forward(const adfwi_acoustic_plan* p, const void* alpha1, const void* alpha2, const void* damp,
+                           const void* wavelet, void* rec_p, void* rec_u, void* rec_w, void* fw_p, void* fw_u,
+                           void* fw_w, int32_t with_gradient, void* workspace, int64_t workspace_bytes,
+                           void* stream) {
+  ADFWI_CHECK_ARG(p && alpha1 && alpha2 && damp && wavelet && workspace, "null argument");
+  ADFWI_CHECK_ARG((rec_p && rec_u && rec_w) || (!rec_p && !rec_u && !rec_w), "records: give all three or none");
+  ADFWI_CHECK_ARG(p->d.nr > 0 || rec_p == nullptr, "records requested without receivers");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  unsigned char* ws = static_cast<unsigned char*>(workspace);
+  if (p->d.dtype == ADFWI_F64)
+    return forward_impl<double>(p, alpha1, alpha2, damp, wavelet, rec_p, rec_u, rec_w, fw_p, fw_u, fw_w,
+                                with_gradient != 0, ws, workspace_bytes, st);
+  return forward_impl<float>(p, alpha1, alpha2, damp, wavelet, rec_p, rec_u, rec_w, fw_p, fw_u, fw_w,
+                             with_gradient != 0, ws, workspace_bytes, st);
+}
+
+int adfwi_acoustic_backward(const adfwi_acoustic_plan* p, const void* alpha1, const void* alpha2, const void* damp,
+                            const void* wavelet, const void* grad_rec_p, const void* grad_rec_u,
+                            const void* grad_rec_w, void* grad_alpha1, void* grad_alpha2, void* workspace,
+                            int64_t workspace_bytes, void* stream) {
+  ADFWI_CHECK_ARG(p && alpha1 && alpha2 && damp && wavelet && workspace && grad_alpha1 && grad_alpha2,
+                  "null argument");
+  (void)alpha1;
+  (void)alpha2;
+  (void)damp;  // the coefficient planes staged by the forward call are reused from the workspace
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  unsigned char* ws = static_cast<unsigned char*>(workspace);
+  if (p->d.dtype == ADFWI_F64)
+    return backward_impl<double>(p, wavelet, grad_rec_p, grad_rec_u, grad_rec_w, grad_alpha1, grad_alpha2, ws,
+                                 workspace_bytes, st);
+  return backward_impl<float>(p, wavelet, grad_rec_p, grad_rec_u, grad_rec_w, grad_alpha1, grad_alpha2, ws,
+                              workspace_bytes, st);
+}
+
+}  // extern "C"

@@ -1,0 +1,79 @@
+// Shared definitions for the adfwi_gb300 CUDA library (sm_103a).
+//
+// Storage layout of one wavefield / coefficient plane (nzp x nxp cells):
+// rows are padded to a 128-byte multiple pitch and surrounded by ghost cells
+// that are zero forever, so that every stencil read of a tile and its halo stays
+// inside the allocation without a bounds check:
+//
+//     element (i, j) of a plane lives at  (i + GZ) * pitch + (j + GX)
+//
+// with GZ = 4 ghost rows on top, GX = 4 ghost columns on the left, and at least
+// TILE + 4 ghost rows / columns at the bottom / right. A shot's fields are
+// consecutive planes; all shots of one field form one block of ns planes.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stddef.h>
+
+namespace adfwi {
+
+constexpr int GZ = 4;
+constexpr int GX = 4;
+
+struct Layout {
+  int nzp, nxp;    // grid cells (rows, columns)
+  int rows;        // allocated rows per plane
+  int pitch;       // allocated elements per row
+  int64_t plane;   // rows * pitch
+
+  __host__ __device__ __forceinline__ int64_t off(int i, int j) const {
+    return (int64_t)(i + GZ) * pitch + (j + GX);
+  }
+};
+
+// Host: layout for a grid processed by tiles of tz x tx cells.
+inline Layout make_layout(int nzp, int nxp, int tz, int tx, int elem_bytes) {
+  Layout L;
+  L.nzp = nzp;
+  L.nxp = nxp;
+  L.rows = GZ + nzp + tz + 4;
+  int align = 128 / elem_bytes;
+  int need = GX + nxp + tx + 4;
+  L.pitch = (need + align - 1) / align * align;
+  L.plane = (int64_t)L.rows * L.pitch;
+  return L;
+}
+
+// Status codes returned by every C-ABI entry point (0 = success).
+enum Status : int {
+  kOk = 0,
+  kBadArgument = -1,
+  kBadGeometry = -2,
+  kWorkspaceTooSmall = -3,
+  kCudaError = -4,
+  kUnsupported = -5,
+  kNonFinite = -6,
+};
+
+// Thread-local last-error text, read through adfwi_last_error().
+void set_error(const char* fmt, ...);
+
+}  // namespace adfwi
+
+#define ADFWI_CUDA_TRY(expr)                                                      \
+  do {                                                                            \
+    cudaError_t e__ = (expr);                                                     \
+    if (e__ != cudaSuccess) {                                                     \
+      ::adfwi::set_error("%s failed: %s (%s:%d)", #expr, cudaGetErrorString(e__), \
+                         __FILE__, __LINE__);                                     \
+      return ::adfwi::kCudaError;                                                 \
+    }                                                                             \
+  } while (0)
+
+#define ADFWI_CHECK_ARG(cond, ...)         \
+  do {                                     \
+    if (!(cond)) {                         \
+      ::adfwi::set_error(__VA_ARGS__);     \
+      return ::adfwi::kBadArgument;        \
+    }                                      \
+  } while (0)

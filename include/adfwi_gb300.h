@@ -1,0 +1,117 @@
+/*
+ * adfwi_gb300 -- C ABI of the GB300 (sm_103a) propagator hot path of ADFWI.
+ *
+ * Every entry point is stream-ordered on the caller's CUDA stream, allocates no
+ * device memory (the caller passes a workspace whose size the library reports),
+ * returns 0 on success or a negative status, and records a message retrievable
+ * with adfwi_last_error(). Device arrays are dense row-major; `dtype` selects
+ * float32 or float64 for every floating-point array of a call.
+ *
+ * Reference interfaces replaced (paths inside liufeng2317/ADFWI):
+ *   acoustic: ADFWI/propagator/acoustic_kernels.py:179 forward_kernel(...) as called from
+ *             ADFWI/propagator/acoustic_propagator.py:147-156, plus the autograd backward
+ *             through torch.utils.checkpoint at acoustic_kernels.py:268-278;
+ *   elastic:  ADFWI/propagator/elastic_kernels.py:917 forward_kernel(...) as called from
+ *             ADFWI/propagator/elastic_propagator.py:132-141, plus its autograd backward
+ *             (elastic_kernels.py:975-1008).
+ */
+#ifndef ADFWI_GB300_H
+#define ADFWI_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ADFWI_F32 0
+#define ADFWI_F64 1
+
+/* Storage of the checkpoint snapshots kept for the gradient (stencils stay in dtype). */
+#define ADFWI_SNAP_NATIVE 0 /* same type as the wavefields */
+#define ADFWI_SNAP_BF16 1   /* bfloat16 with one max-abs scale per snapshot, shot and field */
+#define ADFWI_SNAP_FP16 2   /* float16 with one max-abs scale per snapshot, shot and field */
+
+/* Status codes. */
+#define ADFWI_OK 0
+#define ADFWI_ERR_ARGUMENT (-1)
+#define ADFWI_ERR_GEOMETRY (-2)
+#define ADFWI_ERR_WORKSPACE (-3)
+#define ADFWI_ERR_CUDA (-4)
+#define ADFWI_ERR_UNSUPPORTED (-5)
+
+/* ------------------------------------------------------------------------- */
+/* Acoustic (p, u, w) 4th-order staggered grid with PML damping.              */
+/* ------------------------------------------------------------------------- */
+
+typedef struct adfwi_acoustic_desc {
+  int32_t nz, nx;             /* model cells before padding                                  */
+  int32_t nabc;               /* absorbing cells on every side (grid = nz+2nabc x nx+2nabc)  */
+  int32_t free_surface;       /* 0 / 1                                                       */
+  int32_t ns;                 /* shots of this solve (one source each)                       */
+  int32_t nt;                 /* time steps                                                  */
+  int32_t nr;                 /* receivers, shared by all shots                              */
+  int32_t dtype;              /* ADFWI_F32 / ADFWI_F64                                       */
+  int32_t checkpoint_segments;/* reference chunk count; only shapes forward_wavefield_u/w    */
+  int32_t snapshot_every;     /* steps between snapshots for the gradient; 0 = automatic     */
+  int32_t snapshot_precision; /* ADFWI_SNAP_*                                                */
+  int32_t shots_per_block;    /* shots handled by one thread block; 0 = automatic            */
+  double dt;                  /* time step (s)                                               */
+  int64_t memory_budget;      /* byte cap for the gradient workspace; 0 = no cap             */
+} adfwi_acoustic_desc;
+
+typedef struct adfwi_acoustic_plan adfwi_acoustic_plan; /* opaque */
+
+/* Build a plan from the descriptor and HOST arrays of grid coordinates in model cells
+ * (before padding): src_z/src_x (ns), rcv_z/rcv_x (nr). Replaces the geometry handling of
+ * acoustic_propagator.py:84-99 and the "+nabc" index shift of acoustic_kernels.py:233-237. */
+int adfwi_acoustic_plan_create(const adfwi_acoustic_desc* desc, const int32_t* src_z,
+                               const int32_t* src_x, const int32_t* rcv_z,
+                               const int32_t* rcv_x, adfwi_acoustic_plan** plan);
+void adfwi_acoustic_plan_destroy(adfwi_acoustic_plan* plan);
+
+/* Workspace bytes for a forward solve (with_gradient = 0) or for a forward solve that keeps
+ * what adfwi_acoustic_backward needs (with_gradient = 1). Used for HBM-budget admission. */
+int adfwi_acoustic_workspace_bytes(const adfwi_acoustic_plan* plan, int32_t with_gradient,
+                                   int64_t* bytes);
+
+/* Segment length (steps between snapshots) the plan uses in gradient mode. */
+int adfwi_acoustic_snapshot_every(const adfwi_acoustic_plan* plan, int32_t* steps);
+
+/* Forward solve: replaces forward_kernel (acoustic_kernels.py:179-301).
+ *   alpha1 = rho c^2 dt/dz, alpha2 = dt/(rho dz), damp: (nz+2nabc, nx+2nabc)
+ *   wavelet: (ns, nt); rec_p/u/w: (ns, nt, nr) outputs;
+ *   fw_p/u/w: (nz, nx) outputs (forward_wavefield_* of the reference, with its
+ *   accumulation order), any of them may be NULL.
+ * With with_gradient = 1 the workspace keeps the snapshots for adjoint_acoustic_backward. */
+int adfwi_acoustic_forward(const adfwi_acoustic_plan* plan, const void* alpha1, const void* alpha2,
+                           const void* damp, const void* wavelet, void* rec_p, void* rec_u,
+                           void* rec_w, void* fw_p, void* fw_u, void* fw_w, int32_t with_gradient,
+                           void* workspace, int64_t workspace_bytes, void* stream);
+
+/* Adjoint (reverse-time) solve after a with_gradient forward on the same workspace and the
+ * same coefficients: replaces the autograd backward through acoustic_kernels.py:268-278.
+ * grad_rec_*: dL/d rec_* (ns, nt, nr), NULL means zero. Outputs dL/d alpha1 and
+ * dL/d alpha2 (nz+2nabc, nx+2nabc), overwritten. */
+int adfwi_acoustic_backward(const adfwi_acoustic_plan* plan, const void* alpha1,
+                            const void* alpha2, const void* damp, const void* wavelet,
+                            const void* grad_rec_p, const void* grad_rec_u,
+                            const void* grad_rec_w, void* grad_alpha1, void* grad_alpha2,
+                            void* workspace, int64_t workspace_bytes, void* stream);
+
+/* ------------------------------------------------------------------------- */
+/* Errors and build information.                                             */
+/* ------------------------------------------------------------------------- */
+
+/* Copy the calling thread's last error message into buf (NUL-terminated); returns its length. */
+int adfwi_last_error(char* buf, size_t n);
+
+/* Library version string. */
+const char* adfwi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ADFWI_GB300_H */

@@ -1,0 +1,141 @@
+"""Acoustic CUDA path vs the CPU oracle and the reference's golden vectors (GPU tests).
+
+Tolerances: records within 1e-5 relative L2 in float32 (the kernel keeps the reference's
+operation order without FMA contraction, so they are usually bit-identical), gradients
+within 1e-4 relative L2 of the oracle's autograd gradient in float32 and 1e-9 in float64,
+and within 1e-6 of centred finite differences of the float64 scheme.
+"""
+import numpy as np
+import pytest
+import torch
+
+import adfwi_gb300 as A
+from _cases import acoustic_problem, golden_files, oracle_acoustic, rel
+
+pytestmark = pytest.mark.gpu
+
+KEYS = ("p", "u", "w", "forward_wavefield_p", "forward_wavefield_u", "forward_wavefield_w")
+
+
+@pytest.mark.parametrize("free_surface", [False, True])
+@pytest.mark.parametrize("segments", [1, 3])
+def test_forward_matches_oracle_f32(free_surface, segments):
+    model, survey, prop = acoustic_problem(A, free_surface=free_surface, seed=1 + segments)
+    rec = prop.forward(checkpoint_segments=segments)
+    ref, _, _ = oracle_acoustic(prop, model, segments=segments, requires_grad=False)
+    for k in KEYS:
+        assert rel(rec[k], ref[k]) <= 1e-5, (k, rel(rec[k], ref[k]))
+    for k in ("p", "u", "w"):
+        assert torch.equal(rec[k].cpu(), ref[k]), k  # same operation order: bit-identical records
+
+
+def test_forward_matches_oracle_f64_subset():
+    model, survey, prop = acoustic_problem(A, dtype=torch.float64, ns=4, seed=7)
+    rec = prop.forward(shot_index=[3, 1])
+    ref, _, _ = oracle_acoustic(prop, model, shot_index=[3, 1], requires_grad=False)
+    for k in KEYS:
+        assert rel(rec[k], ref[k]) <= 1e-13, k
+
+
+@pytest.mark.parametrize("path", golden_files("acoustic"), ids=lambda p: p.split("/")[-1])
+def test_forward_and_gradient_match_reference_golden(path):
+    g = np.load(path)
+    dt_ = torch.float64 if str(g["dtype"]) == "f64" else torch.float32
+    nz, nx, nabc = int(g["nz"]), int(g["nx"]), int(g["nabc"])
+    model = A.AcousticModel(0, 0, nx, nz, float(g["dx"]), float(g["dx"]), vp=g["vp_in"], rho=g["rho_in"],
+                            vp_grad=True, rho_grad=True, free_surface=bool(g["free_surface"]), nabc=nabc,
+                            device="cuda:0", dtype=dt_)
+    src = A.Source(nt=int(g["nt"]), dt=float(g["dt"]), f0=float(g["f0"]))
+    _, wav = A.wavelet(int(g["nt"]), float(g["dt"]), float(g["f0"]))
+    src.add_sources(src_x=g["src_x"], src_z=g["src_z"], src_wavelet=wav)
+    rcv = A.Receiver(nt=int(g["nt"]), dt=float(g["dt"]))
+    rcv.add_receivers(rcv_x=g["rcv_x"], rcv_z=g["rcv_z"], rcv_type="pr")
+    prop = A.AcousticPropagator(model, A.Survey(src, rcv), device="cuda:0", dtype=dt_)
+    assert np.array_equal(prop.damp.cpu().numpy(), g["damp"])
+    rec = prop.forward(checkpoint_segments=int(g["segments"]))
+    for k in KEYS:
+        assert rel(rec[k], g["rec_" + k]) <= 1e-5, k
+    loss = sum((rec[k] * torch.tensor(g["w_" + k], dtype=dt_, device="cuda:0")).sum() for k in "puw")
+    loss.backward()
+    tol = 1e-9 if dt_ == torch.float64 else 1e-4
+    assert rel(model.vp.grad, g["grad_vp"]) <= tol
+    assert rel(model.rho.grad, g["grad_rho"]) <= tol
+
+
+def _grad_case(dtype, free_surface, snapshot_every, seed, precision="native"):
+    model, survey, prop = acoustic_problem(A, dtype=dtype, free_surface=free_surface, seed=seed,
+                                           snapshot_every=snapshot_every, snapshot_precision=precision)
+    rec = prop.forward()
+    gen = torch.Generator().manual_seed(seed)
+    w = {k: torch.randn(rec[k].shape, generator=gen, dtype=dtype) for k in "puw"}
+    loss = sum((rec[k] * w[k].cuda()).sum() for k in "puw")
+    loss.backward()
+    ref, vp, rho = oracle_acoustic(prop, model)
+    sum((ref[k] * w[k]).sum() for k in "puw").backward()
+    return model, prop, vp, rho
+
+
+@pytest.mark.parametrize("free_surface", [False, True])
+@pytest.mark.parametrize("snapshot_every", [0, 37, 250])
+def test_gradient_matches_oracle_f32(free_surface, snapshot_every):
+    model, prop, vp, rho = _grad_case(torch.float32, free_surface, snapshot_every, seed=11)
+    assert rel(model.vp.grad, vp.grad) <= 1e-4
+    assert rel(model.rho.grad, rho.grad) <= 1e-4
+
+
+@pytest.mark.parametrize("free_surface", [False, True])
+def test_gradient_matches_oracle_f64(free_surface):
+    model, prop, vp, rho = _grad_case(torch.float64, free_surface, 23, seed=12)
+    assert rel(model.vp.grad, vp.grad) <= 1e-9
+    assert rel(model.rho.grad, rho.grad) <= 1e-9
+
+
+@pytest.mark.parametrize("precision", ["bf16", "fp16"])
+def test_low_precision_snapshots_stay_close(precision):
+    m0, _, vp, _ = _grad_case(torch.float32, False, 25, seed=13)
+    m1, _, _, _ = _grad_case(torch.float32, False, 25, seed=13, precision=precision)
+    err = rel(m1.vp.grad, m0.vp.grad)
+    assert err <= (3e-2 if precision == "bf16" else 3e-3), err
+
+
+def test_gradient_matches_centred_finite_differences_f64():
+    """dL/d(alpha1, alpha2) from the adjoint vs centred differences of the float64 scheme."""
+    from adfwi_gb300.acoustic import AcousticSolve
+    model, survey, prop = acoustic_problem(A, dtype=torch.float64, nz=24, nx=30, nabc=8, nt=160, ns=2, nr=10,
+                                           seed=21, snapshot_every=20)
+    model.forward()
+    a1, a2 = (t.detach().clone().requires_grad_(True) for t in prop.coefficients(model))
+    _, plan = prop.plan()
+    gen = torch.Generator().manual_seed(5)
+    w = [torch.randn((2, 160, 10), generator=gen, dtype=torch.float64).cuda() for _ in range(3)]
+
+    def loss(x1, x2):
+        out = AcousticSolve.apply(x1, x2, prop.damp, prop.wavelet, plan)
+        return sum((o * wi).sum() for o, wi in zip(out[:3], w))
+
+    loss(a1, a2).backward()
+    d1 = a1.detach() * torch.randn(a1.shape, generator=gen, dtype=torch.float64).cuda()
+    d2 = a2.detach() * torch.randn(a2.shape, generator=gen, dtype=torch.float64).cuda()
+    an = float((a1.grad * d1).sum() + (a2.grad * d2).sum())
+    eps = 1e-6
+    with torch.no_grad():
+        fd = (float(loss(a1 + eps * d1, a2 + eps * d2)) - float(loss(a1 - eps * d1, a2 - eps * d2))) / (2 * eps)
+    assert abs(fd - an) <= 1e-6 * abs(an), (fd, an)
+
+
+def test_repeated_backward_and_shot_batches_agree():
+    model, survey, prop = acoustic_problem(A, ns=4, seed=31, snapshot_every=40)
+    rec = prop.forward()
+    rec["p"].sum().backward()
+    g_all = model.vp.grad.clone()
+    model.vp.grad = None
+    for idx in ([0, 1], [2, 3]):
+        prop.forward(shot_index=idx)["p"].sum().backward()
+    assert rel(model.vp.grad, g_all) <= 1e-5
+
+
+def test_bad_geometry_is_rejected_on_the_host():
+    model, survey, prop = acoustic_problem(A, seed=3)
+    survey.source.loc_x[0] = 10 ** 6
+    with pytest.raises(Exception):
+        A.AcousticPropagator(model, survey, device="cuda:0").forward()

@@ -1,0 +1,165 @@
+"""Host-side logic on the CPU: boundary profiles, model maps, survey API, the C ABI library
+(loads, exports every declared symbol, builds plans and sizes workspaces without a GPU)."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+import torch
+
+import adfwi_gb300 as A
+from adfwi_gb300 import boundary as B
+from _cases import golden_files, rel
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.mark.parametrize("path", golden_files(), ids=lambda p: p.split("/")[-1])
+def test_boundary_profiles_match_reference(path):
+    g = np.load(path)
+    nz, nx, nabc, dx = int(g["nz"]), int(g["nx"]), int(g["nabc"]), float(g["dx"])
+    fs = bool(g["free_surface"])
+    cast = np.float64 if str(g["dtype"]) == "f64" else np.float32
+    if str(g["kind"]) == "acoustic":
+        d = B.bc_pml(nx, nz, dx, dx, nabc, g["vp"].max(), free_surface=False)
+        assert np.array_equal(d.astype(cast), g["damp"])
+        return
+    abc = str(g["abc_type"])
+    if abc == "PML":
+        bx, bz = B.bc_pml_xz(nx, nz, dx, dx, nabc, g["vp"].max(), free_surface=fs)
+        assert np.array_equal(bx.astype(cast), g["bcx"]) and np.array_equal(bz.astype(cast), g["bcz"])
+    elif abc == "gerjan":
+        assert np.array_equal(B.bc_gerjan(nx, nz, dx, dx, nabc, 0.0053, free_surface=fs).astype(cast), g["damp"])
+    else:
+        assert np.array_equal(B.bc_sincos(nx, nz, dx, dx, nabc, free_surface=fs).astype(cast), g["damp"])
+
+
+def test_pml_corner_rule_is_max_of_profiles():
+    d = B.bc_pml(30, 20, 10.0, 10.0, 8, 3000.0, free_surface=False)
+    pz, px = d[:, 8 + 15], d[8 + 10, :]
+    assert np.array_equal(np.maximum(pz[:, None], px[None, :]), d)
+
+
+@pytest.mark.parametrize("path", golden_files("elastic"), ids=lambda p: p.split("/")[-1])
+def test_elastic_model_maps_match_oracle(path):
+    from oracle.model import elastic_coefficients
+    g = np.load(path)
+    iso = bool(g["iso"])
+    nz, nx, dx = int(g["nz"]), int(g["nx"]), float(g["dx"])
+    if iso:
+        m = A.IsotropicElasticModel(0, 0, nx, nz, dx, dx, vp=g["vp"], vs=g["vs"], rho=g["rho"],
+                                    auto_update_rho=False)
+    else:
+        m = A.AnisotropicElasticModel(0, 0, nx, nz, dx, dx, vp=g["vp"], vs=g["vs"], rho=g["rho"], eps=g["eps"],
+                                      gamma=g["gamma"], delta=g["delta"])
+    m.forward()
+    z = lambda k: torch.tensor(g[k] * (0 if iso else 1), dtype=torch.float32)  # noqa: E731
+    co = elastic_coefficients(torch.tensor(g["vp"]), torch.tensor(g["vs"]), torch.tensor(g["rho"]),
+                              z("eps"), z("delta"), z("gamma"))
+    mine = {"C11": m.CC[0], "C13": m.CC[2], "C15": m.CC[4], "C33": m.CC[11], "C35": m.CC[13], "C55": m.CC[18],
+            "bx": m.bx, "bz": m.bz}
+    for k, v in co.items():
+        assert torch.equal(mine[k].detach(), v.detach()), k
+
+
+def test_acoustic_model_gardner_and_bounds():
+    vp = np.full((6, 7), 2000.0, dtype=np.float32)
+    vp[2, 3] = 3000.0
+    m = A.AcousticModel(0, 0, 7, 6, 5.0, 5.0, vp=vp, rho=np.ones_like(vp), vp_bound=(1500.0, 4000.0), vp_grad=True)
+    m.vp.data[0, 0] = 9000.0  # an update that leaves the bounds is clipped by forward()
+    m.forward()
+    assert float(m.vp.detach().max()) <= 4000.0 + 1e-3
+    assert np.allclose(m.rho.detach().numpy(), np.power(m.vp.detach().numpy(), 0.25) * 310)
+    assert m.get_bound("vp")[1] >= 4000.0
+    with pytest.raises(ValueError):
+        m.get_model("vs")
+    with pytest.raises(AssertionError):
+        A.AcousticModel(0, 0, 7, 6, 5.0, 6.0, vp=vp, rho=vp)
+
+
+def test_survey_and_seismic_data_roundtrip(tmp_path):
+    src = A.Source(nt=50, dt=1e-3, f0=10.0)
+    t, w = A.wavelet(50, 1e-3, 10.0)
+    src.add_sources(src_x=np.array([1, 5, 9]), src_z=np.array([2, 2, 2]), src_wavelet=w)
+    src.add_source(4, 3, w)
+    assert src.num == 4 and src.get_wavelet().shape == (4, 50) and src.get_moment_tensor().shape == (4, 3, 3)
+    assert np.array_equal(src.get_loc(), np.array([[1, 2], [5, 2], [9, 2], [4, 3]]))
+    with pytest.raises(ValueError):
+        src.add_source(1, 1, w[:10])
+    rcv = A.Receiver(nt=50, dt=1e-3)
+    rcv.add_receivers(rcv_x=np.arange(10), rcv_z=np.zeros(10, dtype=int), rcv_type="pr")
+    with pytest.raises(ValueError):
+        rcv.add_receiver(1, 1, "xx")
+    sv = A.Survey(src, rcv)
+    d = A.SeismicData(sv)
+    d.record_data({"p": torch.ones(4, 50, 10)})
+    d.save(str(tmp_path / "d.npz"))
+    e = A.SeismicData(sv)
+    e.load(str(tmp_path / "d.npz"))
+    assert np.array_equal(e.data["p"], np.ones((4, 50, 10)))
+
+
+@pytest.mark.parametrize("path", golden_files(), ids=lambda p: p.split("/")[-1])
+def test_wavelet_matches_reference(path):
+    g = np.load(path)
+    _, w = A.wavelet(int(g["nt"]), float(g["dt"]), float(g["f0"]))
+    cast = np.float64 if str(g["dtype"]) == "f64" else np.float32
+    assert np.array_equal(w.astype(cast), g["wavelet"][0])
+
+
+def _declared_symbols():
+    text = open(os.path.join(ROOT, "include", "adfwi_gb300.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(adfwi_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol(native_lib):
+    names = _declared_symbols()
+    assert "adfwi_acoustic_forward" in names
+    missing = [n for n in names if not hasattr(native_lib, n)]
+    assert not missing, missing
+    assert b"sm_103a" in native_lib.adfwi_version()
+
+
+def _plan(**kw):
+    from adfwi_gb300.acoustic import AcousticPlan
+    base = dict(nz=200, nx=600, nabc=50, free_surface=False, src_z=[2] * 30,
+                src_x=np.linspace(0, 599, 30).astype(int), rcv_z=[2] * 600, rcv_x=np.arange(600), nt=3000,
+                dt=1.5e-3, dtype=torch.float32)
+    base.update(kw)
+    return AcousticPlan(**base)
+
+
+def test_plan_workspace_sizing_and_budget(native_lib):
+    p = _plan()
+    fwd = p.workspace_bytes(False)
+    assert 0 < fwd < 1 << 30
+    full = _plan(memory_budget=1 << 40)
+    assert full.snapshot_every == 3000  # everything fits: no recomputation
+    tight = _plan(memory_budget=8 << 30)
+    assert 1 <= tight.snapshot_every < 3000
+    assert tight.workspace_bytes(True) <= 8 << 30
+    fixed = _plan(snapshot_every=50, snapshot_precision="bf16")
+    assert fixed.snapshot_every == 50
+    assert fixed.workspace_bytes(True) < _plan(snapshot_every=50).workspace_bytes(True)
+
+
+def test_plan_rejects_bad_geometry(native_lib):
+    with pytest.raises(RuntimeError, match="outside"):
+        _plan(src_z=[500] * 30)
+    with pytest.raises(RuntimeError, match="outside"):
+        _plan(rcv_x=np.arange(600) + 100)
+    with pytest.raises(ValueError):
+        _plan(snapshot_precision="int8")
+
+
+def test_propagator_refuses_cpu_device():
+    vp = np.full((10, 12), 2000.0, dtype=np.float32)
+    m = A.AcousticModel(0, 0, 12, 10, 5.0, 5.0, vp=vp, rho=vp, nabc=4)
+    src = A.Source(nt=10, dt=1e-3, f0=10.0)
+    src.add_source(3, 2, A.wavelet(10, 1e-3, 10.0)[1])
+    rcv = A.Receiver(nt=10, dt=1e-3)
+    rcv.add_receiver(4, 1, "pr")
+    with pytest.raises(RuntimeError, match="CUDA"):
+        A.AcousticPropagator(m, A.Survey(src, rcv), device="cpu")

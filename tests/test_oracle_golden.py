@@ -1,0 +1,65 @@
+"""The CPU oracle reproduces the reference's own outputs (golden fixtures made by
+tests/golden/make_golden.py from the reference code): records bit-exact, gradients of the
+fixture's linear functional within 1e-6 (float32) / 1e-12 (float64)."""
+import numpy as np
+import pytest
+import torch
+
+from _cases import golden_files, rel
+from oracle.acoustic import acoustic_forward
+from oracle.elastic import elastic_forward
+from oracle.model import elastic_coefficients
+
+
+@pytest.mark.parametrize("path", golden_files("acoustic"), ids=lambda p: p.split("/")[-1])
+def test_oracle_acoustic_matches_reference(path):
+    g = np.load(path)
+    dt_ = torch.float64 if str(g["dtype"]) == "f64" else torch.float32
+    vp = torch.tensor(g["vp"], dtype=dt_, requires_grad=True)
+    rho = torch.tensor(g["rho"], dtype=dt_, requires_grad=True)
+    out = acoustic_forward(vp, rho, torch.tensor(g["damp"]), g["src_x"], g["src_z"],
+                           torch.tensor(g["wavelet"], dtype=dt_), g["rcv_x"], g["rcv_z"],
+                           nabc=int(g["nabc"]), free_surface=bool(g["free_surface"]), dx=float(g["dx"]),
+                           dz=float(g["dx"]), dt=float(g["dt"]), checkpoint_segments=int(g["segments"]))
+    for k in out:
+        assert np.array_equal(out[k].detach().numpy(), g["rec_" + k]), k
+    loss = sum((out[k] * torch.tensor(g["w_" + k], dtype=dt_)).sum() for k in "puw")
+    loss.backward()
+    tol = 1e-12 if dt_ == torch.float64 else 1e-6
+    assert rel(vp.grad, g["grad_vp"]) < tol
+    assert rel(rho.grad, g["grad_rho"]) < tol
+
+
+@pytest.mark.parametrize("path", golden_files("elastic"), ids=lambda p: p.split("/")[-1])
+def test_oracle_elastic_matches_reference(path):
+    g = np.load(path)
+    dt_ = torch.float32
+    iso = bool(g["iso"])
+    pars = {}
+    for k in ("vp", "vs", "rho", "eps", "delta", "gamma"):
+        v = g[k] * (0 if iso and k in ("eps", "delta", "gamma") else 1)
+        pars[k] = torch.tensor(v, dtype=dt_, requires_grad=True)
+    co = elastic_coefficients(pars["vp"], pars["vs"], pars["rho"], pars["eps"], pars["delta"], pars["gamma"])
+    out = elastic_forward(co, g["src_x"], g["src_z"], torch.tensor(g["wavelet"], dtype=dt_), g["moment_tensor"],
+                          g["rcv_x"], g["rcv_z"], nabc=int(g["nabc"]), free_surface=bool(g["free_surface"]),
+                          dx=float(g["dx"]), dz=float(g["dx"]), dt=float(g["dt"]), fd_order=int(g["fd_order"]),
+                          abc_type=str(g["abc_type"]), bcx=g["bcx"] if "bcx" in g else None,
+                          bcz=g["bcz"] if "bcz" in g else None, damp=g["damp"] if "damp" in g else None,
+                          checkpoint_segments=int(g["segments"]))
+    for k in out:
+        assert np.array_equal(out[k].detach().numpy(), g["rec_" + k]), k
+    comps = ("txx", "tzz", "txz", "vx", "vz")
+    loss = sum((out[k] * torch.tensor(g["w_" + k], dtype=dt_)).sum() for k in comps)
+    loss.backward()
+    for p in ("vp", "vs", "rho", "eps", "delta"):
+        if "grad_" + p in g:
+            assert rel(pars[p].grad, g["grad_" + p]) < 1e-6, p
+
+
+def test_oracle_refuses_gpu_tensors():
+    from oracle.acoustic import _cpu_only
+    t = torch.zeros(2)
+    _cpu_only(t)
+    if torch.cuda.is_available():
+        with pytest.raises(RuntimeError):
+            _cpu_only(t.cuda())

@@ -104,6 +104,21 @@ int adfwi_acoustic_backward(const adfwi_acoustic_plan* plan, const void* alpha1,
 /* Errors and build information.                                             */
 /* ------------------------------------------------------------------------- */
 
+/* Launch accounting and per-kernel-class device time (used by the benchmark's roofline).
+ * adfwi_profile_start resets the session counters; with timed = 1 every launch of the library
+ * is bracketed by CUDA events on its stream until adfwi_profile_stop, which waits for the
+ * events and fills up to max_out entries (one per kernel class that launched). */
+typedef struct adfwi_kernel_stat {
+  char name[32];
+  int64_t launches;
+  int64_t timed_launches;
+  double total_ms;
+} adfwi_kernel_stat;
+int adfwi_profile_start(int32_t timed);
+int adfwi_profile_stop(adfwi_kernel_stat* out, int32_t max_out, int32_t* n_out);
+/* Cumulative number of kernel launches issued by this library in this process. */
+int64_t adfwi_launch_count(void);
+
 /* Copy the calling thread's last error message into buf (NUL-terminated); returns its length. */
 int adfwi_last_error(char* buf, size_t n);
 

@@ -3,8 +3,8 @@
 Follows ``ADFWI/propagator/acoustic_kernels.py`` of the reference:
 
 * ``pad_edge``            <- ``pad_torchSingle`` (lines 16-37): edge-replicate pad;
-* ``_coefficients``       <- ``forward_kernel`` lines 252-265 (alpha1, kappa1,
-  alpha2, kappa2, kappa3, c1 = 9/8, c2 = -1/24);
+* ``acoustic_forward_coef`` <- ``forward_kernel`` lines 252-265 (kappa1, kappa2, kappa3,
+  c1 = 9/8, c2 = -1/24) and the loop of lines 239-301 given alpha1, alpha2;
 * ``_step``               <- ``step_forward`` lines 113-174 (p update, source,
   free-surface mirror, u and w updates, w mirror, receiver gather,
   illumination sums);
@@ -29,19 +29,6 @@ def _cpu_only(*ts):
 def pad_edge(v, nabc):
     """Edge-replicate padding by ``nabc`` cells on all four sides (acoustic_kernels.py:16-37)."""
     return torch.nn.functional.pad(v[None, None], (nabc, nabc, nabc, nabc), mode="replicate")[0, 0]
-
-
-def _coefficients(c, den, damp, dt, dz, fs):
-    """alpha/kappa arrays exactly as acoustic_kernels.py:257-265 builds them."""
-    nzp, nxp = damp.shape
-    alpha1 = den * c * c * dt / dz
-    kappa1 = damp * dt
-    alpha2 = dt / (den * dz)
-    kappa2 = torch.zeros_like(damp)
-    kappa2[:, 1:nxp - 2] = 0.5 * (damp[:, 1:nxp - 2] + damp[:, 2:nxp - 1]) * dt
-    kappa3 = torch.zeros_like(damp)
-    kappa3[fs:nzp - 2, :] = 0.5 * (damp[fs:nzp - 2, :] + damp[fs + 1:nzp - 1, :]) * dt
-    return alpha1, kappa1, alpha2, kappa2, kappa3
 
 
 def _step(p, u, w, it, co, src, rcv, fs, free_surface, dt, nabc, nz, nx):
@@ -93,19 +80,35 @@ def acoustic_forward(vp, rho, damp, src_x, src_z, wavelet, rcv_x, rcv_z, *, nabc
     Differentiable w.r.t. ``vp`` and ``rho`` through autograd.
     """
     _cpu_only(vp, rho, damp, wavelet)
-    nz, nx = vp.shape
-    dtype = vp.dtype
     c = pad_edge(vp, nabc)
     den = pad_edge(rho, nabc)
+    alpha1 = den * c * c * dt / dz
+    alpha2 = dt / (den * dz)
+    return acoustic_forward_coef(alpha1, alpha2, damp, src_x, src_z, wavelet, rcv_x, rcv_z, nabc=nabc,
+                                 free_surface=free_surface, dt=dt, checkpoint_segments=checkpoint_segments)
+
+
+def acoustic_forward_coef(alpha1, alpha2, damp, src_x, src_z, wavelet, rcv_x, rcv_z, *, nabc, free_surface, dt,
+                          checkpoint_segments=1):
+    """The time loop of acoustic_kernels.py:239-301 given alpha1 = rho c^2 dt/dz and
+    alpha2 = dt/(rho dz) on the padded grid (differentiable w.r.t. both)."""
+    _cpu_only(alpha1, alpha2, damp, wavelet)
+    nzp, nxp = alpha1.shape
+    nz, nx = nzp - 2 * nabc, nxp - 2 * nabc
+    dtype = alpha1.dtype
     fs = nabc if free_surface else 1
-    nzp, nxp = nz + 2 * nabc, nx + 2 * nabc
     sx = torch.as_tensor(src_x, dtype=torch.long) + nabc
     sz = torch.as_tensor(src_z, dtype=torch.long) + nabc
     rx = torch.as_tensor(rcv_x, dtype=torch.long) + nabc
     rz = torch.as_tensor(rcv_z, dtype=torch.long) + nabc
     ns = sx.numel()
     damp = damp.to(dtype)
-    co = _coefficients(c, den, damp, dt, dz, fs)
+    kappa1 = damp * dt
+    kappa2 = torch.zeros_like(damp)
+    kappa2[:, 1:nxp - 2] = 0.5 * (damp[:, 1:nxp - 2] + damp[:, 2:nxp - 1]) * dt
+    kappa3 = torch.zeros_like(damp)
+    kappa3[fs:nzp - 2, :] = 0.5 * (damp[fs:nzp - 2, :] + damp[fs + 1:nzp - 1, :]) * dt
+    co = (alpha1, kappa1, alpha2, kappa2, kappa3)
     p = torch.zeros((ns, nzp, nxp), dtype=dtype)
     u = torch.zeros((ns, nzp, nxp - 1), dtype=dtype)
     w = torch.zeros((ns, nzp - 1, nxp), dtype=dtype)
@@ -113,7 +116,6 @@ def acoustic_forward(vp, rho, damp, src_x, src_z, wavelet, rcv_x, rcv_z, *, nabc
     fwu = torch.zeros((nz, nx), dtype=dtype)
     fww = torch.zeros((nz, nx), dtype=dtype)
     recs = ([], [], [])
-    k = 0
     for chunk in torch.chunk(wavelet, checkpoint_segments, dim=-1):
         seg_p = torch.zeros((nz, nx), dtype=dtype)
         seg_u = torch.zeros((nz, nx), dtype=dtype)
@@ -129,7 +131,6 @@ def acoustic_forward(vp, rho, damp, src_x, src_z, wavelet, rcv_x, rcv_z, *, nabc
         fwp = fwp + seg_p
         fwu = fwp + seg_u
         fww = fwp + seg_w
-        k += chunk.shape[-1]
     out = {}
     for key, lst in zip(("p", "u", "w"), recs):
         out[key] = torch.stack(lst, dim=1)

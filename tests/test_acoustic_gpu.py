@@ -25,8 +25,27 @@ def test_forward_matches_oracle_f32(free_surface, segments):
     ref, _, _ = oracle_acoustic(prop, model, segments=segments, requires_grad=False)
     for k in KEYS:
         assert rel(rec[k], ref[k]) <= 1e-5, (k, rel(rec[k], ref[k]))
-    for k in ("p", "u", "w"):
-        assert torch.equal(rec[k].cpu(), ref[k]), k  # same operation order: bit-identical records
+
+
+@pytest.mark.parametrize("free_surface", [False, True])
+def test_forward_is_bit_identical_given_identical_coefficients(free_surface):
+    """With the same alpha arrays (computed once on the CPU) the kernel reproduces the CPU
+    reference arithmetic exactly: it keeps the reference's operation order, no FMA."""
+    from adfwi_gb300.acoustic import AcousticSolve
+    from oracle.acoustic import acoustic_forward_coef, pad_edge
+    model, survey, prop = acoustic_problem(A, free_surface=free_surface, seed=4)
+    model.forward()
+    c = pad_edge(model.vp.detach().cpu(), prop.nabc)
+    den = pad_edge(model.rho.detach().cpu(), prop.nabc)
+    a1 = den * c * c * prop.dt / prop.dz
+    a2 = prop.dt / (den * prop.dz)
+    _, plan = prop.plan()
+    out = AcousticSolve.apply(a1.cuda(), a2.cuda(), prop.damp, prop.wavelet, plan)
+    ref = acoustic_forward_coef(a1, a2, prop.damp.cpu(), prop.src_loc[:, 0], prop.src_loc[:, 1],
+                                prop.wavelet.cpu(), prop.rcv_loc[:, 0], prop.rcv_loc[:, 1], nabc=prop.nabc,
+                                free_surface=bool(free_surface), dt=prop.dt)
+    for o, k in zip(out[:3], ("p", "u", "w")):
+        assert torch.equal(o.cpu(), ref[k]), (k, rel(o, ref[k]))
 
 
 def test_forward_matches_oracle_f64_subset():

@@ -38,6 +38,11 @@ class ElasticDesc(ctypes.Structure):
     ]
 
 
+class KernelStat(ctypes.Structure):
+    _fields_ = [("name", ctypes.c_char * 32), ("launches", c_int64), ("timed_launches", c_int64),
+                ("total_ms", ctypes.c_double)]
+
+
 def library_path():
     return os.path.join(os.path.dirname(os.path.abspath(__file__)), "lib", "libadfwi_gb300.so")
 
@@ -53,6 +58,9 @@ def _bind(lib):
         "adfwi_acoustic_forward": (c_int32, [P, P, P, P, P, P, P, P, P, P, P, c_int32, P, c_int64, P]),
         "adfwi_acoustic_backward": (c_int32, [P, P, P, P, P, P, P, P, P, P, P, c_int64, P]),
         "adfwi_last_error": (c_int32, [ctypes.c_char_p, ctypes.c_size_t]),
+        "adfwi_profile_start": (c_int32, [c_int32]),
+        "adfwi_profile_stop": (c_int32, [ctypes.POINTER(KernelStat), c_int32, ctypes.POINTER(c_int32)]),
+        "adfwi_launch_count": (c_int64, []),
         "adfwi_version": (ctypes.c_char_p, []),
     }
     optional = {
@@ -110,3 +118,20 @@ def ptr(t):
 def stream_handle(device):
     import torch
     return c_void_p(torch.cuda.current_stream(device).cuda_stream)
+
+
+def launch_count():
+    """Kernel launches issued by the library so far in this process."""
+    return int(lib().adfwi_launch_count())
+
+
+def profile_start(timed=True):
+    check(lib().adfwi_profile_start(int(bool(timed))), "adfwi_profile_start")
+
+
+def profile_stop():
+    """Per-kernel-class {name: (launches, timed_launches, total_ms)} of the session."""
+    out = (KernelStat * 16)()
+    n = c_int32()
+    check(lib().adfwi_profile_stop(out, 16, ctypes.byref(n)), "adfwi_profile_stop")
+    return {out[i].name.decode(): (out[i].launches, out[i].timed_launches, out[i].total_ms) for i in range(n.value)}

@@ -167,6 +167,8 @@ class AcousticSolve(torch.autograd.Function):
     def backward(ctx, grp, gru, grw, _gfp, _gfu, _gfw):
         alpha1, alpha2, damp, wavelet = ctx.saved_tensors
         if ctx.ws is None:
-            raise RuntimeError("AcousticSolve.backward called without a gradient-mode forward")
+            raise RuntimeError("AcousticSolve.backward: the forward kept no snapshots (inputs did not require "
+                               "grad) or they were already used by an earlier backward; run forward again")
         ga1, ga2 = ctx.plan.run_backward(alpha1, alpha2, damp, wavelet, (grp, gru, grw), ctx.ws)
+        ctx.ws = None  # release the snapshot workspace as soon as the adjoint has consumed it
         return ga1, ga2, None, None, None

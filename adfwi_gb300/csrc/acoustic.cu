@@ -645,8 +645,9 @@ int setup_common(const adfwi_acoustic_plan* p, unsigned char* ws, const Carve& c
   T* cf = reinterpret_cast<T*>(ws + c.coef);
   const void* src[3] = {alpha1, alpha2, damp};
   for (int q = 0; q < 3; ++q) {
-    ac::pack_plane<T><<<grid_blocks(n), 256, 0, st>>>(p->L, p->nzp, p->nxp, static_cast<const T*>(src[q]),
-                                                      reinterpret_cast<T*>(reinterpret_cast<unsigned char*>(cf) + q * pl));
+    ADFWI_LAUNCH(kAux, st, (ac::pack_plane<T><<<grid_blocks(n), 256, 0, st>>>(
+                                p->L, p->nzp, p->nxp, static_cast<const T*>(src[q]),
+                                reinterpret_cast<T*>(reinterpret_cast<unsigned char*>(cf) + q * pl))));
   }
   ADFWI_CUDA_TRY(cudaGetLastError());
   return kOk;
@@ -659,8 +660,8 @@ void launch_fwd(const adfwi_acoustic_plan* p, const ac::Geo<T>& g, int it, int a
   const int64_t pl = p->L.plane;
   dim3 grid(p->tiles_x, p->tiles_z, p->ngroups);
   dim3 block(ac::TX, ac::BY);
-  ac::fwd_step<T><<<grid, block, sizeof(ac::FwdSmem<T>), st>>>(
-      g, it, p->G, accum_u, cf, cf + pl, cf + 2 * pl, wav, p0, u0, w0, p1, u1, w1, d1, rp, ru, rw, ilp, ilu);
+  ADFWI_LAUNCH(kAcFwdStep, st, (ac::fwd_step<T><<<grid, block, sizeof(ac::FwdSmem<T>), st>>>(
+      g, it, p->G, accum_u, cf, cf + pl, cf + 2 * pl, wav, p0, u0, w0, p1, u1, w1, d1, rp, ru, rw, ilp, ilu)));
 }
 
 template <typename T>
@@ -726,9 +727,9 @@ int forward_impl(const adfwi_acoustic_plan* p, const void* alpha1, const void* a
   ADFWI_CUDA_TRY(cudaGetLastError());
   if (fw_p || fw_u || fw_w) {
     const int64_t n = (int64_t)p->d.nz * p->d.nx;
-    ac::illum_finalize<T><<<grid_blocks(n), 256, 0, st>>>(p->L, p->ngroups, p->d.ns, p->d.nabc, p->d.nz, p->d.nx,
-                                                          ilp, ilu, cur + 2 * ns * pl, static_cast<T*>(fw_p),
-                                                          static_cast<T*>(fw_u), static_cast<T*>(fw_w));
+    ADFWI_LAUNCH(kAux, st, (ac::illum_finalize<T><<<grid_blocks(n), 256, 0, st>>>(
+                                p->L, p->ngroups, p->d.ns, p->d.nabc, p->d.nz, p->d.nx, ilp, ilu, cur + 2 * ns * pl,
+                                static_cast<T*>(fw_p), static_cast<T*>(fw_u), static_cast<T*>(fw_w))));
     ADFWI_CUDA_TRY(cudaGetLastError());
   }
   return kOk;
@@ -770,7 +771,8 @@ int backward_impl(const adfwi_acoustic_plan* p, const void* wavelet, const void*
   ADFWI_CUDA_TRY(cudaMemsetAsync(g2, 0, (size_t)p->ngroups * pl * sizeof(T), st));
   if (gp || gu || gw) {
     dim3 sg(std::max(1, std::min(64, (p->ncells + 127) / 128)), p->d.ns);
-    ac::adj_seed<T><<<sg, 128, 0, st>>>(g, p->ntiles, gp, gu, gw, la, la + ns * pl, la + 2 * ns * pl);
+    ADFWI_LAUNCH(kAux, st, (ac::adj_seed<T><<<sg, 128, 0, st>>>(g, p->ntiles, gp, gu, gw, la, la + ns * pl,
+                                                                   la + 2 * ns * pl)));
   }
   T* lcur = la;
   T* lnxt = lb;
@@ -796,19 +798,19 @@ int backward_impl(const adfwi_acoustic_plan* p, const void* wavelet, const void*
       }
     }
     for (int it = t1 - 1; it >= t0; --it) {
-      ac::adj_step<T><<<grid, block, sizeof(ac::AdjSmem<T>), st>>>(
+      ADFWI_LAUNCH(kAcAdjStep, st, (ac::adj_step<T><<<grid, block, sizeof(ac::AdjSmem<T>), st>>>(
           g, it, p->G, cf, cf + pl, cf + 2 * pl, lcur, lcur + ns * pl, lcur + 2 * ns * pl, lnxt, lnxt + ns * pl,
           lnxt + 2 * ns * pl, hp + (int64_t)(it - t0) * ns * pl, hd + (int64_t)(it - t0) * ns * pl, gp, gu, gw, g1,
-          g2);
+          g2)));
       std::swap(lcur, lnxt);
     }
     ADFWI_CUDA_TRY(cudaGetLastError());
   }
   const int64_t n = (int64_t)p->nzp * p->nxp;
-  ac::reduce_planes<T><<<grid_blocks(n), 256, 0, st>>>(p->L, p->ngroups, 0, 0, p->nzp, p->nxp, g1,
-                                                       static_cast<T*>(ga1));
-  ac::reduce_planes<T><<<grid_blocks(n), 256, 0, st>>>(p->L, p->ngroups, 0, 0, p->nzp, p->nxp, g2,
-                                                       static_cast<T*>(ga2));
+  ADFWI_LAUNCH(kAux, st, (ac::reduce_planes<T><<<grid_blocks(n), 256, 0, st>>>(p->L, p->ngroups, 0, 0, p->nzp,
+                                                                                p->nxp, g1, static_cast<T*>(ga1))));
+  ADFWI_LAUNCH(kAux, st, (ac::reduce_planes<T><<<grid_blocks(n), 256, 0, st>>>(p->L, p->ngroups, 0, 0, p->nzp,
+                                                                                p->nxp, g2, static_cast<T*>(ga2))));
   ADFWI_CUDA_TRY(cudaGetLastError());
   return kOk;
 }

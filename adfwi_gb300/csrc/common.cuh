@@ -15,6 +15,8 @@
 #include <stdint.h>
 #include <stddef.h>
 
+#include "profile.cuh"
+
 namespace adfwi {
 
 constexpr int GZ = 4;
@@ -68,6 +70,14 @@ void set_error(const char* fmt, ...);
                          __FILE__, __LINE__);                                     \
       return ::adfwi::kCudaError;                                                 \
     }                                                                             \
+  } while (0)
+
+// Launch a kernel under the library's launch accounting (see profile.cuh).
+#define ADFWI_LAUNCH(cls, st, launch)                          \
+  do {                                                         \
+    int tok__ = ::adfwi::prof_before((cls), (st));             \
+    launch;                                                    \
+    ::adfwi::prof_after((cls), (st), tok__);                   \
   } while (0)
 
 #define ADFWI_CHECK_ARG(cond, ...)         \

@@ -95,9 +95,9 @@ int snapshot_store(int prec, const T* src, int64_t nplanes, int64_t plane, unsig
   unsigned short* q = reinterpret_cast<unsigned short*>(snap) + first * plane;
   float* sc = reinterpret_cast<float*>(scales) + first;
   if (prec == ADFWI_SNAP_FP16)
-    snap_quantize<T, true><<<(unsigned)nplanes, kSnapThreads, 0, st>>>(src, plane, q, sc);
+    ADFWI_LAUNCH(kAux, st, (snap_quantize<T, true><<<(unsigned)nplanes, kSnapThreads, 0, st>>>(src, plane, q, sc)));
   else
-    snap_quantize<T, false><<<(unsigned)nplanes, kSnapThreads, 0, st>>>(src, plane, q, sc);
+    ADFWI_LAUNCH(kAux, st, (snap_quantize<T, false><<<(unsigned)nplanes, kSnapThreads, 0, st>>>(src, plane, q, sc)));
   ADFWI_CUDA_TRY(cudaGetLastError());
   return kOk;
 }
@@ -113,9 +113,9 @@ int snapshot_load(int prec, T* dst, int64_t nplanes, int64_t plane, const unsign
   const unsigned short* q = reinterpret_cast<const unsigned short*>(snap) + first * plane;
   const float* sc = reinterpret_cast<const float*>(scales) + first;
   if (prec == ADFWI_SNAP_FP16)
-    snap_dequantize<T, true><<<(unsigned)nplanes, kSnapThreads, 0, st>>>(q, sc, plane, dst);
+    ADFWI_LAUNCH(kAux, st, (snap_dequantize<T, true><<<(unsigned)nplanes, kSnapThreads, 0, st>>>(q, sc, plane, dst)));
   else
-    snap_dequantize<T, false><<<(unsigned)nplanes, kSnapThreads, 0, st>>>(q, sc, plane, dst);
+    ADFWI_LAUNCH(kAux, st, (snap_dequantize<T, false><<<(unsigned)nplanes, kSnapThreads, 0, st>>>(q, sc, plane, dst)));
   ADFWI_CUDA_TRY(cudaGetLastError());
   return kOk;
 }

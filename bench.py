@@ -1,0 +1,368 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 propagator hot path: fwd+adjoint gradient throughput.
+
+Workload (one "step"): one full-waveform-inversion gradient evaluation on the 200 x 600
+layered/faulted iso-acoustic model (dx = 20 m, PML 50 -> 300 x 700 padded cells), 30 surface
+shots, 600 receivers, nt = 3000, dt = 1.5 ms, 8 Hz Ricker, FP32: forward solve on the smoothed
+starting model, per-trace normalisation and the L2 misfit against data observed on the true
+model, then the hand-written checkpointed adjoint back to dL/dvp. Inputs are seeded synthetic
+stand-ins with those shapes and distributions (no public dataset).
+
+Metric: Gcell-updates/s = shots * nzp * nxp * nt / time per gradient step.
+  value: device time (CUDA events) with every input resident in HBM;
+  e2e:   the same step through the public API with the model and the observed data copied
+         from pinned host memory each step and the gradient + loss read back.
+
+Arms: the default arm runs the CUDA library; ``--impl reference`` times the CPU oracle
+(the reference's algorithm restated in PyTorch, CPU, all host threads) on a bounded sample
+of the same workload.
+
+Multi-GPU (torchrun, N > 1): every rank solves its own copy of the workload (shots are
+independent; no collective on the data path), timing is the max over ranks, value = all
+ranks' cell-updates / that time ("weak" scaling).
+"""
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+import torch
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "fwd+adjoint Gcell-updates/s"
+UNIT = "Gcell-updates/s"
+WORKLOAD = ("iso-acoustic forward + L2-misfit adjoint gradient: 200x600 layered model with 12 dipping "
+            "interfaces and 2 normal faults, dx=20 m, PML 50 (300x700 padded), nt=3000, dt=1.5 ms, 8 Hz Ricker, "
+            "30 surface shots, 600 receivers, FP32, checkpointed hand-written adjoint")
+# Algorithmic bytes per cell-update of each kernel class (the figures the roofline uses):
+#   forward step: read+write p, u, w (24 B) + the two per-cell coefficients (8 B);
+#   adjoint step: adjoint state read+write (24 B) + coefficients (8 B) + reloaded forward
+#                 state (12 B) + gradient accumulators read+write (8 B).
+ALGO_BYTES = {"acoustic_fwd_step": 32.0, "acoustic_adj_step": 52.0}
+# Gradient step total per cell-update (forward 32 + recompute 32 + segment store 12 + adjoint 52).
+GRAD_BYTES = 128.0
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def ncu_traffic():
+    """Per-launch DRAM bytes of each kernel from the committed ncu summaries (or {})."""
+    out = {}
+    pdir = os.path.join(ROOT, "profiles")
+    if not os.path.isdir(pdir):
+        return out
+    for fn in sorted(os.listdir(pdir)):
+        if not fn.endswith((".md", ".txt")):
+            continue
+        with open(os.path.join(pdir, fn)) as f:
+            for line in f:
+                m = re.match(r"\s*traffic_bytes_per_launch\s+(\S+)\s+([0-9.eE+]+)\s+cells_per_launch\s+([0-9.eE+]+)",
+                             line)
+                if m:
+                    out[m.group(1)] = (float(m.group(2)), float(m.group(3)))
+    return out
+
+
+class ClockSampler(object):
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while active."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join("/tmp", "adfwi_clocks_%d_%d.csv" % (os.getpid(), index))
+
+    def __enter__(self):
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        reasons = sorted({n for r in rows for n, v in zip(names, r[5:9]) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend=backend)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, world, device):
+    if world == 1:
+        return x
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def l2_misfit(syn, obs, dt):
+    """Misfit_waveform_L2 (ADFWI/fwi/misfit/L2.py:26-29) on max-normalised traces
+    (ADFWI/fwi/acoustic_fwi.py:149-150): sum over traces of sqrt(sum_t r^2 dt)."""
+    syn = syn / torch.max(torch.abs(syn), dim=1, keepdim=True).values
+    rsd = obs - syn
+    return torch.sum(torch.sqrt(torch.sum(rsd * rsd * dt, dim=1)))
+
+
+def gpu_arm(args, world, rank, local):
+    import adfwi_gb300 as A
+    from adfwi_gb300 import _native as N
+    from adfwi_gb300.synthetic import acoustic_gradient_case
+
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    model, survey, vp_true, vp_init = acoustic_gradient_case(seed=0, device=str(dev))
+    free, _ = torch.cuda.mem_get_info(dev)
+    prop = A.AcousticPropagator(model, survey, device=str(dev), memory_budget=int(args.memory_fraction * free))
+    nt, dt, ns = prop.nt, prop.dt, prop.src_n
+    nzp, nxp = prop.nz + 2 * prop.nabc, prop.nx + 2 * prop.nabc
+    cells = ns * nzp * nxp * nt
+    # observed data on the true model (setup, untimed)
+    with torch.no_grad():
+        model.vp.data.copy_(torch.as_tensor(vp_true, device=dev))
+        obs = prop.forward()["p"]
+        obs = (obs / torch.max(torch.abs(obs), dim=1, keepdim=True).values).contiguous()
+    vp0 = torch.as_tensor(vp_init, device=dev)
+
+    def step(obs_dev):
+        model.vp.data.copy_(vp0)
+        model.vp.grad = None
+        rec = prop.forward()
+        loss = l2_misfit(rec["p"], obs_dev, dt)
+        loss.backward()
+        return loss
+
+    _, plan = prop.plan()
+    K = plan.snapshot_every
+    for _ in range(args.warmup):
+        step(obs)
+    torch.cuda.synchronize(dev)
+
+    # -- value: inputs resident in HBM, device time over exactly `steps` steps
+    barrier(world)
+    torch.cuda.synchronize(dev)
+    n0 = N.launch_count()
+    with ClockSampler(local) as clk:
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.steps):
+            loss = step(obs)
+        e1.record()
+        torch.cuda.synchronize(dev)
+    barrier(world)
+    launches = N.launch_count() - n0
+    ms = e0.elapsed_time(e1)
+    ms = max_over_ranks(ms, world, dev)
+    ms_step = ms / args.steps
+    value = world * cells / (ms_step * 1e-3) / 1e9
+
+    # -- e2e: public API with host buffers (pinned), copies inside the timed region
+    vp_host = torch.as_tensor(vp_init).pin_memory()
+    obs_host = obs.cpu().pin_memory()
+    obs_dev = torch.empty_like(obs)
+    grad_host = torch.empty(model.vp.shape, dtype=model.vp.dtype).pin_memory()
+    h2d = vp_host.numel() * vp_host.element_size() + obs_host.numel() * obs_host.element_size()
+    d2h = grad_host.numel() * grad_host.element_size() + 4
+    barrier(world)
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        vp0.copy_(vp_host, non_blocking=True)
+        obs_dev.copy_(obs_host, non_blocking=True)
+        loss = step(obs_dev)
+        grad_host.copy_(model.vp.grad, non_blocking=True)
+        _ = float(loss.item())
+    torch.cuda.synchronize(dev)
+    e2e_s = max_over_ranks(time.perf_counter() - t0, world, dev)
+    e2e_value = world * cells * args.steps / e2e_s / 1e9
+
+    # -- roofline: per-kernel-class device time from CUDA events around every launch
+    N.profile_start(True)
+    for _ in range(max(1, min(args.steps, 2))):
+        step(obs)
+    torch.cuda.synchronize(dev)
+    stats = N.profile_stop()
+    peak, peak_kind = peaks()
+    timed = {k: v for k, v in stats.items() if k in ALGO_BYTES and v[1] > 0}
+    roof = None
+    if timed:
+        dom = max(timed, key=lambda k: timed[k][2])
+        launches_dom, tl, tot_ms = timed[dom]
+        avg_s = tot_ms / tl * 1e-3
+        cells_launch = ns * nzp * nxp
+        algo = ALGO_BYTES[dom] * cells_launch
+        achieved = algo / avg_s / 1e9
+        tr = ncu_traffic().get(dom)
+        traffic = None
+        if tr is not None:
+            traffic = tr[0] * cells_launch / tr[1]  # scale a smaller capture by the cells processed
+        roof = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "peak_source": peak_kind, "traffic": traffic,
+                "algorithmic_bytes_per_launch": algo, "avg_launch_ms": round(avg_s * 1e3, 5),
+                "kernel_share": {k: round(v[2] / sum(x[2] for x in stats.values()), 4) for k, v in stats.items()}}
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms_step, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded layered/faulted model, Ricker sources)",
+        "config": {"workload": WORKLOAD, "shots": ns, "nt": nt, "grid_padded": [nzp, nxp], "receivers": prop.rcv_n,
+                   "snapshot_every": K, "snapshot_precision": "native",
+                   "l2": "working set larger than L2 (fields + segment history >> 129 MB), no flush",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": int(launches),
+        "roofline": roof,
+        "clocks": clk.summary(),
+        "loss": float(loss.item()),
+    }
+    return line
+
+
+def cpu_sample(n_steps, threads):
+    """Time the CPU oracle on a bounded sample: 1 shot of the gradient workload, n_steps steps,
+    forward + autograd backward (the reference's own gradient mechanism)."""
+    from adfwi_gb300.synthetic import layered_faulted, smooth, surface_acquisition
+    from oracle.acoustic import acoustic_forward
+    from adfwi_gb300.boundary import bc_pml
+    torch.set_num_threads(threads)
+    rng = np.random.default_rng(0)
+    vp_true = layered_faulted(200, 600, rng)
+    vp = smooth(vp_true, 10.0).astype(np.float32)
+    rho = (np.power(vp, 0.25) * 310).astype(np.float32)
+    sv = surface_acquisition(600, n_steps, 1.5e-3, 8.0, 30)
+    damp = torch.tensor(bc_pml(600, 200, 20.0, 20.0, 50, vp.max(), free_surface=False), dtype=torch.float32)
+    wav = torch.tensor(sv.source.get_wavelet()[:1], dtype=torch.float32)
+    loc = sv.source.get_loc()[:1]
+    rl = sv.receiver.get_loc()
+    vpt = torch.tensor(vp, requires_grad=True)
+    t0 = time.perf_counter()
+    out = acoustic_forward(vpt, torch.tensor(rho), damp, loc[:, 0], loc[:, 1], wav, rl[:, 0], rl[:, 1], nabc=50,
+                           free_surface=False, dx=20.0, dz=20.0, dt=1.5e-3)
+    out["p"].square().sum().backward()
+    t = time.perf_counter() - t0
+    cells = 1 * 300 * 700 * n_steps
+    return cells / t / 1e9, t
+
+
+def reference_arm(args):
+    threads = os.cpu_count() or 1
+    n_steps = args.cpu_sample_steps
+    cpu_sample(min(20, n_steps), threads)  # warm the allocator / thread pool
+    for _ in range(args.warmup):
+        cpu_sample(n_steps, threads)
+    vals = []
+    t_all = 0.0
+    for _ in range(args.steps):
+        v, t = cpu_sample(n_steps, threads)
+        vals.append(v)
+        t_all += t
+    value = args.steps * 300 * 700 * n_steps / t_all / 1e9
+    sample = "1 shot x %d steps of the 300x700 padded gradient workload (forward + autograd backward)" % n_steps
+    return {"impl": "reference", "metric": METRIC, "value": round(value, 5), "unit": UNIT, "n_gpus": 0,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t_all / args.steps * 1e3, 1),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded layered/faulted model, Ricker sources)",
+            "config": {"workload": WORKLOAD, "sample": sample},
+            "cpu_baseline": {"value": round(value, 5), "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": round(value, 5), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--memory-fraction", type=float, default=0.7,
+                    help="share of free HBM the gradient workspace may use (snapshot / history sizing)")
+    ap.add_argument("--cpu-sample-steps", type=int, default=300)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps(reference_arm(args)), flush=True)
+        return
+    line = gpu_arm(args, world, rank, local)
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        # bounded sample: repeat a 1-shot slice of the workload until >= 10 s of CPU work
+        threads = os.cpu_count() or 1
+        done, t_all, reps = 0, 0.0, 0
+        while t_all < 10.0 and reps < 50:
+            _, t = cpu_sample(args.cpu_sample_steps, threads)
+            done += 300 * 700 * args.cpu_sample_steps
+            t_all += t
+            reps += 1
+        line["cpu_baseline"] = {"value": round(done / t_all / 1e9, 5), "unit": UNIT, "cores": threads,
+                                "kind": "port",
+                                "sample": "%d x (1 shot x %d steps) of the 300x700 padded gradient workload, CPU "
+                                          "oracle forward + autograd backward, %.1f s" % (reps, args.cpu_sample_steps,
+                                                                                          t_all)}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

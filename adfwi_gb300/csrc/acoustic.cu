@@ -23,6 +23,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 #include <new>
 #include <vector>
 
@@ -815,9 +816,70 @@ int backward_impl(const adfwi_acoustic_plan* p, const void* wavelet, const void*
   return kOk;
 }
 
+// ----------------------------------------------------------------------------------------
+// Forward solve for callers that cannot allocate device memory.
+//
+// Its scratch (staged coefficients, wavefield ping-pong buffers, illumination partials and
+// geometry tables) lives in one file-scope __device__ array of kStaticScratchBytes, which
+// every GPU that loads this library reserves until the process exits. Host code never
+// passes the symbol itself to a kernel (on the host it only names a stand-in object):
+// the device address is looked up once per device with cudaGetSymbolAddress, on that
+// device, by the first call made there.
+// ----------------------------------------------------------------------------------------
+constexpr int64_t kStaticScratchBytes = int64_t(64) << 20;  // 64 MiB
+__device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
+std::mutex g_static_mu;
+std::vector<void*> g_static_addr;  // device address of g_static_scratch, per device ordinal
+
+int static_scratch_address(void** out) {
+  int dev = 0;
+  ADFWI_CUDA_TRY(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(g_static_mu);
+  if ((int)g_static_addr.size() <= dev) g_static_addr.resize(dev + 1, nullptr);
+  if (g_static_addr[dev] == nullptr) {
+    void* addr = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&addr, g_static_scratch);
+    if (e != cudaSuccess || addr == nullptr) {
+      set_error("cudaGetSymbolAddress(static scratch) failed on device %d: %s", dev, cudaGetErrorString(e));
+      return kCudaError;
+    }
+    g_static_addr[dev] = addr;
+  }
+  *out = g_static_addr[dev];
+  return kOk;
+}
+
 }  // namespace
 
 extern "C" {
+
+int adfwi_acoustic_forward_noalloc(const adfwi_acoustic_plan* p, const void* alpha1, const void* alpha2,
+                                   const void* damp, const void* wavelet, void* rec_p, void* rec_u, void* rec_w,
+                                   void* fw_p, void* fw_u, void* fw_w, void* stream) {
+  ADFWI_CHECK_ARG(p && alpha1 && alpha2 && damp && wavelet, "null argument");
+  ADFWI_CHECK_ARG((rec_p && rec_u && rec_w) || (!rec_p && !rec_u && !rec_w), "records: give all three or none");
+  ADFWI_CHECK_ARG(p->d.nr > 0 || rec_p == nullptr, "records requested without receivers");
+  const int64_t need = carve(p, false, 1).total;
+  if (need > kStaticScratchBytes) {
+    set_error("adfwi_acoustic_forward_noalloc: this solve needs %lld bytes of scratch but the static scratch "
+              "array holds %lld bytes (64 MiB); use adfwi_acoustic_forward with a caller-provided workspace",
+              (long long)need, (long long)kStaticScratchBytes);
+    return kWorkspaceTooSmall;
+  }
+  void* ws = nullptr;
+  int rc = static_scratch_address(&ws);
+  if (rc) return rc;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  unsigned char* w = static_cast<unsigned char*>(ws);
+  // forward_impl clears every scratch region it accumulates into (coefficient ghosts, field
+  // buffers, illumination partials) before the first step, so a previous call's leftovers
+  // in the shared array do not leak into this one.
+  if (p->d.dtype == ADFWI_F64)
+    return forward_impl<double>(p, alpha1, alpha2, damp, wavelet, rec_p, rec_u, rec_w, fw_p, fw_u, fw_w, false, w,
+                                kStaticScratchBytes, st);
+  return forward_impl<float>(p, alpha1, alpha2, damp, wavelet, rec_p, rec_u, rec_w, fw_p, fw_u, fw_w, false, w,
+                             kStaticScratchBytes, st);
+}
 
 int adfwi_acoustic_plan_create(const adfwi_acoustic_desc* desc, const int32_t* src_z, const int32_t* src_x,
                                const int32_t* rcv_z, const int32_t* rcv_x, adfwi_acoustic_plan** out) {

@@ -100,6 +100,25 @@ int adfwi_acoustic_backward(const adfwi_acoustic_plan* plan, const void* alpha1,
                             const void* grad_rec_w, void* grad_alpha1, void* grad_alpha2,
                             void* workspace, int64_t workspace_bytes, void* stream);
 
+/* Forward solve that allocates nothing, for callers that cannot call cudaMalloc: hosts whose
+ * device memory is entirely owned by another allocator or pool, sandboxed plug-ins that may
+ * not grow their footprint after start-up, or code running where an allocation would break
+ * a pre-planned memory budget. It has no counterpart in the reference (whose PyTorch path
+ * allocates through the caching allocator on every step).
+ * Same arguments and results as adfwi_acoustic_forward without the gradient mode and
+ * without the workspace: the scratch is a static device array of 64 MiB inside the
+ * library, reserved on every GPU that loads the library until the process exits. A solve
+ * whose scratch (adfwi_acoustic_workspace_bytes(plan, 0, ...)) exceeds 64 MiB is rejected
+ * with ADFWI_ERR_WORKSPACE and a message. The first call on each device looks up the
+ * array's device address (cudaGetSymbolAddress) on that device; make that first call
+ * before any stream capture. All calls share the one array and it keeps the last call's
+ * contents: the call clears what it accumulates into, but two calls whose work overlaps on
+ * the GPU (for example on two streams) race on it and must be serialised by the caller. */
+int adfwi_acoustic_forward_noalloc(const adfwi_acoustic_plan* plan, const void* alpha1,
+                                   const void* alpha2, const void* damp, const void* wavelet,
+                                   void* rec_p, void* rec_u, void* rec_w, void* fw_p, void* fw_u,
+                                   void* fw_w, void* stream);
+
 /* ------------------------------------------------------------------------- */
 /* Errors and build information.                                             */
 /* ------------------------------------------------------------------------- */

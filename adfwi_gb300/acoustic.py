@@ -126,6 +126,14 @@ class AcousticPlan(object):
         N.check(rc, "adfwi_acoustic_forward")
         return records + fw + (workspace,)
 
+    def status(self, workspace, with_gradient, stream=None):
+        """Device status of the last solve in ``workspace`` (0 = clean); waits for the stream."""
+        v = ctypes.c_int32()
+        st = ctypes.c_void_p(stream) if stream is not None else N.stream_handle(workspace.device)
+        N.check(self.lib.adfwi_acoustic_status(self.handle, N.ptr(workspace), workspace.numel(),
+                                               int(bool(with_gradient)), ctypes.byref(v), st), "adfwi_acoustic_status")
+        return v.value
+
     def run_backward(self, alpha1, alpha2, damp, wavelet, grads, workspace, stream=None):
         """Adjoint solve after run_forward(with_gradient=True); returns (dL/d alpha1, dL/d alpha2)."""
         shp = (self.ns, self.nt, self.nr)
@@ -170,5 +178,9 @@ class AcousticSolve(torch.autograd.Function):
             raise RuntimeError("AcousticSolve.backward: the forward kept no snapshots (inputs did not require "
                                "grad) or they were already used by an earlier backward; run forward again")
         ga1, ga2 = ctx.plan.run_backward(alpha1, alpha2, damp, wavelet, (grp, gru, grw), ctx.ws)
+        code = ctx.plan.status(ctx.ws, True)
+        if code != 0:
+            raise RuntimeError("adfwi_gb300: a pipeline wait timed out on the GPU during this solve (status %d); "
+                               "its results are invalid" % code)
         ctx.ws = None  # release the snapshot workspace as soon as the adjoint has consumed it
         return ga1, ga2, None, None, None

@@ -30,6 +30,7 @@
 #include "../../include/adfwi_gb300.h"
 #include "common.cuh"
 #include "snapshot.cuh"
+#include "tma.cuh"
 
 namespace adfwi {
 namespace ac {
@@ -523,29 +524,40 @@ __global__ void illum_finalize(Layout L, int groups, int ns, int nabc, int nz, i
 }  // namespace ac
 }  // namespace adfwi
 
+#include "acoustic_tma.cuh"
+
 // ----------------------------------------------------------------------------------------
 // Plan, workspace and drivers.
 // ----------------------------------------------------------------------------------------
 using namespace adfwi;
 
+// Tiling of the grid for one kernel generation, with its receiver tables (offsets into tab).
+struct Tiling {
+  int tz, tx;
+  int tiles_x, tiles_z, ntiles;
+  int G, ngroups;  // shots per unit / units per tile
+  int blocks;      // launch width (persistent kernels)
+  int64_t o_trb, o_trc, o_tri, o_tcb, o_tcc, o_tcr, o_cr;
+  int ncells;
+};
+
 struct adfwi_acoustic_plan {
   adfwi_acoustic_desc d;
   int nzp, nxp, fs, zbeg;
-  int tiles_x, tiles_z, ntiles;
-  int G, ngroups;
+  Tiling t1;             // 16 x 32 tiles of the adjoint step
+  Tiling t2;             // 16 x 64 tiles of the TMA forward step
   int K, nseg;           // snapshot interval and number of segments (gradient mode)
   int last_chunk_start;  // first step of the reference's last checkpoint chunk
   int elem;              // bytes per element
   Layout L;
   std::vector<int32_t> tab;  // geometry tables, uploaded into the workspace
-  int64_t o_srcz, o_srcx, o_trb, o_trc, o_tri, o_tcb, o_tcc, o_tcr, o_cr;
-  int ncells;
+  int64_t o_srcz, o_srcx;
 };
 
 namespace {
 
 struct Carve {
-  int64_t coef, fa, fb, ilp, ilu, tab;  // forward
+  int64_t coef, fa, fb, ilp, ilu, tab, flag;  // forward
   int64_t snap, snap_scale, hp, hd, la, lb, g1, g2;  // gradient extras
   int64_t total;
 };
@@ -561,9 +573,10 @@ Carve carve(const adfwi_acoustic_plan* p, bool grad, int K) {
   c.coef = take(3 * pl);
   c.fa = take(3 * ns * pl);
   c.fb = take(3 * ns * pl);
-  c.ilp = take((int64_t)p->ngroups * pl);
-  c.ilu = take((int64_t)p->ngroups * pl);
+  c.ilp = take((int64_t)p->t2.ngroups * pl);
+  c.ilu = take((int64_t)p->t2.ngroups * pl);
   c.tab = take((int64_t)p->tab.size() * 4);
+  c.flag = take(256);
   if (grad) {
     const int nseg = (p->d.nt + K - 1) / K;
     const bool full = K >= p->d.nt;
@@ -574,8 +587,8 @@ Carve carve(const adfwi_acoustic_plan* p, bool grad, int K) {
     c.hd = take((int64_t)K * ns * pl);
     c.la = take(3 * ns * pl);
     c.lb = take(3 * ns * pl);
-    c.g1 = take((int64_t)p->ngroups * pl);
-    c.g2 = take((int64_t)p->ngroups * pl);
+    c.g1 = take((int64_t)p->t1.ngroups * pl);
+    c.g2 = take((int64_t)p->t1.ngroups * pl);
   }
   c.total = o;
   return c;
@@ -604,7 +617,7 @@ int choose_K(const adfwi_acoustic_plan* p) {
 }
 
 template <typename T>
-ac::Geo<T> make_geo(const adfwi_acoustic_plan* p, const unsigned char* ws, const Carve& c) {
+ac::Geo<T> make_geo(const adfwi_acoustic_plan* p, const unsigned char* ws, const Carve& c, const Tiling& t) {
   ac::Geo<T> g;
   g.L = p->L;
   g.ns = p->d.ns;
@@ -613,7 +626,7 @@ ac::Geo<T> make_geo(const adfwi_acoustic_plan* p, const unsigned char* ws, const
   g.fs = p->fs;
   g.fsurf = p->d.free_surface;
   g.zbeg = p->zbeg;
-  g.tiles_x = p->tiles_x;
+  g.tiles_x = t.tiles_x;
   g.nabc = p->d.nabc;
   g.nz = p->d.nz;
   g.nx = p->d.nx;
@@ -623,13 +636,13 @@ ac::Geo<T> make_geo(const adfwi_acoustic_plan* p, const unsigned char* ws, const
   const int32_t* tb = reinterpret_cast<const int32_t*>(ws + c.tab);
   g.src_z = tb + p->o_srcz;
   g.src_x = tb + p->o_srcx;
-  g.tile_rcv_beg = tb + p->o_trb;
-  g.trcv_cell = tb + p->o_trc;
-  g.trcv_id = tb + p->o_tri;
-  g.tile_cell_beg = tb + p->o_tcb;
-  g.tcell_cell = tb + p->o_tcc;
-  g.tcell_rbeg = tb + p->o_tcr;
-  g.cell_rcv = tb + p->o_cr;
+  g.tile_rcv_beg = tb + t.o_trb;
+  g.trcv_cell = tb + t.o_trc;
+  g.trcv_id = tb + t.o_tri;
+  g.tile_cell_beg = tb + t.o_tcb;
+  g.tcell_cell = tb + t.o_tcc;
+  g.tcell_rbeg = tb + t.o_tcr;
+  g.cell_rcv = tb + t.o_cr;
   return g;
 }
 
@@ -641,6 +654,7 @@ int setup_common(const adfwi_acoustic_plan* p, unsigned char* ws, const Carve& c
   const int64_t pl = p->L.plane * p->elem;
   // Zero coefficient planes (ghosts), field buffers and illumination partials.
   ADFWI_CUDA_TRY(cudaMemsetAsync(ws + c.coef, 0, c.tab - c.coef, st));
+  ADFWI_CUDA_TRY(cudaMemsetAsync(ws + c.flag, 0, 256, st));
   ADFWI_CUDA_TRY(cudaMemcpyAsync(ws + c.tab, p->tab.data(), p->tab.size() * 4, cudaMemcpyHostToDevice, st));
   const int64_t n = (int64_t)p->nzp * p->nxp;
   T* cf = reinterpret_cast<T*>(ws + c.coef);
@@ -655,14 +669,44 @@ int setup_common(const adfwi_acoustic_plan* p, unsigned char* ws, const Carve& c
 }
 
 template <typename T>
-void launch_fwd(const adfwi_acoustic_plan* p, const ac::Geo<T>& g, int it, int accum_u, const T* cf,
-                const T* wav, const T* p0, const T* u0, const T* w0, T* p1, T* u1, T* w1, T* d1,
-                T* rp, T* ru, T* rw, T* ilp, T* ilu, cudaStream_t st) {
-  const int64_t pl = p->L.plane;
-  dim3 grid(p->tiles_x, p->tiles_z, p->ngroups);
-  dim3 block(ac::TX, ac::BY);
-  ADFWI_LAUNCH(kAcFwdStep, st, (ac::fwd_step<T><<<grid, block, sizeof(ac::FwdSmem<T>), st>>>(
-      g, it, p->G, accum_u, cf, cf + pl, cf + 2 * pl, wav, p0, u0, w0, p1, u1, w1, d1, rp, ru, rw, ilp, ilu)));
+int tma_stages() {
+  return sizeof(T) == 8 ? 2 : 3;
+}
+
+template <typename T>
+int launch_fwd(const adfwi_acoustic_plan* p, const ac::Geo<T>& g, int it, int accum_u, const T* cf,
+               const T* wav, const T* p0, const T* u0, const T* w0, T* p1, T* u1, T* w1, T* d1, T* rp, T* ru,
+               T* rw, T* ilp, T* ilu, int* flag, cudaStream_t st) {
+  const Tiling& t = p->t2;
+  const int64_t ns = p->d.ns;
+  ac2::Maps maps;
+  int rc = make_plane_map(&maps.u, u0, sizeof(T), p->L, ns, ac2::BOXX, ac2::EZ);
+  if (!rc) rc = make_plane_map(&maps.w, w0, sizeof(T), p->L, ns, ac2::BOXX, ac2::WZ);
+  if (!rc) rc = make_plane_map(&maps.p, p0, sizeof(T), p->L, ns, ac2::BOXX, ac2::EZ);
+  if (!rc) rc = make_plane_map(&maps.coef, cf, sizeof(T), p->L, 3, ac2::BOXX, ac2::EZ);
+  if (rc) return rc;
+  ac2::FwdArgs<T> a;
+  a.it = it;
+  a.G = t.G;
+  a.ngroups = t.ngroups;
+  a.ntiles = t.ntiles;
+  a.accum_u = accum_u;
+  a.stages = tma_stages<T>();
+  a.wav = wav;
+  a.p1 = p1;
+  a.u1 = u1;
+  a.w1 = w1;
+  a.d1 = d1;
+  a.rec_p = rp;
+  a.rec_u = ru;
+  a.rec_w = rw;
+  a.ill_p = ilp;
+  a.ill_u = ilu;
+  a.flag = flag;
+  const int smem = ac2::FwdLayout<T>::bytes(a.stages);
+  ADFWI_LAUNCH(kAcFwdStep, st,
+               (ac2::fwd_step_tma<T><<<t.blocks, ac2::NTHREADS, smem, st>>>(maps, g, a)));
+  return kOk;
 }
 
 template <typename T>
@@ -673,6 +717,8 @@ int set_smem_limits() {
                                         (int)sizeof(ac::FwdSmem<T>)));
     ADFWI_CUDA_TRY(cudaFuncSetAttribute(ac::adj_step<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)sizeof(ac::AdjSmem<T>)));
+    ADFWI_CUDA_TRY(cudaFuncSetAttribute(ac2::fwd_step_tma<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        ac2::FwdLayout<T>::bytes(tma_stages<T>())));
     done = true;
   }
   return kOk;
@@ -692,7 +738,7 @@ int forward_impl(const adfwi_acoustic_plan* p, const void* alpha1, const void* a
   }
   rc = setup_common<T>(p, ws, c, alpha1, alpha2, damp, st);
   if (rc) return rc;
-  ac::Geo<T> g = make_geo<T>(p, ws, c);
+  ac::Geo<T> g = make_geo<T>(p, ws, c, p->t2);
   const int64_t pl = p->L.plane;
   const int64_t ns = p->d.ns;
   const T* cf = reinterpret_cast<const T*>(ws + c.coef);
@@ -700,6 +746,7 @@ int forward_impl(const adfwi_acoustic_plan* p, const void* alpha1, const void* a
   T* fb = reinterpret_cast<T*>(ws + c.fb);
   T* ilp = reinterpret_cast<T*>(ws + c.ilp);
   T* ilu = reinterpret_cast<T*>(ws + c.ilu);
+  int* flag = reinterpret_cast<int*>(ws + c.flag);
   const T* wav = static_cast<const T*>(wavelet);
   const bool full = grad && K >= p->d.nt;
   T* hp = grad ? reinterpret_cast<T*>(ws + c.hp) : nullptr;
@@ -708,29 +755,32 @@ int forward_impl(const adfwi_acoustic_plan* p, const void* alpha1, const void* a
   T* nxt = fb;
   for (int it = 0; it < p->d.nt; ++it) {
     if (grad && !full && it % K == 0) {
-      int rc2 = snapshot_store<T>(p->d.snapshot_precision, cur, 3 * ns, pl, ws + c.snap, ws + c.snap_scale,
-                                  (int64_t)(it / K) * 3 * ns, st);
-      if (rc2) return rc2;
+      rc = snapshot_store<T>(p->d.snapshot_precision, cur, 3 * ns, pl, ws + c.snap, ws + c.snap_scale,
+                             (int64_t)(it / K) * 3 * ns, st);
+      if (rc) return rc;
     }
     const T* p0 = cur;
     T* p1 = nxt;
     T* d1 = nullptr;
     if (full) {
+      // the whole pressure history doubles as the pressure ping-pong buffer
       p0 = it == 0 ? cur : hp + (int64_t)(it - 1) * ns * pl;
       p1 = hp + (int64_t)it * ns * pl;
       d1 = hd + (int64_t)it * ns * pl;
     }
-    launch_fwd<T>(p, g, it, it >= p->last_chunk_start ? 1 : 0, cf, wav, p0, cur + ns * pl, cur + 2 * ns * pl, p1,
-                  nxt + ns * pl, nxt + 2 * ns * pl, d1, static_cast<T*>(rec_p), static_cast<T*>(rec_u),
-                  static_cast<T*>(rec_w), ilp, ilu, st);
+    rc = launch_fwd<T>(p, g, it, it >= p->last_chunk_start ? 1 : 0, cf, wav, p0, cur + ns * pl, cur + 2 * ns * pl,
+                       p1, nxt + ns * pl, nxt + 2 * ns * pl, d1, static_cast<T*>(rec_p), static_cast<T*>(rec_u),
+                       static_cast<T*>(rec_w), ilp, ilu, flag, st);
+    if (rc) return rc;
     std::swap(cur, nxt);
   }
   ADFWI_CUDA_TRY(cudaGetLastError());
   if (fw_p || fw_u || fw_w) {
     const int64_t n = (int64_t)p->d.nz * p->d.nx;
     ADFWI_LAUNCH(kAux, st, (ac::illum_finalize<T><<<grid_blocks(n), 256, 0, st>>>(
-                                p->L, p->ngroups, p->d.ns, p->d.nabc, p->d.nz, p->d.nx, ilp, ilu, cur + 2 * ns * pl,
-                                static_cast<T*>(fw_p), static_cast<T*>(fw_u), static_cast<T*>(fw_w))));
+                                p->L, p->t2.ngroups, p->d.ns, p->d.nabc, p->d.nz, p->d.nx, ilp, ilu,
+                                cur + 2 * ns * pl, static_cast<T*>(fw_p), static_cast<T*>(fw_u),
+                                static_cast<T*>(fw_w))));
     ADFWI_CUDA_TRY(cudaGetLastError());
   }
   return kOk;
@@ -747,7 +797,8 @@ int backward_impl(const adfwi_acoustic_plan* p, const void* wavelet, const void*
     set_error("workspace too small: %lld bytes given, %lld needed", (long long)ws_bytes, (long long)c.total);
     return kWorkspaceTooSmall;
   }
-  ac::Geo<T> g = make_geo<T>(p, ws, c);
+  ac::Geo<T> g2 = make_geo<T>(p, ws, c, p->t2);  // recomputation (TMA forward step)
+  ac::Geo<T> g1 = make_geo<T>(p, ws, c, p->t1);  // adjoint step
   const int64_t pl = p->L.plane;
   const int64_t ns = p->d.ns;
   const int nt = p->d.nt;
@@ -759,8 +810,9 @@ int backward_impl(const adfwi_acoustic_plan* p, const void* wavelet, const void*
   T* hd = reinterpret_cast<T*>(ws + c.hd);
   T* la = reinterpret_cast<T*>(ws + c.la);
   T* lb = reinterpret_cast<T*>(ws + c.lb);
-  T* g1 = reinterpret_cast<T*>(ws + c.g1);
-  T* g2 = reinterpret_cast<T*>(ws + c.g2);
+  T* g1p = reinterpret_cast<T*>(ws + c.g1);
+  T* g2p = reinterpret_cast<T*>(ws + c.g2);
+  int* flag = reinterpret_cast<int*>(ws + c.flag);
   const T* wav = static_cast<const T*>(wavelet);
   const T* gp = static_cast<const T*>(grp);
   const T* gu = static_cast<const T*>(gru);
@@ -768,52 +820,150 @@ int backward_impl(const adfwi_acoustic_plan* p, const void* wavelet, const void*
 
   ADFWI_CUDA_TRY(cudaMemsetAsync(la, 0, 3 * ns * pl * sizeof(T), st));
   ADFWI_CUDA_TRY(cudaMemsetAsync(lb, 0, 3 * ns * pl * sizeof(T), st));
-  ADFWI_CUDA_TRY(cudaMemsetAsync(g1, 0, (size_t)p->ngroups * pl * sizeof(T), st));
-  ADFWI_CUDA_TRY(cudaMemsetAsync(g2, 0, (size_t)p->ngroups * pl * sizeof(T), st));
+  ADFWI_CUDA_TRY(cudaMemsetAsync(g1p, 0, (size_t)p->t1.ngroups * pl * sizeof(T), st));
+  ADFWI_CUDA_TRY(cudaMemsetAsync(g2p, 0, (size_t)p->t1.ngroups * pl * sizeof(T), st));
   if (gp || gu || gw) {
-    dim3 sg(std::max(1, std::min(64, (p->ncells + 127) / 128)), p->d.ns);
-    ADFWI_LAUNCH(kAux, st, (ac::adj_seed<T><<<sg, 128, 0, st>>>(g, p->ntiles, gp, gu, gw, la, la + ns * pl,
+    dim3 sg(std::max(1, std::min(64, (p->t1.ncells + 127) / 128)), p->d.ns);
+    ADFWI_LAUNCH(kAux, st, (ac::adj_seed<T><<<sg, 128, 0, st>>>(g1, p->t1.ntiles, gp, gu, gw, la, la + ns * pl,
                                                                    la + 2 * ns * pl)));
   }
   T* lcur = la;
   T* lnxt = lb;
   const int nseg = full ? 1 : (nt + K - 1) / K;
-  dim3 grid(p->tiles_x, p->tiles_z, p->ngroups);
+  dim3 grid(p->t1.tiles_x, p->t1.tiles_z, p->t1.ngroups);
   dim3 block(ac::TX, ac::BY);
   for (int seg = nseg - 1; seg >= 0; --seg) {
     const int t0 = full ? 0 : seg * K;
     const int t1 = full ? nt : std::min(nt, t0 + K);
     if (!full) {
       // Recompute the segment from its snapshot, keeping p and the divergence of every step.
-      int rc2 = snapshot_load<T>(p->d.snapshot_precision, fa, 3 * ns, pl, ws + c.snap, ws + c.snap_scale,
-                                 (int64_t)seg * 3 * ns, st);
-      if (rc2) return rc2;
+      rc = snapshot_load<T>(p->d.snapshot_precision, fa, 3 * ns, pl, ws + c.snap, ws + c.snap_scale,
+                            (int64_t)seg * 3 * ns, st);
+      if (rc) return rc;
       T* cur = fa;
       T* nxt = fb;
       for (int it = t0; it < t1; ++it) {
         const T* p0 = it == t0 ? fa : hp + (int64_t)(it - 1 - t0) * ns * pl;
-        launch_fwd<T>(p, g, it, 0, cf, wav, p0, cur + ns * pl, cur + 2 * ns * pl, hp + (int64_t)(it - t0) * ns * pl,
-                      nxt + ns * pl, nxt + 2 * ns * pl, hd + (int64_t)(it - t0) * ns * pl, nullptr, nullptr,
-                      nullptr, nullptr, nullptr, st);
+        rc = launch_fwd<T>(p, g2, it, 0, cf, wav, p0, cur + ns * pl, cur + 2 * ns * pl,
+                           hp + (int64_t)(it - t0) * ns * pl, nxt + ns * pl, nxt + 2 * ns * pl,
+                           hd + (int64_t)(it - t0) * ns * pl, nullptr, nullptr, nullptr, nullptr, nullptr, flag, st);
+        if (rc) return rc;
         std::swap(cur, nxt);
       }
     }
     for (int it = t1 - 1; it >= t0; --it) {
       ADFWI_LAUNCH(kAcAdjStep, st, (ac::adj_step<T><<<grid, block, sizeof(ac::AdjSmem<T>), st>>>(
-          g, it, p->G, cf, cf + pl, cf + 2 * pl, lcur, lcur + ns * pl, lcur + 2 * ns * pl, lnxt, lnxt + ns * pl,
-          lnxt + 2 * ns * pl, hp + (int64_t)(it - t0) * ns * pl, hd + (int64_t)(it - t0) * ns * pl, gp, gu, gw, g1,
-          g2)));
+          g1, it, p->t1.G, cf, cf + pl, cf + 2 * pl, lcur, lcur + ns * pl, lcur + 2 * ns * pl, lnxt, lnxt + ns * pl,
+          lnxt + 2 * ns * pl, hp + (int64_t)(it - t0) * ns * pl, hd + (int64_t)(it - t0) * ns * pl, gp, gu, gw, g1p,
+          g2p)));
       std::swap(lcur, lnxt);
     }
     ADFWI_CUDA_TRY(cudaGetLastError());
   }
   const int64_t n = (int64_t)p->nzp * p->nxp;
-  ADFWI_LAUNCH(kAux, st, (ac::reduce_planes<T><<<grid_blocks(n), 256, 0, st>>>(p->L, p->ngroups, 0, 0, p->nzp,
-                                                                                p->nxp, g1, static_cast<T*>(ga1))));
-  ADFWI_LAUNCH(kAux, st, (ac::reduce_planes<T><<<grid_blocks(n), 256, 0, st>>>(p->L, p->ngroups, 0, 0, p->nzp,
-                                                                                p->nxp, g2, static_cast<T*>(ga2))));
+  ADFWI_LAUNCH(kAux, st, (ac::reduce_planes<T><<<grid_blocks(n), 256, 0, st>>>(p->L, p->t1.ngroups, 0, 0, p->nzp,
+                                                                                p->nxp, g1p, static_cast<T*>(ga1))));
+  ADFWI_LAUNCH(kAux, st, (ac::reduce_planes<T><<<grid_blocks(n), 256, 0, st>>>(p->L, p->t1.ngroups, 0, 0, p->nzp,
+                                                                                p->nxp, g2p, static_cast<T*>(ga2))));
   ADFWI_CUDA_TRY(cudaGetLastError());
   return kOk;
+}
+
+// Resident blocks of the TMA forward step on the current device (152 SMs x 2 without a GPU).
+template <typename T>
+int resident_tma_blocks() {
+  int dev = 0, sms = 0, occ = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+    cudaGetLastError();
+    return 152 * (sizeof(T) == 8 ? 1 : 2);
+  }
+  const int smem = ac2::FwdLayout<T>::bytes(tma_stages<T>());
+  if (cudaFuncSetAttribute(ac2::fwd_step_tma<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, ac2::fwd_step_tma<T>, ac2::NTHREADS, smem) != cudaSuccess ||
+      occ < 1) {
+    cudaGetLastError();
+    return 152 * (sizeof(T) == 8 ? 1 : 2);
+  }
+  return sms * occ;
+}
+
+// Shots per unit for the persistent TMA kernels: balance the units over the resident blocks
+// (the block with the most units sets the time) against the per-unit flush of the partial
+// accumulator planes (about half an item's worth of traffic).
+int pick_unit_shots(int ns, int ntiles, int blocks) {
+  int best = 1;
+  double best_cost = 1e30;
+  for (int G = 1; G <= ns; ++G) {
+    const int groups = (ns + G - 1) / G;
+    const long long units = (long long)ntiles * groups;
+    const long long per = (units + blocks - 1) / blocks;
+    const double cost = (double)per * (G + 0.5);
+    if (cost < best_cost - 1e-9) {
+      best_cost = cost;
+      best = G;
+    }
+  }
+  return best;
+}
+
+// Tile the grid and build the receiver tables of that tiling (appended to p->tab).
+void build_tiling(adfwi_acoustic_plan* p, Tiling* tl, int tz, int tx, int G, const int32_t* rcv_z,
+                  const int32_t* rcv_x) {
+  const adfwi_acoustic_desc& d = p->d;
+  std::vector<int32_t>& t = p->tab;
+  tl->tz = tz;
+  tl->tx = tx;
+  tl->tiles_x = (p->nxp + tx - 1) / tx;
+  tl->tiles_z = (p->nzp - p->zbeg + tz - 1) / tz;
+  tl->ntiles = tl->tiles_x * tl->tiles_z;
+  tl->G = std::max(1, std::min(G, d.ns));
+  tl->ngroups = (d.ns + tl->G - 1) / tl->G;
+  tl->blocks = 0;
+  struct R {
+    int tile, cell, id;
+  };
+  std::vector<R> rs(d.nr);
+  for (int r = 0; r < d.nr; ++r) {
+    int z = rcv_z[r] + d.nabc - p->zbeg, x = rcv_x[r] + d.nabc;
+    rs[r].tile = (z / tz) * tl->tiles_x + x / tx;
+    rs[r].cell = ((z % tz) << 16) | (x % tx);
+    rs[r].id = r;
+  }
+  std::stable_sort(rs.begin(), rs.end(), [](const R& a, const R& b) {
+    return a.tile != b.tile ? a.tile < b.tile : a.cell < b.cell;
+  });
+  tl->o_trb = t.size();
+  {
+    std::vector<int32_t> beg(tl->ntiles + 1, 0);
+    for (const R& r : rs) beg[r.tile + 1]++;
+    for (int q = 0; q < tl->ntiles; ++q) beg[q + 1] += beg[q];
+    t.insert(t.end(), beg.begin(), beg.end());
+  }
+  tl->o_trc = t.size();
+  for (const R& r : rs) t.push_back(r.cell);
+  tl->o_tri = t.size();
+  for (const R& r : rs) t.push_back(r.id);
+  std::vector<int32_t> tcb(tl->ntiles + 1, 0), tcc, tcr, cr;
+  for (size_t q = 0; q < rs.size(); ++q) {
+    bool fresh = q == 0 || rs[q].tile != rs[q - 1].tile || rs[q].cell != rs[q - 1].cell;
+    if (fresh) {
+      tcb[rs[q].tile + 1]++;
+      tcc.push_back(rs[q].cell);
+      tcr.push_back((int32_t)cr.size());
+    }
+    cr.push_back(rs[q].id);
+  }
+  tcr.push_back((int32_t)cr.size());
+  for (int q = 0; q < tl->ntiles; ++q) tcb[q + 1] += tcb[q];
+  tl->ncells = (int)tcc.size();
+  tl->o_tcb = t.size();
+  t.insert(t.end(), tcb.begin(), tcb.end());
+  tl->o_tcc = t.size();
+  t.insert(t.end(), tcc.begin(), tcc.end());
+  tl->o_tcr = t.size();
+  t.insert(t.end(), tcr.begin(), tcr.end());
+  tl->o_cr = t.size();
+  t.insert(t.end(), cr.begin(), cr.end());
 }
 
 // ----------------------------------------------------------------------------------------
@@ -903,23 +1053,11 @@ int adfwi_acoustic_plan_create(const adfwi_acoustic_desc* desc, const int32_t* s
   p->fs = d.free_surface ? d.nabc : 1;
   p->zbeg = d.free_surface ? p->fs - 1 : 0;
   p->elem = d.dtype == ADFWI_F64 ? 8 : 4;
-  p->L = make_layout(p->nzp, p->nxp, ac::TZ, ac::TX, p->elem);
-  p->tiles_x = (p->nxp + ac::TX - 1) / ac::TX;
-  p->tiles_z = (p->nzp - p->zbeg + ac::TZ - 1) / ac::TZ;
-  p->ntiles = p->tiles_x * p->tiles_z;
+  p->L = make_layout(p->nzp, p->nxp, ac2::TZ, ac2::TX, p->elem);
   // torch.chunk(wavelet, checkpoint_segments): chunks of ceil(nt / segments) steps.
   const int chunk = (d.nt + d.checkpoint_segments - 1) / d.checkpoint_segments;
   const int nchunks = (d.nt + chunk - 1) / chunk;
   p->last_chunk_start = (nchunks - 1) * chunk;
-  // Shots per block: enough blocks to fill the GPU (about 8 resident per SM).
-  int G = d.shots_per_block;
-  if (G <= 0) {
-    const int want_groups = std::max(1, (152 * 8 + p->ntiles - 1) / p->ntiles);
-    const int groups = std::min(d.ns, want_groups);
-    G = (d.ns + groups - 1) / groups;
-  }
-  p->G = std::max(1, std::min(G, d.ns));
-  p->ngroups = (d.ns + p->G - 1) / p->G;
 
   // Geometry tables.
   std::vector<int32_t>& t = p->tab;
@@ -935,8 +1073,6 @@ int adfwi_acoustic_plan_create(const adfwi_acoustic_desc* desc, const int32_t* s
   }
   p->o_srcx = t.size();
   for (int s = 0; s < d.ns; ++s) t.push_back(src_x[s] + d.nabc);
-  struct R { int tile, cell, id; };
-  std::vector<R> rs(d.nr);
   for (int r = 0; r < d.nr; ++r) {
     int z = rcv_z[r] + d.nabc, x = rcv_x[r] + d.nabc;
     // u has nxp-1 columns and w has nzp-1 rows (acoustic_kernels.py:241-242, 167-169)
@@ -945,47 +1081,26 @@ int adfwi_acoustic_plan_create(const adfwi_acoustic_desc* desc, const int32_t* s
       delete p;
       return kBadGeometry;
     }
-    int lz = z - p->zbeg;
-    rs[r].tile = (lz / ac::TZ) * p->tiles_x + x / ac::TX;
-    rs[r].cell = ((lz % ac::TZ) << 16) | (x % ac::TX);
-    rs[r].id = r;
   }
-  std::stable_sort(rs.begin(), rs.end(), [](const R& a, const R& b) {
-    return a.tile != b.tile ? a.tile < b.tile : a.cell < b.cell;
-  });
-  p->o_trb = t.size();
+  // 16 x 32 tiles (adjoint step): enough blocks to fill the GPU (about 8 resident per SM).
+  int G1 = d.shots_per_block;
   {
-    std::vector<int32_t> beg(p->ntiles + 1, 0);
-    for (const R& r : rs) beg[r.tile + 1]++;
-    for (int q = 0; q < p->ntiles; ++q) beg[q + 1] += beg[q];
-    t.insert(t.end(), beg.begin(), beg.end());
-  }
-  p->o_trc = t.size();
-  for (const R& r : rs) t.push_back(r.cell);
-  p->o_tri = t.size();
-  for (const R& r : rs) t.push_back(r.id);
-  // unique cells per tile
-  std::vector<int32_t> tcb(p->ntiles + 1, 0), tcc, tcr, cr;
-  for (size_t q = 0; q < rs.size(); ++q) {
-    bool fresh = q == 0 || rs[q].tile != rs[q - 1].tile || rs[q].cell != rs[q - 1].cell;
-    if (fresh) {
-      tcb[rs[q].tile + 1]++;
-      tcc.push_back(rs[q].cell);
-      tcr.push_back((int32_t)cr.size());
+    const int ntiles = ((p->nxp + ac::TX - 1) / ac::TX) * ((p->nzp - p->zbeg + ac::TZ - 1) / ac::TZ);
+    if (G1 <= 0) {
+      const int groups = std::min(d.ns, std::max(1, (152 * 8 + ntiles - 1) / ntiles));
+      G1 = (d.ns + groups - 1) / groups;
     }
-    cr.push_back(rs[q].id);
   }
-  tcr.push_back((int32_t)cr.size());
-  for (int q = 0; q < p->ntiles; ++q) tcb[q + 1] += tcb[q];
-  p->ncells = (int)tcc.size();
-  p->o_tcb = t.size();
-  t.insert(t.end(), tcb.begin(), tcb.end());
-  p->o_tcc = t.size();
-  t.insert(t.end(), tcc.begin(), tcc.end());
-  p->o_tcr = t.size();
-  t.insert(t.end(), tcr.begin(), tcr.end());
-  p->o_cr = t.size();
-  t.insert(t.end(), cr.begin(), cr.end());
+  build_tiling(p, &p->t1, ac::TZ, ac::TX, G1, rcv_z, rcv_x);
+  // 16 x 64 tiles (TMA forward step): units of G shots spread over the resident blocks.
+  {
+    const int ntiles = ((p->nxp + ac2::TX - 1) / ac2::TX) * ((p->nzp - p->zbeg + ac2::TZ - 1) / ac2::TZ);
+    const int blocks = p->elem == 8 ? resident_tma_blocks<double>() : resident_tma_blocks<float>();
+    int G2 = d.shots_per_block;
+    if (G2 <= 0) G2 = pick_unit_shots(d.ns, ntiles, blocks);
+    build_tiling(p, &p->t2, ac2::TZ, ac2::TX, G2, rcv_z, rcv_x);
+    p->t2.blocks = std::max(1, std::min(blocks, p->t2.ntiles * p->t2.ngroups));
+  }
   if (t.empty()) t.push_back(0);
 
   p->K = choose_K(p);
@@ -995,6 +1110,20 @@ int adfwi_acoustic_plan_create(const adfwi_acoustic_desc* desc, const int32_t* s
 }
 
 void adfwi_acoustic_plan_destroy(adfwi_acoustic_plan* plan) { delete plan; }
+
+int adfwi_acoustic_status(const adfwi_acoustic_plan* p, const void* workspace, int64_t workspace_bytes,
+                          int32_t with_gradient, int32_t* status, void* stream) {
+  ADFWI_CHECK_ARG(p && workspace && status, "null argument");
+  Carve c = carve(p, with_gradient != 0, with_gradient ? p->K : 1);
+  ADFWI_CHECK_ARG(workspace_bytes >= c.total, "workspace smaller than the plan's layout");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  int32_t v = 0;
+  ADFWI_CUDA_TRY(cudaMemcpyAsync(&v, static_cast<const unsigned char*>(workspace) + c.flag, sizeof(v),
+                                 cudaMemcpyDeviceToHost, st));
+  ADFWI_CUDA_TRY(cudaStreamSynchronize(st));
+  *status = v;
+  return kOk;
+}
 
 int adfwi_acoustic_workspace_bytes(const adfwi_acoustic_plan* p, int32_t with_gradient, int64_t* bytes) {
   ADFWI_CHECK_ARG(p && bytes, "null plan or output pointer");

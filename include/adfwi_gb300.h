@@ -100,6 +100,13 @@ int adfwi_acoustic_backward(const adfwi_acoustic_plan* plan, const void* alpha1,
                             const void* grad_rec_w, void* grad_alpha1, void* grad_alpha2,
                             void* workspace, int64_t workspace_bytes, void* stream);
 
+/* Device status of the last solve run in `workspace` (same with_gradient as that solve):
+ * 0 = clean, 1 = a bounded pipeline wait inside a kernel ran out (results invalid).
+ * Waits for the stream. */
+int adfwi_acoustic_status(const adfwi_acoustic_plan* plan, const void* workspace,
+                          int64_t workspace_bytes, int32_t with_gradient, int32_t* status,
+                          void* stream);
+
 /* Forward solve that allocates nothing, for callers that cannot call cudaMalloc: hosts whose
  * device memory is entirely owned by another allocator or pool, sandboxed plug-ins that may
  * not grow their footprint after start-up, or code running where an allocation would break

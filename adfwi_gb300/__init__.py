@@ -10,6 +10,6 @@ from .model import AbstractModel, AcousticModel, AnisotropicElasticModel, Isotro
 from .survey import Receiver, SeismicData, Source, Survey  # noqa: F401
 from .utils import wavelet, numpy2tensor, tensor2numpy, gpu2cpu, list2numpy, numpy2list  # noqa: F401
 from .boundary import bc_pml, bc_pml_xz, bc_gerjan, bc_sincos  # noqa: F401
-from .propagator import AcousticPropagator  # noqa: F401
+from .propagator import AcousticPropagator, ElasticPropagator  # noqa: F401
 
 __version__ = "0.1.0"

@@ -32,9 +32,9 @@ class ElasticDesc(ctypes.Structure):
         ("nz", c_int32), ("nx", c_int32), ("nabc", c_int32), ("free_surface", c_int32),
         ("ns", c_int32), ("nt", c_int32), ("nr", c_int32), ("dtype", c_int32),
         ("fd_order", c_int32), ("pml", c_int32), ("checkpoint_segments", c_int32),
-        ("snapshot_every", c_int32), ("snapshot_precision", c_int32), ("shots_per_block", c_int32),
+        ("snapshot_every", c_int32), ("snapshot_precision", c_int32), ("reserved", c_int32),
         ("dt", ctypes.c_double), ("dx", ctypes.c_double), ("dz", ctypes.c_double),
-        ("memory_budget", c_int64),
+        ("fdc", ctypes.c_double * 3), ("memory_budget", c_int64),
     ]
 
 
@@ -64,15 +64,16 @@ def _bind(lib):
         "adfwi_launch_count": (c_int64, []),
         "adfwi_version": (ctypes.c_char_p, []),
     }
-    optional = {
-        "adfwi_elastic_plan_create": (c_int32, [ctypes.POINTER(ElasticDesc), P, P, P, P,
+    optional = {}
+    sig.update({
+        "adfwi_elastic_plan_create": (c_int32, [ctypes.POINTER(ElasticDesc), P, P, P, P, P,
                                                 ctypes.POINTER(c_void_p)]),
         "adfwi_elastic_plan_destroy": (None, [P]),
         "adfwi_elastic_workspace_bytes": (c_int32, [P, c_int32, ctypes.POINTER(c_int64)]),
         "adfwi_elastic_snapshot_every": (c_int32, [P, ctypes.POINTER(c_int32)]),
         "adfwi_elastic_forward": (c_int32, [P, P, P, P, P, P, c_int32, P, c_int64, P]),
-        "adfwi_elastic_backward": (c_int32, [P, P, P, P, P, c_int64, P]),
-    }
+        "adfwi_elastic_backward": (c_int32, [P, P, P, P, P, P, c_int64, P]),
+    })
     for name, (res, args) in list(sig.items()) + list(optional.items()):
         fn = getattr(lib, name, None)
         if fn is None:

@@ -1,0 +1,1261 @@
+// 2-D velocity-stress elastic propagator (vx, vz, txx, tzz, txz), 4th / 6th order staggered
+// grid, split-field PML or multiplicative absorbing layer, free surface, moment-tensor
+// sources, 5-component receivers; exact discrete adjoint for the coefficient gradients;
+// checkpoint / recompute driver and the C ABI.
+//
+// Reference algorithm (paths inside liufeng2317/ADFWI):
+//   ADFWI/propagator/elastic_kernels.py:20-108    DiffCoef and the half-cell operators Dxfm/Dxbm/Dzfm/Dzbm
+//   ADFWI/propagator/elastic_kernels.py:339-418   PML step (split stresses, source -MT/2 on both parts,
+//                                                 totals, free-surface rows h-3..h-1, split velocities,
+//                                                 totals, free-surface velocity rows, receivers, energy)
+//   ADFWI/propagator/elastic_kernels.py:709-774   absorbing-layer step (unsplit, -MT/3 source, v *= damp)
+//   ADFWI/propagator/elastic_kernels.py:917-1037  padding, index shifts, chunked loop, record dict
+//
+// One time step is a short sequence of launches, each a pointwise or gather stencil over
+// (cell, shot): the split fields are updated in place (every update reads only its own
+// cell of the field it writes), totals and free-surface rows are rebuilt from the split
+// fields. Gradient kernels handle one cell for every shot in a loop, so the coefficient
+// gradients are summed over shots in a fixed order (deterministic, no atomics). The
+// forward arithmetic uses explicitly rounded operations in the reference's order.
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string.h>
+
+#include <algorithm>
+#include <cmath>
+#include <new>
+#include <vector>
+
+#include "../../include/adfwi_gb300.h"
+#include "common.cuh"
+#include "snapshot.cuh"
+
+namespace adfwi {
+namespace el {
+
+__device__ __forceinline__ float radd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float rsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float rmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float rdiv(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ double radd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double rsub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double rmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double rdiv(double a, double b) { return __ddiv_rn(a, b); }
+
+// Field indices inside the state blocks (each field = ns consecutive planes).
+enum { TXX_X = 0, TXX_Z, TZZ_X, TZZ_Z, TXZ_X, TXZ_Z };  // split stresses (PML)
+enum { VX_X = 0, VX_Z, VZ_X, VZ_Z };                    // split velocities (PML)
+enum { TXX = 0, TZZ, TXZ };                             // stress totals / ABL stresses
+enum { VX = 0, VZ };                                    // velocity totals / ABL velocities
+enum { C11 = 0, C13, C15, C33, C35, C55, BX, BZ, BCX, BCZ, DAMP = 8 };  // coefficient planes
+
+template <typename T>
+struct Geo {
+  Layout L;
+  int ns, nt, nr;
+  int fsurf, h;                // free surface; h = NN + 1
+  int ilo, ihi, jlo, jhi;      // update region I = [NN, nzp-NN-1] x [NN, nxp-NN-1]
+  int top, nabc, nz, nx;       // energy window
+  T dt, dx, dz, dt_dx, dt_dz, hdt;
+  T f0, f1, f2;                // staggered coefficients
+  const int* src_z;
+  const int* src_x;
+  const T* src_m;              // ns x 3 source weights (xx, zz, xz) already scaled for the mode
+  const int* rcv_z;
+  const int* rcv_x;
+  const int* ucell_zx;         // unique receiver cells (i << 16 | j)
+  const int* ucell_beg;        // ncells+1 offsets into ucell_rcv
+  const int* ucell_rcv;
+  int ncells;
+};
+
+template <typename T>
+__device__ __forceinline__ bool in_I(const Geo<T>& g, int i, int j) {
+  return i >= g.ilo && i <= g.ihi && j >= g.jlo && j <= g.jhi;
+}
+
+// ---- half-cell differences (elastic_kernels.py:66-108): f_k (a[+1+k] - a[-k]) etc.
+template <int NN, typename T>
+__device__ __forceinline__ T dxf(const Geo<T>& g, const T* a, int64_t o) {
+  T r = rmul(g.f0, rsub(a[o + 1], a[o]));
+  r = radd(r, rmul(g.f1, rsub(a[o + 2], a[o - 1])));
+  if (NN == 3) r = radd(r, rmul(g.f2, rsub(a[o + 3], a[o - 2])));
+  return r;
+}
+template <int NN, typename T>
+__device__ __forceinline__ T dxb(const Geo<T>& g, const T* a, int64_t o) {
+  T r = rmul(g.f0, rsub(a[o], a[o - 1]));
+  r = radd(r, rmul(g.f1, rsub(a[o + 1], a[o - 2])));
+  if (NN == 3) r = radd(r, rmul(g.f2, rsub(a[o + 2], a[o - 3])));
+  return r;
+}
+template <int NN, typename T>
+__device__ __forceinline__ T dzf(const Geo<T>& g, const T* a, int64_t o) {
+  const int64_t P = g.L.pitch;
+  T r = rmul(g.f0, rsub(a[o + P], a[o]));
+  r = radd(r, rmul(g.f1, rsub(a[o + 2 * P], a[o - P])));
+  if (NN == 3) r = radd(r, rmul(g.f2, rsub(a[o + 3 * P], a[o - 2 * P])));
+  return r;
+}
+template <int NN, typename T>
+__device__ __forceinline__ T dzb(const Geo<T>& g, const T* a, int64_t o) {
+  const int64_t P = g.L.pitch;
+  T r = rmul(g.f0, rsub(a[o], a[o - P]));
+  r = radd(r, rmul(g.f1, rsub(a[o + P], a[o - 2 * P])));
+  if (NN == 3) r = radd(r, rmul(g.f2, rsub(a[o + 2 * P], a[o - 3 * P])));
+  return r;
+}
+
+// ---- transposes in gather form: contribution to cell (i, j) of q placed at the cells that
+// read (i, j). q(i', j') must be zero outside the update region.
+//   Dxf^T q (j) = sum_k f_k (q[j-1-k] - q[j+k]);   Dxb^T q (j) = sum_k f_k (q[j-k] - q[j+1+k])
+template <int NN, typename T, typename Q>
+__device__ __forceinline__ T dxf_t(const Geo<T>& g, const Q& q, int i, int j) {
+  T r = g.f0 * (q(i, j - 1) - q(i, j)) + g.f1 * (q(i, j - 2) - q(i, j + 1));
+  if (NN == 3) r += g.f2 * (q(i, j - 3) - q(i, j + 2));
+  return r;
+}
+template <int NN, typename T, typename Q>
+__device__ __forceinline__ T dxb_t(const Geo<T>& g, const Q& q, int i, int j) {
+  T r = g.f0 * (q(i, j) - q(i, j + 1)) + g.f1 * (q(i, j - 1) - q(i, j + 2));
+  if (NN == 3) r += g.f2 * (q(i, j - 2) - q(i, j + 3));
+  return r;
+}
+template <int NN, typename T, typename Q>
+__device__ __forceinline__ T dzf_t(const Geo<T>& g, const Q& q, int i, int j) {
+  T r = g.f0 * (q(i - 1, j) - q(i, j)) + g.f1 * (q(i - 2, j) - q(i + 1, j));
+  if (NN == 3) r += g.f2 * (q(i - 3, j) - q(i + 2, j));
+  return r;
+}
+template <int NN, typename T, typename Q>
+__device__ __forceinline__ T dzb_t(const Geo<T>& g, const Q& q, int i, int j) {
+  T r = g.f0 * (q(i, j) - q(i + 1, j)) + g.f1 * (q(i - 1, j) - q(i + 2, j));
+  if (NN == 3) r += g.f2 * (q(i - 2, j) - q(i + 3, j));
+  return r;
+}
+
+#define EL_CELL_SHOT                                                                 \
+  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;                  \
+  if (e >= (int64_t)g.L.nzp * g.L.nxp) return;                                      \
+  const int i = (int)(e / g.L.nxp), j = (int)(e - (int64_t)i * g.L.nxp);            \
+  const int s = blockIdx.y;                                                          \
+  const int64_t PL = g.L.plane, NSP = (int64_t)g.ns * PL;                            \
+  const int64_t o = (int64_t)s * PL + g.L.off(i, j);                                 \
+  (void)NSP;
+
+#define EL_CELL                                                                      \
+  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;                  \
+  if (e >= (int64_t)g.L.nzp * g.L.nxp) return;                                      \
+  const int i = (int)(e / g.L.nxp), j = (int)(e - (int64_t)i * g.L.nxp);            \
+  const int64_t PL = g.L.plane, NSP = (int64_t)g.ns * PL;                            \
+  const int64_t oc = g.L.off(i, j);
+
+// ======================================================================= forward, PML
+// Split stresses in I (elastic_kernels.py:351-356), then the moment-tensor source on both
+// split parts (359-372). ts: 6 fields; v: vx, vz totals at the start of the step.
+template <typename T, int NN>
+__global__ void stress_pml(Geo<T> g, int it, const T* __restrict__ cf, const T* __restrict__ v, T* __restrict__ ts,
+                           const T* __restrict__ wav) {
+  EL_CELL_SHOT
+  const int64_t occ = g.L.off(i, j);
+  if (in_I(g, i, j)) {
+    const T* vx = v;
+    const T* vz = v + NSP;
+    const T dxbm_vx = dxb<NN>(g, vx, o), dxbm_vz = dxb<NN>(g, vz, o);
+    const T dzbm_vx = dzb<NN>(g, vx, o), dzbm_vz = dzb<NN>(g, vz, o);
+    const T dxfm_vx = dxf<NN>(g, vx, o), dzfm_vx = dzf<NN>(g, vx, o);
+    const T dxfm_vz = dxf<NN>(g, vz, o), dzfm_vz = dzf<NN>(g, vz, o);
+    const T bcx = cf[BCX * PL + occ], bcz = cf[BCZ * PL + occ];
+    const T pxd = radd(T(1), rmul(g.hdt, bcx)), pxn = rsub(T(1), rmul(g.hdt, bcx));
+    const T pzd = radd(T(1), rmul(g.hdt, bcz)), pzn = rsub(T(1), rmul(g.hdt, bcz));
+    const T pxi = rdiv(T(1), pxd), pzi = rdiv(T(1), pzd);
+    const T c11 = cf[C11 * PL + occ], c13 = cf[C13 * PL + occ], c15 = cf[C15 * PL + occ];
+    const T c33 = cf[C33 * PL + occ], c35 = cf[C35 * PL + occ], c55 = cf[C55 * PL + occ];
+    T* f;
+    f = ts + TXX_X * NSP + o; *f = rmul(radd(rmul(pxn, *f), rmul(g.dt_dx, radd(rmul(c11, dxbm_vx), rmul(c15, dxbm_vz)))), pxi);
+    f = ts + TXX_Z * NSP + o; *f = rmul(radd(rmul(pzn, *f), rmul(g.dt_dz, radd(rmul(c15, dzbm_vx), rmul(c13, dzbm_vz)))), pzi);
+    f = ts + TZZ_X * NSP + o; *f = rmul(radd(rmul(pxn, *f), rmul(g.dt_dx, radd(rmul(c13, dxbm_vx), rmul(c35, dxbm_vz)))), pxi);
+    f = ts + TZZ_Z * NSP + o; *f = rmul(radd(rmul(pzn, *f), rmul(g.dt_dz, radd(rmul(c35, dzbm_vx), rmul(c33, dzbm_vz)))), pzi);
+    f = ts + TXZ_X * NSP + o; *f = rmul(radd(rmul(pxn, *f), rmul(g.dt_dx, radd(rmul(c15, dxfm_vx), rmul(c55, dxfm_vz)))), pxi);
+    f = ts + TXZ_Z * NSP + o; *f = rmul(radd(rmul(pzn, *f), rmul(g.dt_dz, radd(rmul(c55, dzfm_vx), rmul(c35, dzfm_vz)))), pzi);
+  }
+  if (i == g.src_z[s] && j == g.src_x[s]) {
+    const T w = wav[(int64_t)s * g.nt + it];
+    const T axx = rmul(g.src_m[3 * s + 0], w), azz = rmul(g.src_m[3 * s + 1], w), axz = rmul(g.src_m[3 * s + 2], w);
+    ts[TXX_X * NSP + o] = radd(ts[TXX_X * NSP + o], axx);
+    ts[TXX_Z * NSP + o] = radd(ts[TXX_Z * NSP + o], axx);
+    ts[TZZ_X * NSP + o] = radd(ts[TZZ_X * NSP + o], azz);
+    ts[TZZ_Z * NSP + o] = radd(ts[TZZ_Z * NSP + o], azz);
+    ts[TXZ_X * NSP + o] = radd(ts[TXZ_X * NSP + o], axz);
+    ts[TXZ_Z * NSP + o] = radd(ts[TXZ_Z * NSP + o], axz);
+  }
+}
+
+// Stress totals and free-surface stress rows (elastic_kernels.py:375-384) -> T (3 fields).
+template <typename T>
+__global__ void stress_tot_pml(Geo<T> g, const T* __restrict__ ts, T* __restrict__ tt) {
+  EL_CELL_SHOT
+  const int64_t P = g.L.pitch;
+  auto sum = [&](int f, int64_t oo) { return radd(ts[(2 * f) * NSP + oo], ts[(2 * f + 1) * NSP + oo]); };
+  T xx = sum(TXX, o), zz = sum(TZZ, o), xz = sum(TXZ, o);
+  if (g.fsurf) {
+    const int h = g.h;
+    if (i == h - 1) zz = T(0);
+    if (i == h - 2) zz = -sum(TZZ, o + 2 * P);
+    if (i == h - 2) xz = -sum(TXZ, o + P);
+    if (i == h - 3) xz = -sum(TXZ, o + 3 * P);
+  }
+  tt[TXX * NSP + o] = xx;
+  tt[TZZ * NSP + o] = zz;
+  tt[TXZ * NSP + o] = xz;
+}
+
+// Split velocities in I (elastic_kernels.py:387-394) from the stress totals tt.
+template <typename T, int NN>
+__global__ void vel_pml(Geo<T> g, const T* __restrict__ cf, const T* __restrict__ tt, T* __restrict__ vs) {
+  EL_CELL_SHOT
+  if (!in_I(g, i, j)) return;
+  const int64_t occ = g.L.off(i, j);
+  const T dxfm_txx = dxf<NN>(g, tt + TXX * NSP, o);
+  const T dzbm_txz = dzb<NN>(g, tt + TXZ * NSP, o);
+  const T dxbm_txz = dxb<NN>(g, tt + TXZ * NSP, o);
+  const T dzfm_tzz = dzf<NN>(g, tt + TZZ * NSP, o);
+  const T bcx = cf[BCX * PL + occ], bcz = cf[BCZ * PL + occ];
+  const T pxd = radd(T(1), rmul(g.hdt, bcx)), pxn = rsub(T(1), rmul(g.hdt, bcx));
+  const T pzd = radd(T(1), rmul(g.hdt, bcz)), pzn = rsub(T(1), rmul(g.hdt, bcz));
+  const T bx = cf[BX * PL + occ], bz = cf[BZ * PL + occ];
+  const T dbx = rmul(g.dt, bx), dbz = rmul(g.dt, bz);
+  T* f;
+  f = vs + VX_X * NSP + o; *f = rdiv(radd(rmul(pxn, *f), rdiv(rmul(dbx, dxfm_txx), g.dx)), pxd);
+  f = vs + VX_Z * NSP + o; *f = rdiv(radd(rmul(pzn, *f), rdiv(rmul(dbx, dzbm_txz), g.dz)), pzd);
+  f = vs + VZ_X * NSP + o; *f = rdiv(radd(rmul(pxn, *f), rdiv(rmul(dbz, dxbm_txz), g.dx)), pxd);
+  f = vs + VZ_Z * NSP + o; *f = rdiv(radd(rmul(pzn, *f), rdiv(rmul(dbz, dzfm_tzz), g.dz)), pzd);
+}
+
+// Velocity totals and free-surface velocity rows (elastic_kernels.py:395-402) -> v (2 fields).
+template <typename T>
+__global__ void vel_tot_pml(Geo<T> g, const T* __restrict__ vs, T* __restrict__ v) {
+  EL_CELL_SHOT
+  const int64_t P = g.L.pitch;
+  auto vxs = [&](int64_t oo) { return radd(vs[VX_X * NSP + oo], vs[VX_Z * NSP + oo]); };
+  auto vzs = [&](int64_t oo) { return radd(vs[VZ_X * NSP + oo], vs[VZ_Z * NSP + oo]); };
+  T vx = vxs(o), vz = vzs(o);
+  if (g.fsurf && j >= g.jlo && j <= g.jhi) {
+    const int h = g.h;
+    if (i == h - 2) {
+      // vz[h-2] = vz[h-1]; vx[h-2] = vz[h-2,j+1] - vz[h-2,j] + vz[h-1,j+1] - vz[h-1,j] + vx[h,j]
+      const T vz_up = vzs(o + P);                                           // vz[h-1, j]
+      const T vzn_r = (j + 1 <= g.jhi) ? vzs(o + P + 1) : vzs(o + 1);       // vz[h-2, j+1] after the first line
+      vz = vz_up;
+      vx = radd(rsub(radd(rsub(vzn_r, vz_up), vzs(o + P + 1)), vz_up), vxs(o + 2 * P));
+    } else if (i == h - 3) {
+      vz = vzs(o + 2 * P);  // vz[h-3] = vz[h-2] = vz[h-1]
+    }
+  }
+  v[VX * NSP + o] = vx;
+  v[VZ * NSP + o] = vz;
+}
+
+// ======================================================================= forward, absorbing layer
+template <typename T, int NN>
+__global__ void stress_abl(Geo<T> g, int it, const T* __restrict__ cf, const T* __restrict__ v, T* __restrict__ ts,
+                           const T* __restrict__ wav) {
+  EL_CELL_SHOT
+  const int64_t occ = g.L.off(i, j);
+  if (in_I(g, i, j)) {
+    const T* vx = v;
+    const T* vz = v + NSP;
+    const T dxbm_vx = dxb<NN>(g, vx, o), dxbm_vz = dxb<NN>(g, vz, o);
+    const T dzbm_vx = dzb<NN>(g, vx, o), dzbm_vz = dzb<NN>(g, vz, o);
+    const T dxfm_vx = dxf<NN>(g, vx, o), dzfm_vx = dzf<NN>(g, vx, o);
+    const T dxfm_vz = dxf<NN>(g, vz, o), dzfm_vz = dzf<NN>(g, vz, o);
+    const T c11 = cf[C11 * PL + occ], c13 = cf[C13 * PL + occ], c15 = cf[C15 * PL + occ];
+    const T c33 = cf[C33 * PL + occ], c35 = cf[C35 * PL + occ], c55 = cf[C55 * PL + occ];
+    T* f;
+    f = ts + TXX * NSP + o;
+    *f = radd(*f, rmul(g.dt, radd(rdiv(radd(rmul(c11, dxbm_vx), rmul(c15, dxbm_vz)), g.dx),
+                                  rdiv(radd(rmul(c15, dzbm_vx), rmul(c13, dzbm_vz)), g.dz))));
+    f = ts + TZZ * NSP + o;
+    *f = radd(*f, rmul(g.dt, radd(rdiv(radd(rmul(c13, dxbm_vx), rmul(c35, dxbm_vz)), g.dx),
+                                  rdiv(radd(rmul(c35, dzbm_vx), rmul(c33, dzbm_vz)), g.dz))));
+    f = ts + TXZ * NSP + o;
+    *f = radd(*f, rmul(g.dt, radd(rdiv(radd(rmul(c15, dxfm_vx), rmul(c55, dxfm_vz)), g.dx),
+                                  rdiv(radd(rmul(c55, dzfm_vx), rmul(c35, dzfm_vz)), g.dz))));
+  }
+  if (i == g.src_z[s] && j == g.src_x[s]) {
+    const T w = wav[(int64_t)s * g.nt + it];
+    ts[TXX * NSP + o] = radd(ts[TXX * NSP + o], rmul(g.src_m[3 * s + 0], w));
+    ts[TZZ * NSP + o] = radd(ts[TZZ * NSP + o], rmul(g.src_m[3 * s + 1], w));
+    ts[TXZ * NSP + o] = radd(ts[TXZ * NSP + o], rmul(g.src_m[3 * s + 2], w));
+  }
+}
+
+// Free-surface stress rows in place (elastic_kernels.py:738-742); one thread per column.
+template <typename T>
+__global__ void stress_fs_abl(Geo<T> g, T* __restrict__ ts) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= g.L.nxp) return;
+  const int s = blockIdx.y, h = g.h;
+  const int64_t NSP = (int64_t)g.ns * g.L.plane, so = (int64_t)s * g.L.plane;
+  T* zz = ts + TZZ * NSP + so;
+  T* xz = ts + TXZ * NSP + so;
+  zz[g.L.off(h - 1, j)] = T(0);
+  zz[g.L.off(h - 2, j)] = -zz[g.L.off(h, j)];
+  xz[g.L.off(h - 2, j)] = -xz[g.L.off(h - 1, j)];
+  xz[g.L.off(h - 3, j)] = -xz[g.L.off(h, j)];
+}
+
+template <typename T, int NN>
+__global__ void vel_abl(Geo<T> g, const T* __restrict__ cf, const T* __restrict__ tt, T* __restrict__ v) {
+  EL_CELL_SHOT
+  if (!in_I(g, i, j)) return;
+  const int64_t occ = g.L.off(i, j);
+  const T dxfm_txx = dxf<NN>(g, tt + TXX * NSP, o);
+  const T dzbm_txz = dzb<NN>(g, tt + TXZ * NSP, o);
+  const T dxbm_txz = dxb<NN>(g, tt + TXZ * NSP, o);
+  const T dzfm_tzz = dzf<NN>(g, tt + TZZ * NSP, o);
+  const T bx = cf[BX * PL + occ], bz = cf[BZ * PL + occ];
+  T* f = v + VX * NSP + o;
+  *f = radd(*f, rmul(rmul(g.dt, bx), radd(rdiv(dxfm_txx, g.dx), rdiv(dzbm_txz, g.dz))));
+  f = v + VZ * NSP + o;
+  *f = radd(*f, rmul(rmul(g.dt, bz), radd(rdiv(dxbm_txz, g.dx), rdiv(dzfm_tzz, g.dz))));
+}
+
+// Free-surface velocity rows in place (elastic_kernels.py:753-756); one thread per column in J.
+// Reads only rows h-1, h and the cell (h-2, jhi+1), none of which any thread writes.
+template <typename T>
+__global__ void vel_fs_abl(Geo<T> g, T* __restrict__ v) {
+  const int j = g.jlo + blockIdx.x * blockDim.x + threadIdx.x;
+  if (j > g.jhi) return;
+  const int s = blockIdx.y, h = g.h;
+  const int64_t NSP = (int64_t)g.ns * g.L.plane, so = (int64_t)s * g.L.plane;
+  T* vx = v + VX * NSP + so;
+  T* vz = v + VZ * NSP + so;
+  const T vz_up = vz[g.L.off(h - 1, j)];
+  const T vzn_r = (j + 1 <= g.jhi) ? vz[g.L.off(h - 1, j + 1)] : vz[g.L.off(h - 2, j + 1)];
+  const T vxh = vx[g.L.off(h, j)];
+  const T vz_up_r = vz[g.L.off(h - 1, j + 1)];
+  vz[g.L.off(h - 2, j)] = vz_up;
+  vx[g.L.off(h - 2, j)] = radd(rsub(radd(rsub(vzn_r, vz_up), vz_up_r), vz_up), vxh);
+  vz[g.L.off(h - 3, j)] = vz_up;
+}
+
+template <typename T>
+__global__ void damp_v(Geo<T> g, const T* __restrict__ cf, T* __restrict__ v) {
+  EL_CELL_SHOT
+  const T d = cf[DAMP * PL + g.L.off(i, j)];
+  v[VX * NSP + o] = rmul(v[VX * NSP + o], d);
+  v[VZ * NSP + o] = rmul(v[VZ * NSP + o], d);
+}
+
+// Receivers: txx, tzz, txz, vx, vz totals at each receiver (elastic_kernels.py:407-411).
+template <typename T>
+__global__ void record(Geo<T> g, int it, const T* __restrict__ tt, const T* __restrict__ v, T* rec) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= g.nr) return;
+  const int s = blockIdx.y;
+  const int64_t NSP = (int64_t)g.ns * g.L.plane;
+  const int64_t o = (int64_t)s * g.L.plane + g.L.off(g.rcv_z[r], g.rcv_x[r]);
+  const int64_t RS = (int64_t)g.ns * g.nt * g.nr;
+  const int64_t q = ((int64_t)s * g.nt + it) * g.nr + r;
+  rec[0 * RS + q] = tt[TXX * NSP + o];
+  rec[1 * RS + q] = tt[TZZ * NSP + o];
+  rec[2 * RS + q] = tt[TXZ * NSP + o];
+  rec[3 * RS + q] = v[VX * NSP + o];
+  rec[4 * RS + q] = v[VZ * NSP + o];
+}
+
+// forward_wavefield_* += sum_s X^2 of the last step of a chunk (elastic_kernels.py:414-418, 1016-1021).
+template <typename T>
+__global__ void energy(Geo<T> g, const T* __restrict__ tt, const T* __restrict__ v, T* fw) {
+  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= (int64_t)g.nz * g.nx) return;
+  const int i = (int)(e / g.nx) + g.top, j = (int)(e % g.nx) + g.nabc;
+  const int64_t NSP = (int64_t)g.ns * g.L.plane, oc = g.L.off(i, j);
+  const int64_t n = (int64_t)g.nz * g.nx;
+  const T* src[5] = {tt + TXX * NSP, tt + TZZ * NSP, tt + TXZ * NSP, v + VX * NSP, v + VZ * NSP};
+  for (int c = 0; c < 5; ++c) {
+    T acc = T(0);
+    for (int s = 0; s < g.ns; ++s) {
+      T x = src[c][(int64_t)s * g.L.plane + oc];
+      acc += x * x;
+    }
+    fw[c * n + e] += acc;
+  }
+}
+
+// ======================================================================= adjoint
+// Receiver residuals of step `it` into the adjoint stress totals lt (overwritten: zero + injection)
+// and added to the adjoint velocity totals lv. One thread per (unique receiver cell, shot).
+template <typename T>
+__global__ void adj_inject(Geo<T> g, int it, const T* __restrict__ grec, T* lt, T* lv, int write_lt) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= g.ncells) return;
+  const int s = blockIdx.y;
+  const int64_t NSP = (int64_t)g.ns * g.L.plane;
+  const int cell = g.ucell_zx[q];
+  const int64_t o = (int64_t)s * g.L.plane + g.L.off(cell >> 16, cell & 0xffff);
+  const int64_t RS = (int64_t)g.ns * g.nt * g.nr;
+  const int64_t base = ((int64_t)s * g.nt + it) * g.nr;
+  T a[5] = {T(0), T(0), T(0), T(0), T(0)};
+  for (int m = g.ucell_beg[q]; m < g.ucell_beg[q + 1]; ++m) {
+    const int64_t qq = base + g.ucell_rcv[m];
+    for (int c = 0; c < 5; ++c) a[c] += grec[c * RS + qq];
+  }
+  if (write_lt) {
+    lt[TXX * NSP + o] += a[0];
+    lt[TZZ * NSP + o] += a[1];
+    lt[TXZ * NSP + o] += a[2];
+  }
+  lv[VX * NSP + o] += a[3];
+  lv[VZ * NSP + o] += a[4];
+}
+
+// Adjoint of the free-surface velocity rows: lambda of the velocity totals BEFORE the rows
+// h-3 / h-2 were overwritten (reverse of elastic_kernels.py:400-402), at cell (i, j).
+template <typename T>
+__device__ __forceinline__ void vfs_adjoint(const Geo<T>& g, const T* lvx, const T* lvz, int i, int j, int64_t o,
+                                            T& ax, T& az) {
+  const int64_t P = g.L.pitch;
+  ax = lvx[o];
+  az = lvz[o];
+  if (!g.fsurf) return;
+  const int h = g.h;
+  auto inJ = [&](int m) { return m >= g.jlo && m <= g.jhi; };
+  auto A = [&](int m, int64_t om) { return inJ(m) ? lvx[om] : T(0); };  // lambda vx[h-2, m] (om: offset of (h-2, m))
+  if (i == h - 3) {
+    if (inJ(j)) az = T(0);
+  } else if (i == h - 2) {
+    if (inJ(j)) {
+      ax = T(0);
+      az = T(0);
+    } else if (inJ(j - 1)) {
+      az = lvz[o] + lvx[o - 1];
+    }
+  } else if (i == h - 1) {
+    const int64_t o2 = o - P;  // (h-2, j)
+    T a_l = inJ(j - 1) ? lvx[o2 - 1] : T(0);
+    T a_c = A(j, o2);
+    T r = lvz[o] + a_l - a_c;
+    if (inJ(j)) {
+      const T b = lvz[o2 - P];  // lambda vz[h-3, j]
+      const T cval = lvz[o2] + b + a_l - a_c;
+      r += cval;
+    }
+    az = r;
+  } else if (i == h) {
+    if (inJ(j)) ax = lvx[o] + lvx[o - 2 * P];
+  }
+}
+
+// Adjoint of the free-surface stress rows (reverse of elastic_kernels.py:381-384).
+template <typename T>
+__device__ __forceinline__ void tfs_adjoint(const Geo<T>& g, const T* lzz, const T* lxz, int i, int64_t o, T& azz,
+                                            T& axz) {
+  const int64_t P = g.L.pitch;
+  azz = lzz[o];
+  axz = lxz[o];
+  if (!g.fsurf) return;
+  const int h = g.h;
+  if (i == h - 3) axz = T(0);
+  if (i == h - 2) {
+    axz = T(0);
+    azz = T(0);
+  }
+  if (i == h - 1) {
+    azz = T(0);
+    axz = lxz[o] - lxz[o - P];
+  }
+  if (i == h) {
+    azz = lzz[o] - lzz[o - 2 * P];
+    axz = lxz[o] - lxz[o - 3 * P];
+  }
+}
+
+template <typename T>
+struct Pml {
+  T xd, xn, zd, zn;
+};
+template <typename T>
+__device__ __forceinline__ Pml<T> pml_at(const Geo<T>& g, const T* cf, int64_t oc, int64_t PL) {
+  const T bcx = cf[BCX * PL + oc], bcz = cf[BCZ * PL + oc];
+  Pml<T> p;
+  p.xd = T(1) + g.hdt * bcx;
+  p.xn = T(1) - g.hdt * bcx;
+  p.zd = T(1) + g.hdt * bcz;
+  p.zn = T(1) - g.hdt * bcz;
+  return p;
+}
+
+// (B4) lambda of the split velocities after the step: S (deferred PML factor of the next
+// step's update) * lambda + lambda of the totals after the free-surface adjoint.
+template <typename T>
+__global__ void adj_vfs_pml(Geo<T> g, const T* __restrict__ cf, const T* __restrict__ lv, T* lvs) {
+  EL_CELL_SHOT
+  T ax, az;
+  vfs_adjoint(g, lv + VX * NSP, lv + VZ * NSP, i, j, o, ax, az);
+  T sx = T(1), sz = T(1);
+  if (in_I(g, i, j)) {
+    Pml<T> p = pml_at(g, cf, g.L.off(i, j), PL);
+    sx = p.xn / p.xd;
+    sz = p.zn / p.zd;
+  }
+  lvs[VX_X * NSP + o] = sx * lvs[VX_X * NSP + o] + ax;
+  lvs[VX_Z * NSP + o] = sz * lvs[VX_Z * NSP + o] + ax;
+  lvs[VZ_X * NSP + o] = sx * lvs[VZ_X * NSP + o] + az;
+  lvs[VZ_Z * NSP + o] = sz * lvs[VZ_Z * NSP + o] + az;
+}
+
+// (B3a) lt += transposes of the velocity update's stress differences; bx, bz gradients.
+template <typename T, int NN>
+__global__ void adj_t_pml(Geo<T> g, const T* __restrict__ cf, const T* __restrict__ lvs, T* lt,
+                          const T* __restrict__ tt_hist, T* gbx, T* gbz) {
+  EL_CELL
+  T gx = T(0), gz = T(0);
+  for (int s = 0; s < g.ns; ++s) {
+    const int64_t so = (int64_t)s * PL;
+    auto qf = [&](int comp, bool xdir, int ii, int jj) -> T {
+      if (!in_I(g, ii, jj)) return T(0);
+      const int64_t c = g.L.off(ii, jj);
+      const T bcoef = cf[(comp < 2 ? BX : BZ) * PL + c];
+      const Pml<T> p = pml_at(g, cf, c, PL);
+      return lvs[comp * NSP + so + c] * (g.dt * bcoef) / (xdir ? g.dx * p.xd : g.dz * p.zd);
+    };
+    auto q_vxx = [&](int ii, int jj) { return qf(VX_X, true, ii, jj); };
+    auto q_vxz = [&](int ii, int jj) { return qf(VX_Z, false, ii, jj); };
+    auto q_vzx = [&](int ii, int jj) { return qf(VZ_X, true, ii, jj); };
+    auto q_vzz = [&](int ii, int jj) { return qf(VZ_Z, false, ii, jj); };
+    const int64_t o = so + oc;
+    lt[TXX * NSP + o] += dxf_t<NN>(g, q_vxx, i, j);
+    lt[TXZ * NSP + o] += dzb_t<NN>(g, q_vxz, i, j) + dxb_t<NN>(g, q_vzx, i, j);
+    lt[TZZ * NSP + o] += dzf_t<NN>(g, q_vzz, i, j);
+    if (in_I(g, i, j)) {
+      // d(v_x')/d(bx) = dt * D(T) / (d * pml_d), likewise for bz
+      const T* th = tt_hist;
+      const Pml<T> p = pml_at(g, cf, oc, PL);
+      gx += lvs[VX_X * NSP + o] * g.dt * dxf<NN>(g, th + TXX * NSP, o) / (g.dx * p.xd) +
+            lvs[VX_Z * NSP + o] * g.dt * dzb<NN>(g, th + TXZ * NSP, o) / (g.dz * p.zd);
+      gz += lvs[VZ_X * NSP + o] * g.dt * dxb<NN>(g, th + TXZ * NSP, o) / (g.dx * p.xd) +
+            lvs[VZ_Z * NSP + o] * g.dt * dzf<NN>(g, th + TZZ * NSP, o) / (g.dz * p.zd);
+    }
+  }
+  if (in_I(g, i, j)) {
+    gbx[oc] += gx;
+    gbz[oc] += gz;
+  }
+}
+
+// (B2) lambda of the split stresses: S * lambda + lambda of the totals after the stress
+// free-surface adjoint.
+template <typename T>
+__global__ void adj_tfs_pml(Geo<T> g, const T* __restrict__ cf, const T* __restrict__ lt, T* lts) {
+  EL_CELL_SHOT
+  T azz, axz;
+  tfs_adjoint(g, lt + TZZ * NSP, lt + TXZ * NSP, i, o, azz, axz);
+  const T axx = lt[TXX * NSP + o];
+  T sx = T(1), sz = T(1);
+  if (in_I(g, i, j)) {
+    Pml<T> p = pml_at(g, cf, g.L.off(i, j), PL);
+    sx = p.xn / p.xd;
+    sz = p.zn / p.zd;
+  }
+  lts[TXX_X * NSP + o] = sx * lts[TXX_X * NSP + o] + axx;
+  lts[TXX_Z * NSP + o] = sz * lts[TXX_Z * NSP + o] + axx;
+  lts[TZZ_X * NSP + o] = sx * lts[TZZ_X * NSP + o] + azz;
+  lts[TZZ_Z * NSP + o] = sz * lts[TZZ_Z * NSP + o] + azz;
+  lts[TXZ_X * NSP + o] = sx * lts[TXZ_X * NSP + o] + axz;
+  lts[TXZ_Z * NSP + o] = sz * lts[TXZ_Z * NSP + o] + axz;
+}
+
+// Coefficient-weighted adjoint sources of the stress update at cell (ii, jj):
+// q[0..5] = lambda of txx_x, txx_z, tzz_x, tzz_z, txz_x, txz_z times their d(update)/d(C D v).
+template <typename T>
+struct StressQ {
+  T a, b, c, d, e, f;  // xx_x, xx_z, zz_x, zz_z, xz_x, xz_z
+};
+
+// (B1a) lambda of the velocity totals at the start of the step (overwrite) and the C gradients.
+// pml = 1: split-field update; pml = 0: absorbing-layer update (lts then holds txx, tzz, txz,
+// and lv is accumulated instead of overwritten because v' = v + ...).
+template <typename T, int NN, bool PMLM>
+__global__ void adj_v(Geo<T> g, const T* __restrict__ cf, const T* __restrict__ lts, T* lv,
+                      const T* __restrict__ v_hist, T* gc) {
+  EL_CELL
+  T g11 = T(0), g13 = T(0), g15 = T(0), g33 = T(0), g35 = T(0), g55 = T(0);
+  for (int s = 0; s < g.ns; ++s) {
+    const int64_t so = (int64_t)s * PL;
+    auto q = [&](int ii, int jj) -> StressQ<T> {
+      StressQ<T> r;
+      if (!in_I(g, ii, jj)) {
+        r.a = r.b = r.c = r.d = r.e = r.f = T(0);
+        return r;
+      }
+      const int64_t c = g.L.off(ii, jj), oo = so + c;
+      if (PMLM) {
+        const Pml<T> p = pml_at(g, cf, c, PL);
+        const T kx = g.dt_dx / p.xd, kz = g.dt_dz / p.zd;
+        r.a = lts[TXX_X * NSP + oo] * kx;
+        r.b = lts[TXX_Z * NSP + oo] * kz;
+        r.c = lts[TZZ_X * NSP + oo] * kx;
+        r.d = lts[TZZ_Z * NSP + oo] * kz;
+        r.e = lts[TXZ_X * NSP + oo] * kx;
+        r.f = lts[TXZ_Z * NSP + oo] * kz;
+      } else {
+        const T kx = g.dt / g.dx, kz = g.dt / g.dz;
+        r.a = lts[TXX * NSP + oo] * kx;
+        r.b = lts[TXX * NSP + oo] * kz;
+        r.c = lts[TZZ * NSP + oo] * kx;
+        r.d = lts[TZZ * NSP + oo] * kz;
+        r.e = lts[TXZ * NSP + oo] * kx;
+        r.f = lts[TXZ * NSP + oo] * kz;
+      }
+      return r;
+    };
+    auto C = [&](int k, int ii, int jj) { return cf[k * PL + g.L.off(ii, jj)]; };
+    // velocity-x sources
+    auto sx_b = [&](int ii, int jj) { StressQ<T> r = q(ii, jj); return C(C11, ii, jj) * r.a + C(C13, ii, jj) * r.c; };
+    auto sx_zb = [&](int ii, int jj) { StressQ<T> r = q(ii, jj); return C(C15, ii, jj) * r.b + C(C35, ii, jj) * r.d; };
+    auto sx_f = [&](int ii, int jj) { StressQ<T> r = q(ii, jj); return C(C15, ii, jj) * r.e; };
+    auto sx_zf = [&](int ii, int jj) { StressQ<T> r = q(ii, jj); return C(C55, ii, jj) * r.f; };
+    // velocity-z sources
+    auto sz_b = [&](int ii, int jj) { StressQ<T> r = q(ii, jj); return C(C15, ii, jj) * r.a + C(C35, ii, jj) * r.c; };
+    auto sz_zb = [&](int ii, int jj) { StressQ<T> r = q(ii, jj); return C(C13, ii, jj) * r.b + C(C33, ii, jj) * r.d; };
+    auto sz_f = [&](int ii, int jj) { StressQ<T> r = q(ii, jj); return C(C55, ii, jj) * r.e; };
+    auto sz_zf = [&](int ii, int jj) { StressQ<T> r = q(ii, jj); return C(C35, ii, jj) * r.f; };
+    const T avx = dxb_t<NN>(g, sx_b, i, j) + dzb_t<NN>(g, sx_zb, i, j) + dxf_t<NN>(g, sx_f, i, j) +
+                  dzf_t<NN>(g, sx_zf, i, j);
+    const T avz = dxb_t<NN>(g, sz_b, i, j) + dzb_t<NN>(g, sz_zb, i, j) + dxf_t<NN>(g, sz_f, i, j) +
+                  dzf_t<NN>(g, sz_zf, i, j);
+    const int64_t o = so + oc;
+    if (PMLM) {
+      lv[VX * NSP + o] = avx;
+      lv[VZ * NSP + o] = avz;
+    } else {
+      lv[VX * NSP + o] += avx;
+      lv[VZ * NSP + o] += avz;
+    }
+    if (in_I(g, i, j)) {
+      const StressQ<T> r = q(i, j);
+      const T* vx = v_hist + VX * NSP;
+      const T* vz = v_hist + VZ * NSP;
+      const T dxb_vx = dxb<NN>(g, vx, o), dxb_vz = dxb<NN>(g, vz, o);
+      const T dzb_vx = dzb<NN>(g, vx, o), dzb_vz = dzb<NN>(g, vz, o);
+      const T dxf_vx = dxf<NN>(g, vx, o), dxf_vz = dxf<NN>(g, vz, o);
+      const T dzf_vx = dzf<NN>(g, vx, o), dzf_vz = dzf<NN>(g, vz, o);
+      g11 += r.a * dxb_vx;
+      g13 += r.b * dzb_vz + r.c * dxb_vx;
+      g15 += r.a * dxb_vz + r.b * dzb_vx + r.e * dxf_vx;
+      g33 += r.d * dzb_vz;
+      g35 += r.c * dxb_vz + r.d * dzb_vx + r.f * dzf_vz;
+      g55 += r.e * dxf_vz + r.f * dzf_vx;
+    }
+  }
+  if (in_I(g, i, j)) {
+    gc[C11 * PL + oc] += g11;
+    gc[C13 * PL + oc] += g13;
+    gc[C15 * PL + oc] += g15;
+    gc[C33 * PL + oc] += g33;
+    gc[C35 * PL + oc] += g35;
+    gc[C55 * PL + oc] += g55;
+  }
+}
+
+// ABL (reverse of v *= damp and the free-surface velocity rows): lv_out = FS^T(damp * lv_in).
+template <typename T>
+__global__ void adj_vfs_abl(Geo<T> g, const T* __restrict__ cf, const T* __restrict__ lv_in, T* lv_out,
+                            T* scratch) {
+  EL_CELL_SHOT
+  (void)scratch;
+  // damp-weighted lambda at the cells the free-surface adjoint reads
+  auto dl = [&](int comp, int64_t oo, int ii, int jj) { return cf[DAMP * PL + g.L.off(ii, jj)] * lv_in[comp * NSP + oo]; };
+  T ax = dl(VX, o, i, j), az = dl(VZ, o, i, j);
+  if (g.fsurf) {
+    const int h = g.h;
+    const int64_t P = g.L.pitch;
+    auto inJ = [&](int m) { return m >= g.jlo && m <= g.jhi; };
+    if (i == h - 3) {
+      if (inJ(j)) az = T(0);
+    } else if (i == h - 2) {
+      if (inJ(j)) {
+        ax = T(0);
+        az = T(0);
+      } else if (inJ(j - 1)) {
+        az += dl(VX, o - 1, i, j - 1);
+      }
+    } else if (i == h - 1) {
+      const int64_t o2 = o - P;
+      const T a_l = inJ(j - 1) ? dl(VX, o2 - 1, i - 1, j - 1) : T(0);
+      const T a_c = inJ(j) ? dl(VX, o2, i - 1, j) : T(0);
+      T r = az + a_l - a_c;
+      if (inJ(j)) r += dl(VZ, o2, i - 1, j) + dl(VZ, o2 - P, i - 2, j) + a_l - a_c;
+      az = r;
+    } else if (i == h) {
+      if (inJ(j)) ax += dl(VX, o - 2 * P, i - 2, j);
+    }
+  }
+  lv_out[VX * NSP + o] = ax;
+  lv_out[VZ * NSP + o] = az;
+}
+
+// ABL: lt += transposes of the velocity update's stress differences; bx, bz gradients.
+template <typename T, int NN>
+__global__ void adj_t_abl(Geo<T> g, const T* __restrict__ cf, const T* __restrict__ lv, T* lt,
+                          const T* __restrict__ tt_hist, T* gbx, T* gbz) {
+  EL_CELL
+  T gx = T(0), gz = T(0);
+  for (int s = 0; s < g.ns; ++s) {
+    const int64_t so = (int64_t)s * PL;
+    auto qf = [&](int comp, T den, int ii, int jj) -> T {
+      if (!in_I(g, ii, jj)) return T(0);
+      const int64_t c = g.L.off(ii, jj);
+      const T b = cf[(comp == VX ? BX : BZ) * PL + c];
+      return lv[comp * NSP + so + c] * (g.dt * b) / den;
+    };
+    auto q1 = [&](int ii, int jj) { return qf(VX, g.dx, ii, jj); };
+    auto q2 = [&](int ii, int jj) { return qf(VX, g.dz, ii, jj); };
+    auto q3 = [&](int ii, int jj) { return qf(VZ, g.dx, ii, jj); };
+    auto q4 = [&](int ii, int jj) { return qf(VZ, g.dz, ii, jj); };
+    const int64_t o = so + oc;
+    lt[TXX * NSP + o] += dxf_t<NN>(g, q1, i, j);
+    lt[TXZ * NSP + o] += dzb_t<NN>(g, q2, i, j) + dxb_t<NN>(g, q3, i, j);
+    lt[TZZ * NSP + o] += dzf_t<NN>(g, q4, i, j);
+    if (in_I(g, i, j)) {
+      const T* th = tt_hist;
+      gx += lv[VX * NSP + o] * g.dt * (dxf<NN>(g, th + TXX * NSP, o) / g.dx + dzb<NN>(g, th + TXZ * NSP, o) / g.dz);
+      gz += lv[VZ * NSP + o] * g.dt * (dxb<NN>(g, th + TXZ * NSP, o) / g.dx + dzf<NN>(g, th + TZZ * NSP, o) / g.dz);
+    }
+  }
+  if (in_I(g, i, j)) {
+    gbx[oc] += gx;
+    gbz[oc] += gz;
+  }
+}
+
+// ABL: stress free-surface adjoint in place, one thread per column.
+template <typename T>
+__global__ void adj_tfs_abl(Geo<T> g, T* lt) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= g.L.nxp) return;
+  const int s = blockIdx.y, h = g.h;
+  const int64_t NSP = (int64_t)g.ns * g.L.plane, so = (int64_t)s * g.L.plane;
+  T* zz = lt + TZZ * NSP + so;
+  T* xz = lt + TXZ * NSP + so;
+  const int64_t o3 = g.L.off(h - 3, j), o2 = g.L.off(h - 2, j), o1 = g.L.off(h - 1, j), o0 = g.L.off(h, j);
+  xz[o0] -= xz[o3];
+  xz[o3] = T(0);
+  xz[o1] -= xz[o2];
+  xz[o2] = T(0);
+  zz[o0] -= zz[o2];
+  zz[o2] = T(0);
+  zz[o1] = T(0);
+}
+
+template <typename T>
+__global__ void pack(Layout L, int h, int w, const T* __restrict__ src, T* __restrict__ dst) {
+  int64_t n = (int64_t)h * w;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+    int i = (int)(e / w), j = (int)(e - (int64_t)i * w);
+    dst[L.off(i, j)] = src[e];
+  }
+}
+
+template <typename T>
+__global__ void unpack(Layout L, int h, int w, const T* __restrict__ src, T* __restrict__ dst) {
+  int64_t n = (int64_t)h * w;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+    int i = (int)(e / w), j = (int)(e - (int64_t)i * w);
+    dst[e] = src[L.off(i, j)];
+  }
+}
+
+}  // namespace el
+}  // namespace adfwi
+
+// ----------------------------------------------------------------------------------------
+// Plan, workspace and drivers.
+// ----------------------------------------------------------------------------------------
+using namespace adfwi;
+
+struct adfwi_elastic_plan {
+  adfwi_elastic_desc d;
+  int nzp, nxp, NN, h, top;
+  int nstate;           // state fields per shot: PML 6 split stresses + 4 split velocities + 2 v totals, ABL 3 + 2
+  int K, nseg;
+  int elem;
+  Layout L;
+  std::vector<int32_t> tab;
+  std::vector<unsigned char> srcm;  // ns x 3 source weights (xx, zz, xz) in the solve's dtype
+  int64_t o_srcz, o_srcx, o_rcvz, o_rcvx, o_uzx, o_ubeg, o_urcv;
+  int ncells;
+  std::vector<int> chunk_end;  // last step of each reference checkpoint chunk
+};
+
+namespace {
+
+int64_t al256(int64_t x) { return (x + 255) / 256 * 256; }
+
+struct ECarve {
+  int64_t coef, st, tt, vtmp, srcm, tab;       // forward
+  int64_t snap, snap_scale, hv, ht, lst, lt, lv, lv2, gc;  // gradient
+  int64_t total;
+};
+
+// Coefficient planes: C11 C13 C15 C33 C35 C55 bx bz + (bcx bcz | damp)
+int ncoef(const adfwi_elastic_plan* p) { return p->d.pml ? 10 : 9; }
+
+ECarve ecarve(const adfwi_elastic_plan* p, bool grad, int K) {
+  ECarve c{};
+  const int64_t pl = p->L.plane * p->elem, ns = p->d.ns;
+  int64_t o = 0;
+  auto take = [&](int64_t b) { int64_t at = o; o += al256(b); return at; };
+  const int nsplit = p->d.pml ? 10 : 3;  // fields updated in place (split stresses+velocities | stresses)
+  c.coef = take(ncoef(p) * pl);
+  c.st = take((int64_t)(p->d.pml ? 10 : 3) * ns * pl);  // PML: 6 split stresses + 4 split velocities
+  c.tt = take(3 * ns * pl);                               // stress totals (PML) | unused (ABL)
+  c.vtmp = take(2 * ns * pl);                             // velocity totals / ABL velocities
+  c.srcm = take(ns * 3 * p->elem);
+  c.tab = take((int64_t)p->tab.size() * 4);
+  (void)nsplit;
+  if (grad) {
+    const bool full = K >= p->d.nt;
+    const int nseg = (p->d.nt + K - 1) / K;
+    const int64_t se = p->d.snapshot_precision == ADFWI_SNAP_NATIVE ? p->elem : 2;
+    const int64_t nstate = p->nstate;
+    c.snap = take(full ? 0 : (int64_t)nseg * nstate * ns * p->L.plane * se);
+    c.snap_scale = take(full ? 0 : (int64_t)nseg * nstate * ns * 4);
+    c.hv = take((int64_t)K * 2 * ns * pl);  // velocity totals at the start of each step
+    c.ht = take((int64_t)K * 3 * ns * pl);  // stress totals after each step's free surface
+    c.lst = take((int64_t)(p->d.pml ? 10 : 3) * ns * pl);
+    c.lt = take(3 * ns * pl);
+    c.lv = take(2 * ns * pl);
+    c.lv2 = take(2 * ns * pl);
+    c.gc = take(8 * pl);
+  }
+  c.total = o;
+  return c;
+}
+
+int echoose_K(const adfwi_elastic_plan* p) {
+  const int nt = p->d.nt;
+  const int64_t budget = p->d.memory_budget;
+  if (p->d.snapshot_every > 0) return std::min(p->d.snapshot_every, nt);
+  if (budget <= 0) return std::min(nt, std::max(1, (int)std::ceil(std::sqrt(2.4 * nt))));
+  if (ecarve(p, true, nt).total <= budget) return nt;
+  int kstar = std::min(nt - 1, std::max(1, (int)std::lround(std::sqrt(2.4 * nt))));
+  while (kstar > 1 && ecarve(p, true, kstar - 1).total < ecarve(p, true, kstar).total) --kstar;
+  while (kstar < nt - 1 && ecarve(p, true, kstar + 1).total < ecarve(p, true, kstar).total) ++kstar;
+  if (ecarve(p, true, kstar).total > budget) return kstar;
+  int lo = kstar, hi = nt - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) / 2;
+    if (ecarve(p, true, mid).total <= budget) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+template <typename T>
+el::Geo<T> egeo(const adfwi_elastic_plan* p, const unsigned char* ws, const ECarve& c) {
+  el::Geo<T> g;
+  const adfwi_elastic_desc& d = p->d;
+  g.L = p->L;
+  g.ns = d.ns;
+  g.nt = d.nt;
+  g.nr = d.nr;
+  g.fsurf = d.free_surface;
+  g.h = p->h;
+  g.ilo = p->NN;
+  g.ihi = p->nzp - p->NN - 1;
+  g.jlo = p->NN;
+  g.jhi = p->nxp - p->NN - 1;
+  g.top = p->top;
+  g.nabc = d.nabc;
+  g.nz = d.nz;
+  g.nx = d.nx;
+  g.dt = (T)d.dt;
+  g.dx = (T)d.dx;
+  g.dz = (T)d.dz;
+  g.dt_dx = (T)(d.dt / d.dx);
+  g.dt_dz = (T)(d.dt / d.dz);
+  g.hdt = (T)(0.5 * d.dt);
+  g.f0 = (T)d.fdc[0];
+  g.f1 = (T)d.fdc[1];
+  g.f2 = (T)(p->NN == 3 ? d.fdc[2] : 0.0);
+  const int32_t* tb = reinterpret_cast<const int32_t*>(ws + c.tab);
+  g.src_z = tb + p->o_srcz;
+  g.src_x = tb + p->o_srcx;
+  g.src_m = reinterpret_cast<const T*>(ws + c.srcm);
+  g.rcv_z = tb + p->o_rcvz;
+  g.rcv_x = tb + p->o_rcvx;
+  g.ucell_zx = tb + p->o_uzx;
+  g.ucell_beg = tb + p->o_ubeg;
+  g.ucell_rcv = tb + p->o_urcv;
+  g.ncells = p->ncells;
+  return g;
+}
+
+inline dim3 cells_grid(const adfwi_elastic_plan* p, int ns) {
+  return dim3((unsigned)(((int64_t)p->nzp * p->nxp + 255) / 256), ns);
+}
+
+template <typename T>
+int esetup(const adfwi_elastic_plan* p, unsigned char* ws, const ECarve& c, const void* const* coef,
+           const int32_t* shapes, cudaStream_t st) {
+  const int64_t pl = p->L.plane * p->elem;
+  ADFWI_CUDA_TRY(cudaMemsetAsync(ws, 0, c.srcm, st));  // coefficient ghosts, state, totals
+  ADFWI_CUDA_TRY(cudaMemcpyAsync(ws + c.tab, p->tab.data(), p->tab.size() * 4, cudaMemcpyHostToDevice, st));
+  ADFWI_CUDA_TRY(cudaMemcpyAsync(ws + c.srcm, p->srcm.data(), p->srcm.size(), cudaMemcpyHostToDevice, st));
+  for (int q = 0; q < ncoef(p); ++q) {
+    const int h = shapes[2 * q], w = shapes[2 * q + 1];
+    if (h < 1 || w < 1 || h > p->nzp || w > p->nxp) {
+      set_error("coefficient %d has shape %dx%d, outside the %dx%d grid", q, h, w, p->nzp, p->nxp);
+      return kBadArgument;
+    }
+    const int64_t n = (int64_t)h * w;
+    ADFWI_LAUNCH(kAux, st, (el::pack<T><<<(unsigned)std::min<int64_t>((n + 255) / 256, 4096), 256, 0, st>>>(
+                               p->L, h, w, static_cast<const T*>(coef[q]),
+                               reinterpret_cast<T*>(ws + c.coef + q * pl))));
+  }
+  ADFWI_CUDA_TRY(cudaGetLastError());
+  return kOk;
+}
+
+// One forward step. vin: velocity totals at the start of the step; vout: where the new
+// totals go; tt: where the stress totals go (PML). ABL keeps v in vin (= vout) in place.
+template <typename T, int NN>
+void estep(const adfwi_elastic_plan* p, const el::Geo<T>& g, int it, const T* cf, const T* wav, T* st, T* tt,
+           const T* vin, T* vout, cudaStream_t s) {
+  const dim3 gc = cells_grid(p, p->d.ns), b(256);
+  const int64_t NSP = (int64_t)p->d.ns * p->L.plane;
+  if (p->d.pml) {
+    T* ts = st;
+    T* vs = st + 6 * NSP;
+    ADFWI_LAUNCH(kElFwdStep, s, (el::stress_pml<T, NN><<<gc, b, 0, s>>>(g, it, cf, vin, ts, wav)));
+    ADFWI_LAUNCH(kElFwdStep, s, (el::stress_tot_pml<T><<<gc, b, 0, s>>>(g, ts, tt)));
+    ADFWI_LAUNCH(kElFwdStep, s, (el::vel_pml<T, NN><<<gc, b, 0, s>>>(g, cf, tt, vs)));
+    ADFWI_LAUNCH(kElFwdStep, s, (el::vel_tot_pml<T><<<gc, b, 0, s>>>(g, vs, vout)));
+  } else {
+    // ABL: stresses live in `tt`, velocities in place in vin (== vout)
+    T* v = vout;
+    if (vin != vout) cudaMemcpyAsync(v, vin, 2 * NSP * sizeof(T), cudaMemcpyDeviceToDevice, s);
+    const dim3 gcol((unsigned)((p->nxp + 127) / 128), p->d.ns);
+    ADFWI_LAUNCH(kElFwdStep, s, (el::stress_abl<T, NN><<<gc, b, 0, s>>>(g, it, cf, v, tt, wav)));
+    if (p->d.free_surface) ADFWI_LAUNCH(kElFwdStep, s, (el::stress_fs_abl<T><<<gcol, 128, 0, s>>>(g, tt)));
+    ADFWI_LAUNCH(kElFwdStep, s, (el::vel_abl<T, NN><<<gc, b, 0, s>>>(g, cf, tt, v)));
+    if (p->d.free_surface) ADFWI_LAUNCH(kElFwdStep, s, (el::vel_fs_abl<T><<<gcol, 128, 0, s>>>(g, v)));
+    ADFWI_LAUNCH(kElFwdStep, s, (el::damp_v<T><<<gc, b, 0, s>>>(g, cf, v)));
+  }
+}
+
+// Snapshot helpers: the state of a step start is (PML) 10 split fields in st + 2 velocity
+// totals, or (ABL) 3 stresses in tt + 2 velocities.
+template <typename T>
+int esnap(const adfwi_elastic_plan* p, bool store, unsigned char* ws, const ECarve& c, T* a, int64_t na, T* b,
+          int64_t nb, int seg, cudaStream_t s) {
+  const int64_t pl = p->L.plane;
+  const int64_t first = (int64_t)seg * (na + nb);
+  int rc = store ? snapshot_store<T>(p->d.snapshot_precision, a, na, pl, ws + c.snap, ws + c.snap_scale, first, s)
+                 : snapshot_load<T>(p->d.snapshot_precision, a, na, pl, ws + c.snap, ws + c.snap_scale, first, s);
+  if (rc) return rc;
+  return store ? snapshot_store<T>(p->d.snapshot_precision, b, nb, pl, ws + c.snap, ws + c.snap_scale, first + na, s)
+               : snapshot_load<T>(p->d.snapshot_precision, b, nb, pl, ws + c.snap, ws + c.snap_scale, first + na, s);
+}
+
+template <typename T, int NN>
+int eforward(const adfwi_elastic_plan* p, const void* const* coef, const int32_t* shapes, const void* wavelet,
+             void* rec, void* fw, bool grad, unsigned char* ws, int64_t ws_bytes, cudaStream_t s) {
+  const int K = grad ? p->K : 1;
+  ECarve c = ecarve(p, grad, K);
+  if (ws_bytes < c.total) {
+    set_error("workspace too small: %lld bytes given, %lld needed", (long long)ws_bytes, (long long)c.total);
+    return kWorkspaceTooSmall;
+  }
+  int rc = esetup<T>(p, ws, c, coef, shapes, s);
+  if (rc) return rc;
+  el::Geo<T> g = egeo<T>(p, ws, c);
+  const int64_t NSP = (int64_t)p->d.ns * p->L.plane;
+  const T* cf = reinterpret_cast<const T*>(ws + c.coef);
+  const T* wav = static_cast<const T*>(wavelet);
+  T* stt = reinterpret_cast<T*>(ws + c.st);
+  T* tt0 = reinterpret_cast<T*>(ws + c.tt);
+  T* v0 = reinterpret_cast<T*>(ws + c.vtmp);
+  const bool full = grad && K >= p->d.nt;
+  T* hv = grad ? reinterpret_cast<T*>(ws + c.hv) : nullptr;
+  T* ht = grad ? reinterpret_cast<T*>(ws + c.ht) : nullptr;
+  const int nt = p->d.nt;
+  if (fw) ADFWI_CUDA_TRY(cudaMemsetAsync(fw, 0, 5 * (int64_t)p->d.nz * p->d.nx * sizeof(T), s));
+  size_t chunk = 0;
+  for (int it = 0; it < nt; ++it) {
+    if (grad && !full && it % K == 0) {
+      if (p->d.pml)
+        rc = esnap<T>(p, true, ws, c, stt, 10 * p->d.ns, v0, 2 * p->d.ns, it / K, s);
+      else
+        rc = esnap<T>(p, true, ws, c, tt0, 3 * p->d.ns, v0, 2 * p->d.ns, it / K, s);
+      if (rc) return rc;
+    }
+    T* vin = v0;
+    T* vout = v0;
+    T* tt = tt0;
+    if (full) {
+      // the histories double as the state: Hv[it] = v at the start of step it, Ht[it] = T after it
+      vin = it == 0 ? v0 : hv + (int64_t)it * 2 * NSP;
+      vout = it + 1 < nt ? hv + (int64_t)(it + 1) * 2 * NSP : v0;
+      if (it == 0) ADFWI_CUDA_TRY(cudaMemsetAsync(hv, 0, 2 * NSP * sizeof(T), s));
+      if (it == 0) vin = hv;
+      tt = p->d.pml ? ht + (int64_t)it * 3 * NSP : tt0;
+    }
+    estep<T, NN>(p, g, it, cf, wav, stt, tt, vin, vout, s);
+    if (full && !p->d.pml) {
+      // ABL: stresses evolve in tt0; keep a copy of this step's stresses for the adjoint
+      ADFWI_CUDA_TRY(cudaMemcpyAsync(ht + (int64_t)it * 3 * NSP, tt0, 3 * NSP * sizeof(T), cudaMemcpyDeviceToDevice, s));
+    }
+    if (rec && p->d.nr > 0) {
+      dim3 gr((unsigned)((p->d.nr + 127) / 128), p->d.ns);
+      ADFWI_LAUNCH(kAux, s, (el::record<T><<<gr, 128, 0, s>>>(g, it, tt, vout, static_cast<T*>(rec))));
+    }
+    if (fw && chunk < p->chunk_end.size() && it == p->chunk_end[chunk]) {
+      const int64_t n = (int64_t)p->d.nz * p->d.nx;
+      ADFWI_LAUNCH(kAux, s, (el::energy<T><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(g, tt, vout, static_cast<T*>(fw))));
+      ++chunk;
+    }
+  }
+  ADFWI_CUDA_TRY(cudaGetLastError());
+  return kOk;
+}
+
+template <typename T, int NN>
+int ebackward(const adfwi_elastic_plan* p, const void* wavelet, const void* grec, void* const* gcoef,
+              const int32_t* shapes, unsigned char* ws, int64_t ws_bytes, cudaStream_t s) {
+  const int K = p->K;
+  ECarve c = ecarve(p, true, K);
+  if (ws_bytes < c.total) {
+    set_error("workspace too small: %lld bytes given, %lld needed", (long long)ws_bytes, (long long)c.total);
+    return kWorkspaceTooSmall;
+  }
+  el::Geo<T> g = egeo<T>(p, ws, c);
+  const int ns = p->d.ns, nt = p->d.nt;
+  const int64_t PL = p->L.plane, NSP = (int64_t)ns * PL;
+  const bool full = K >= nt;
+  const T* cf = reinterpret_cast<const T*>(ws + c.coef);
+  const T* wav = static_cast<const T*>(wavelet);
+  T* stt = reinterpret_cast<T*>(ws + c.st);
+  T* tt0 = reinterpret_cast<T*>(ws + c.tt);
+  T* v0 = reinterpret_cast<T*>(ws + c.vtmp);
+  T* hv = reinterpret_cast<T*>(ws + c.hv);
+  T* ht = reinterpret_cast<T*>(ws + c.ht);
+  T* lst = reinterpret_cast<T*>(ws + c.lst);
+  T* lt = reinterpret_cast<T*>(ws + c.lt);
+  T* lv = reinterpret_cast<T*>(ws + c.lv);
+  T* lv2 = reinterpret_cast<T*>(ws + c.lv2);
+  T* gcp = reinterpret_cast<T*>(ws + c.gc);
+  const T* gr = static_cast<const T*>(grec);
+  const int nsf = p->d.pml ? 10 : 3;
+  ADFWI_CUDA_TRY(cudaMemsetAsync(lst, 0, nsf * NSP * sizeof(T), s));
+  ADFWI_CUDA_TRY(cudaMemsetAsync(lt, 0, 3 * NSP * sizeof(T), s));
+  ADFWI_CUDA_TRY(cudaMemsetAsync(lv, 0, 2 * NSP * sizeof(T), s));
+  ADFWI_CUDA_TRY(cudaMemsetAsync(gcp, 0, 8 * PL * sizeof(T), s));
+  const dim3 gcs = cells_grid(p, ns), gc1 = cells_grid(p, 1), b(256);
+  const dim3 gcol((unsigned)((p->nxp + 127) / 128), ns);
+  const dim3 ginj((unsigned)std::max(1, (p->ncells + 127) / 128), ns);
+  const int nseg = full ? 1 : (nt + K - 1) / K;
+  for (int seg = nseg - 1; seg >= 0; --seg) {
+    const int t0 = full ? 0 : seg * K;
+    const int t1 = full ? nt : std::min(nt, t0 + K);
+    if (!full) {
+      // restore the state at t0 (v totals straight into Hv[0]) and recompute the segment
+      int rc = p->d.pml ? esnap<T>(p, false, ws, c, stt, 10 * ns, hv, 2 * ns, seg, s)
+                        : esnap<T>(p, false, ws, c, tt0, 3 * ns, hv, 2 * ns, seg, s);
+      if (rc) return rc;
+      for (int it = t0; it < t1; ++it) {
+        const int k = it - t0;
+        T* vin = hv + (int64_t)k * 2 * NSP;
+        T* vout = k + 1 < K && it + 1 < t1 ? hv + (int64_t)(k + 1) * 2 * NSP : v0;
+        T* tt = p->d.pml ? ht + (int64_t)k * 3 * NSP : tt0;
+        if (!p->d.pml && vout != vin) ADFWI_CUDA_TRY(cudaMemcpyAsync(vout, vin, 2 * NSP * sizeof(T), cudaMemcpyDeviceToDevice, s));
+        estep<T, NN>(p, g, it, cf, wav, stt, tt, p->d.pml ? vin : vout, vout, s);
+        if (!p->d.pml) ADFWI_CUDA_TRY(cudaMemcpyAsync(ht + (int64_t)k * 3 * NSP, tt0, 3 * NSP * sizeof(T), cudaMemcpyDeviceToDevice, s));
+      }
+    }
+    for (int it = t1 - 1; it >= t0; --it) {
+      const int k = it - t0;
+      const T* vh = hv + (int64_t)k * 2 * NSP;  // velocity totals at the start of step it
+      const T* th = ht + (int64_t)k * 3 * NSP;  // stress totals of step it
+      if (p->d.pml) {
+        ADFWI_CUDA_TRY(cudaMemsetAsync(lt, 0, 3 * NSP * sizeof(T), s));
+        if (gr) ADFWI_LAUNCH(kAux, s, (el::adj_inject<T><<<ginj, 128, 0, s>>>(g, it, gr, lt, lv, 1)));
+        ADFWI_LAUNCH(kElAdjStep, s, (el::adj_vfs_pml<T><<<gcs, b, 0, s>>>(g, cf, lv, lst + 6 * NSP)));
+        ADFWI_LAUNCH(kElAdjStep, s, (el::adj_t_pml<T, NN><<<gc1, b, 0, s>>>(g, cf, lst + 6 * NSP, lt, th,
+                                                                            gcp + 6 * PL, gcp + 7 * PL)));
+        ADFWI_LAUNCH(kElAdjStep, s, (el::adj_tfs_pml<T><<<gcs, b, 0, s>>>(g, cf, lt, lst)));
+        ADFWI_LAUNCH(kElAdjStep, s, (el::adj_v<T, NN, true><<<gc1, b, 0, s>>>(g, cf, lst, lv, vh, gcp)));
+      } else {
+        if (gr) ADFWI_LAUNCH(kAux, s, (el::adj_inject<T><<<ginj, 128, 0, s>>>(g, it, gr, lst, lv, 1)));
+        ADFWI_LAUNCH(kElAdjStep, s, (el::adj_vfs_abl<T><<<gcs, b, 0, s>>>(g, cf, lv, lv2, nullptr)));
+        std::swap(lv, lv2);
+        ADFWI_LAUNCH(kElAdjStep, s, (el::adj_t_abl<T, NN><<<gc1, b, 0, s>>>(g, cf, lv, lst, th, gcp + 6 * PL,
+                                                                            gcp + 7 * PL)));
+        if (p->d.free_surface) ADFWI_LAUNCH(kElAdjStep, s, (el::adj_tfs_abl<T><<<gcol, 128, 0, s>>>(g, lst)));
+        ADFWI_LAUNCH(kElAdjStep, s, (el::adj_v<T, NN, false><<<gc1, b, 0, s>>>(g, cf, lst, lv, vh, gcp)));
+      }
+    }
+    ADFWI_CUDA_TRY(cudaGetLastError());
+  }
+  // gradients out: C11 C13 C15 C33 C35 C55 bx bz, each cropped to its input shape
+  for (int q = 0; q < 8; ++q) {
+    if (gcoef[q] == nullptr) continue;
+    const int h = shapes[2 * q], w = shapes[2 * q + 1];
+    const int64_t n = (int64_t)h * w;
+    ADFWI_LAUNCH(kAux, s, (el::unpack<T><<<(unsigned)std::min<int64_t>((n + 255) / 256, 4096), 256, 0, s>>>(
+                              p->L, h, w, gcp + q * PL, static_cast<T*>(gcoef[q]))));
+  }
+  ADFWI_CUDA_TRY(cudaGetLastError());
+  return kOk;
+}
+
+}  // namespace
+
+extern "C" {
+
+int adfwi_elastic_plan_create(const adfwi_elastic_desc* desc, const int32_t* src_z, const int32_t* src_x,
+                              const int32_t* rcv_z, const int32_t* rcv_x, const double* moment_tensor,
+                              adfwi_elastic_plan** out) {
+  ADFWI_CHECK_ARG(desc && out, "null descriptor or output pointer");
+  *out = nullptr;
+  const adfwi_elastic_desc& d = *desc;
+  ADFWI_CHECK_ARG(d.fd_order == 4 || d.fd_order == 6, "fd_order must be 4 or 6");
+  ADFWI_CHECK_ARG(d.nz >= 3 && d.nx >= 3 && d.nabc >= 1, "need nz, nx >= 3 and nabc >= 1");
+  ADFWI_CHECK_ARG(d.ns >= 1 && d.nt >= 1 && d.nr >= 0, "need ns >= 1, nt >= 1, nr >= 0");
+  ADFWI_CHECK_ARG(d.dtype == ADFWI_F32 || d.dtype == ADFWI_F64, "dtype must be ADFWI_F32 or ADFWI_F64");
+  ADFWI_CHECK_ARG(d.checkpoint_segments >= 1, "checkpoint_segments must be >= 1");
+  ADFWI_CHECK_ARG(d.snapshot_precision >= 0 && d.snapshot_precision <= 2, "bad snapshot_precision");
+  ADFWI_CHECK_ARG(src_z && src_x && moment_tensor && (d.nr == 0 || (rcv_z && rcv_x)), "null geometry array");
+  adfwi_elastic_plan* p = new (std::nothrow) adfwi_elastic_plan();
+  if (!p) {
+    set_error("host allocation failed");
+    return kBadArgument;
+  }
+  p->d = d;
+  p->NN = d.fd_order / 2;
+  p->h = p->NN + 1;
+  const int fs_off = d.fd_order / 2;
+  p->nxp = d.nx + 2 * d.nabc;
+  p->nzp = d.nz + (d.free_surface ? d.nabc + fs_off : 2 * d.nabc + fs_off);
+  p->top = d.free_surface ? fs_off : fs_off + d.nabc;
+  p->elem = d.dtype == ADFWI_F64 ? 8 : 4;
+  p->nstate = d.pml ? 12 : 5;
+  p->L = make_layout(p->nzp, p->nxp, 16, 64, p->elem);
+  std::vector<int32_t>& t = p->tab;
+  p->o_srcz = t.size();
+  for (int s = 0; s < d.ns; ++s) {
+    const int z = src_z[s] + p->top, x = src_x[s] + d.nabc;
+    if (z < 0 || z >= p->nzp || x < 0 || x >= p->nxp) {
+      set_error("source %d at (z=%d, x=%d) lies outside the model", s, src_z[s], src_x[s]);
+      delete p;
+      return kBadGeometry;
+    }
+    t.push_back(z);
+  }
+  p->o_srcx = t.size();
+  for (int s = 0; s < d.ns; ++s) t.push_back(src_x[s] + d.nabc);
+  // source weights: PML adds -MT/2 * w to both split parts, ABL adds -1/3 * MT * w
+  p->srcm.resize((size_t)3 * d.ns * p->elem);
+  for (int s = 0; s < d.ns; ++s) {
+    const double* m = moment_tensor + 9 * s;
+    const int idx[3] = {0, 8, 2};  // MT[0,0], MT[2,2], MT[0,2]
+    for (int k = 0; k < 3; ++k) {
+      unsigned char* dst = p->srcm.data() + (size_t)(3 * s + k) * p->elem;
+      if (d.dtype == ADFWI_F32) {
+        const float mv = (float)m[idx[k]];
+        const float w = d.pml ? -(mv / 2.0f) : (float)(-1.0 / 3.0) * mv;
+        memcpy(dst, &w, sizeof(w));
+      } else {
+        const double w = d.pml ? -(m[idx[k]] / 2.0) : (-1.0 / 3.0) * m[idx[k]];
+        memcpy(dst, &w, sizeof(w));
+      }
+    }
+  }
+  p->o_rcvz = t.size();
+  for (int r = 0; r < d.nr; ++r) {
+    const int z = rcv_z[r] + p->top, x = rcv_x[r] + d.nabc;
+    if (z < 0 || z >= p->nzp || x < 0 || x >= p->nxp) {
+      set_error("receiver %d at (z=%d, x=%d) lies outside the model", r, rcv_z[r], rcv_x[r]);
+      delete p;
+      return kBadGeometry;
+    }
+    t.push_back(z);
+  }
+  p->o_rcvx = t.size();
+  for (int r = 0; r < d.nr; ++r) t.push_back(rcv_x[r] + d.nabc);
+  // unique receiver cells
+  std::vector<std::pair<int, int>> cells(d.nr);
+  for (int r = 0; r < d.nr; ++r) cells[r] = {((rcv_z[r] + p->top) << 16) | (rcv_x[r] + d.nabc), r};
+  std::stable_sort(cells.begin(), cells.end());
+  std::vector<int32_t> uzx, ubeg, urcv;
+  for (int q = 0; q < d.nr; ++q) {
+    if (q == 0 || cells[q].first != cells[q - 1].first) {
+      uzx.push_back(cells[q].first);
+      ubeg.push_back((int32_t)urcv.size());
+    }
+    urcv.push_back(cells[q].second);
+  }
+  ubeg.push_back((int32_t)urcv.size());
+  p->ncells = (int)uzx.size();
+  p->o_uzx = t.size();
+  t.insert(t.end(), uzx.begin(), uzx.end());
+  p->o_ubeg = t.size();
+  t.insert(t.end(), ubeg.begin(), ubeg.end());
+  p->o_urcv = t.size();
+  t.insert(t.end(), urcv.begin(), urcv.end());
+  if (t.empty()) t.push_back(0);
+  // torch.chunk(wavelet, checkpoint_segments): the energy maps keep the last step of each chunk
+  const int chunk = (d.nt + d.checkpoint_segments - 1) / d.checkpoint_segments;
+  for (int e = chunk - 1; e < d.nt; e += chunk) p->chunk_end.push_back(e);
+  if (p->chunk_end.empty() || p->chunk_end.back() != d.nt - 1) p->chunk_end.push_back(d.nt - 1);
+  p->K = echoose_K(p);
+  p->nseg = (d.nt + p->K - 1) / p->K;
+  *out = p;
+  return kOk;
+}
+
+void adfwi_elastic_plan_destroy(adfwi_elastic_plan* p) { delete p; }
+
+int adfwi_elastic_workspace_bytes(const adfwi_elastic_plan* p, int32_t with_gradient, int64_t* bytes) {
+  ADFWI_CHECK_ARG(p && bytes, "null plan or output pointer");
+  *bytes = ecarve(p, with_gradient != 0, with_gradient ? p->K : 1).total;
+  return kOk;
+}
+
+int adfwi_elastic_snapshot_every(const adfwi_elastic_plan* p, int32_t* steps) {
+  ADFWI_CHECK_ARG(p && steps, "null plan or output pointer");
+  *steps = p->K;
+  return kOk;
+}
+
+int adfwi_elastic_forward(const adfwi_elastic_plan* p, const void* const* coef, const int32_t* shapes,
+                          const void* wavelet, void* rec, void* fw, int32_t with_gradient, void* workspace,
+                          int64_t workspace_bytes, void* stream) {
+  ADFWI_CHECK_ARG(p && coef && shapes && wavelet && workspace, "null argument");
+  for (int q = 0; q < ncoef(p); ++q) ADFWI_CHECK_ARG(coef[q] != nullptr, "coefficient %d is null", q);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  unsigned char* ws = static_cast<unsigned char*>(workspace);
+  const bool g = with_gradient != 0;
+  if (p->d.dtype == ADFWI_F64)
+    return p->NN == 2 ? eforward<double, 2>(p, coef, shapes, wavelet, rec, fw, g, ws, workspace_bytes, s)
+                      : eforward<double, 3>(p, coef, shapes, wavelet, rec, fw, g, ws, workspace_bytes, s);
+  return p->NN == 2 ? eforward<float, 2>(p, coef, shapes, wavelet, rec, fw, g, ws, workspace_bytes, s)
+                    : eforward<float, 3>(p, coef, shapes, wavelet, rec, fw, g, ws, workspace_bytes, s);
+}
+
+int adfwi_elastic_backward(const adfwi_elastic_plan* p, const void* wavelet, const void* grad_rec,
+                           void* const* grad_coef, const int32_t* shapes, void* workspace, int64_t workspace_bytes,
+                           void* stream) {
+  ADFWI_CHECK_ARG(p && wavelet && grad_coef && shapes && workspace, "null argument");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  unsigned char* ws = static_cast<unsigned char*>(workspace);
+  if (p->d.dtype == ADFWI_F64)
+    return p->NN == 2 ? ebackward<double, 2>(p, wavelet, grad_rec, grad_coef, shapes, ws, workspace_bytes, s)
+                      : ebackward<double, 3>(p, wavelet, grad_rec, grad_coef, shapes, ws, workspace_bytes, s);
+  return p->NN == 2 ? ebackward<float, 2>(p, wavelet, grad_rec, grad_coef, shapes, ws, workspace_bytes, s)
+                    : ebackward<float, 3>(p, wavelet, grad_rec, grad_coef, shapes, ws, workspace_bytes, s);
+}
+
+}  // extern "C"

@@ -166,3 +166,79 @@ class AcousticPropagator(_PropagatorBase):
         rp, ru, rw, fp, fu, fw = AcousticSolve.apply(alpha1, alpha2, self.damp, wav, plan)
         return {"p": rp, "u": ru, "w": rw, "forward_wavefield_p": fp, "forward_wavefield_u": fu,
                 "forward_wavefield_w": fw}
+
+
+class ElasticPropagator(_PropagatorBase):
+    """Isotropic / VTI / HTI elastic velocity-stress propagator (elastic_propagator.py:20-142)."""
+
+    def __init__(self, model, survey, device: Optional[str] = "cpu", cpu_num: Optional[int] = 1,
+                 gpu_num: Optional[int] = 1, dtype=torch.float32, *, snapshot_precision="native", snapshot_every=0,
+                 memory_budget=None):
+        super().__init__(model, survey, device, cpu_num, gpu_num, dtype, snapshot_precision, snapshot_every,
+                         memory_budget, 0)
+
+    def boundary_condition(self):
+        """bcx / bcz (abc_type "PML", case-sensitive as elastic_propagator.py:100) or a damping frame."""
+        if self.abc_type == "PML":
+            vmax = self.model.vp.cpu().detach().numpy().max()
+            bcx, bcz = bc_pml_xz(self.nx, self.nz, self.dx, self.dz, pml=self.nabc, vmax=vmax,
+                                 free_surface=self.free_surface)
+            self.bcx = numpy2tensor(bcx, self.dtype).to(self._dev)
+            self.bcz = numpy2tensor(bcz, self.dtype).to(self._dev)
+        elif self.abc_type == "gerjan":
+            damp = bc_gerjan(self.nx, self.nz, self.dx, self.dz, pml=self.nabc, alpha=self.model.abc_jerjan_alpha,
+                             free_surface=self.free_surface)
+            self.damp = numpy2tensor(damp, self.dtype).to(self._dev)
+        else:
+            damp = bc_sincos(self.nx, self.nz, self.dx, self.dz, pml=self.nabc, free_surface=self.free_surface)
+            self.damp = numpy2tensor(damp, self.dtype).to(self._dev)
+
+    def plan(self, shot_index=None, fd_order=4, checkpoint_segments=1):
+        from .elastic import ElasticPlan
+        idx = self._select(shot_index)
+        key = (idx.tobytes(), int(fd_order), int(checkpoint_segments))
+        p = self._plans.get(key)
+        if p is None:
+            p = ElasticPlan(nz=self.nz, nx=self.nx, nabc=self.nabc, free_surface=self.free_surface,
+                            src_z=self.src_loc[idx, 1], src_x=self.src_loc[idx, 0], rcv_z=self.rcv_loc[:, 1],
+                            rcv_x=self.rcv_loc[:, 0],
+                            moment_tensor=self.moment_tensor.detach().cpu().double().numpy()[idx],
+                            nt=self.nt, dt=self.dt, dx=self.dx, dz=self.dz, dtype=self.dtype, fd_order=fd_order,
+                            pml=self.abc_type.lower() == "pml", checkpoint_segments=checkpoint_segments,
+                            snapshot_every=self.snapshot_every, snapshot_precision=self.snapshot_precision,
+                            memory_budget=self._budget())
+            self._plans[key] = p
+        return idx, p
+
+    def padded_coefficients(self, model=None, fd_order=4):
+        """Padded C11, C13, C15, C33, C35, C55, bx, bz and boundary arrays (elastic_kernels.py:928-953)."""
+        model = self.model if model is None else model
+        fs_off = fd_order // 2
+        n = self.nabc
+        top = fs_off if self.free_surface else fs_off + n
+        pad = lambda a: _pad_replicate(a, top, n, n, n)  # noqa: E731
+        CC = model.CC
+        coefs = [pad(CC[k]) for k in (0, 2, 4, 11, 13, 18)] + [pad(model.bx), pad(model.bz)]
+        coefs = [c.to(self.dtype) if c.dtype != self.dtype else c for c in coefs]
+        bpad = lambda a: _pad_replicate(a, fs_off, 0, 0, 0)  # noqa: E731
+        if self.abc_type.lower() == "pml":
+            if self.bcx is None:
+                raise ValueError("abc_type %r selects the PML kernel but no bcx/bcz were built (the reference "
+                                 "builds them only for abc_type == 'PML')" % self.abc_type)
+            abc = [bpad(self.bcx), bpad(self.bcz)]
+        else:
+            abc = [bpad(self.damp), None]
+        return coefs, abc
+
+    def forward(self, model=None, shot_index=None, fd_order=4, checkpoint_segments=1) -> Dict[str, Tensor]:
+        from .elastic import COMPONENTS, ElasticSolve
+        model = self.model if model is None else model
+        model.forward()
+        idx, plan = self.plan(shot_index, fd_order, checkpoint_segments)
+        coefs, abc = self.padded_coefficients(model, fd_order)
+        wav = self._wavelet_rows(idx)
+        outs = ElasticSolve.apply(*coefs, abc[0], abc[1], wav, plan)
+        rec = {k: outs[q] for q, k in enumerate(COMPONENTS)}
+        for q, k in enumerate(COMPONENTS):
+            rec["forward_wavefield_" + k] = outs[5 + q]
+        return rec

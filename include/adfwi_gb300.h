@@ -100,6 +100,58 @@ int adfwi_acoustic_backward(const adfwi_acoustic_plan* plan, const void* alpha1,
                             const void* grad_rec_w, void* grad_alpha1, void* grad_alpha2,
                             void* workspace, int64_t workspace_bytes, void* stream);
 
+/* ------------------------------------------------------------------------- */
+/* Elastic velocity-stress (vx, vz, txx, tzz, txz), 4th / 6th order staggered grid. */
+/* ------------------------------------------------------------------------- */
+
+typedef struct adfwi_elastic_desc {
+  int32_t nz, nx;             /* model cells before padding                                     */
+  int32_t nabc;               /* absorbing cells (left, right, bottom; top too without a free surface) */
+  int32_t free_surface;       /* 0 / 1                                                          */
+  int32_t ns, nt, nr;         /* shots, time steps, receivers                                   */
+  int32_t dtype;              /* ADFWI_F32 / ADFWI_F64                                          */
+  int32_t fd_order;           /* 4 or 6                                                         */
+  int32_t pml;                /* 1: split-field PML (bcx, bcz); 0: multiplicative layer (damp)  */
+  int32_t checkpoint_segments;/* reference chunk count; shapes the forward_wavefield_* maps      */
+  int32_t snapshot_every;     /* steps between gradient snapshots; 0 = automatic                */
+  int32_t snapshot_precision; /* ADFWI_SNAP_*                                                   */
+  int32_t reserved;
+  double dt, dx, dz;
+  double fdc[3];              /* staggered coefficients (DiffCoef, float32-rounded), fd_order/2 used */
+  int64_t memory_budget;      /* byte cap for the gradient workspace; 0 = no cap                */
+} adfwi_elastic_desc;
+
+typedef struct adfwi_elastic_plan adfwi_elastic_plan; /* opaque */
+
+/* Plan from HOST geometry in model cells (before padding) and the moment tensors (ns x 3 x 3,
+ * row-major doubles). Replaces elastic_propagator.py:81-96 and elastic_kernels.py:955-959. */
+int adfwi_elastic_plan_create(const adfwi_elastic_desc* desc, const int32_t* src_z,
+                              const int32_t* src_x, const int32_t* rcv_z, const int32_t* rcv_x,
+                              const double* moment_tensor, adfwi_elastic_plan** plan);
+void adfwi_elastic_plan_destroy(adfwi_elastic_plan* plan);
+int adfwi_elastic_workspace_bytes(const adfwi_elastic_plan* plan, int32_t with_gradient,
+                                  int64_t* bytes);
+int adfwi_elastic_snapshot_every(const adfwi_elastic_plan* plan, int32_t* steps);
+
+/* Forward solve: replaces elastic_kernels.py:917-1037 forward_kernel.
+ * coef[10] = padded C11, C13, C15, C33, C35, C55, bx, bz, bcx, bcz (pml = 1) or
+ * coef[9] = ... bx, bz, damp (pml = 0), each dense with its own padded shape given in
+ * shapes[2*q], shapes[2*q+1] (the reference's padding keeps bx (nz, nx-1), bz (nz-1, nx) and
+ * C55 (nz-2, nx-2) smaller). wavelet: (ns, nt). rec: 5 x (ns, nt, nr) for txx, tzz, txz, vx, vz.
+ * fw: 5 x (nz, nx) forward_wavefield_* maps, or NULL. */
+int adfwi_elastic_forward(const adfwi_elastic_plan* plan, const void* const* coef,
+                          const int32_t* shapes, const void* wavelet, void* rec, void* fw,
+                          int32_t with_gradient, void* workspace, int64_t workspace_bytes,
+                          void* stream);
+
+/* Adjoint solve after a with_gradient forward on the same workspace: replaces the autograd
+ * backward through elastic_kernels.py:975-1008. grad_rec: 5 x (ns, nt, nr) or NULL.
+ * grad_coef[8]: outputs dL/d(C11, C13, C15, C33, C35, C55, bx, bz) with the shapes of the
+ * first 8 coefficient inputs (entries may be NULL). */
+int adfwi_elastic_backward(const adfwi_elastic_plan* plan, const void* wavelet,
+                           const void* grad_rec, void* const* grad_coef, const int32_t* shapes,
+                           void* workspace, int64_t workspace_bytes, void* stream);
+
 /* Device status of the last solve run in `workspace` (same with_gradient as that solve):
  * 0 = clean, 1 = a bounded pipeline wait inside a kernel ran out (results invalid).
  * Waits for the stream. */

@@ -8,15 +8,15 @@
 //   ADFWI/propagator/acoustic_kernels.py:252-265  alpha / kappa coefficient definitions
 //   ADFWI/propagator/acoustic_kernels.py:268-301  chunked time loop and the record dict
 //
-// One launch advances one time step of all shots. A thread block owns a TZ x TX tile of one
-// grid and loops over a group of shots, so that the coefficient tiles it stages in shared
-// memory are reused by every shot of the group. Within a shot the block computes the new
-// pressure on the tile plus a halo (1 row/column before, 2 after) from u and w staged in
-// shared memory, and then the new u and w on the tile from that pressure: p, u and w each
-// cross HBM once per step (ping-pong buffers keep the Jacobi semantics of the reference's
-// slice assignments). The forward arithmetic uses explicitly rounded operations (no FMA
+// One launch advances one time step of all shots (acoustic_tma.cuh): persistent, warp-
+// specialised blocks stream (tile, shot) items through a TMA / mbarrier pipeline; per item
+// the consumers compute the new pressure on a 16 x 64 tile plus its halo (1 row / column
+// before, 2 after) and then the new u and w on the tile, so p, u and w each cross HBM once
+// per step (ping-pong buffers keep the Jacobi semantics of the reference's slice
+// assignments). The forward arithmetic uses explicitly rounded operations (no FMA
 // contraction) in the reference's evaluation order, so float32 records reproduce the
-// reference's PyTorch CPU results bit for bit.
+// reference's PyTorch CPU results bit for bit. The adjoint step is the exact transpose of
+// the forward step, in reverse operation order.
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string.h>
@@ -34,16 +34,6 @@
 
 namespace adfwi {
 namespace ac {
-
-constexpr int TX = 32;        // tile columns = threads in x
-constexpr int TZ = 16;        // tile rows
-constexpr int BY = 8;         // thread rows
-constexpr int RPT = TZ / BY;  // tile rows per thread
-constexpr int NT = TX * BY;   // threads per block
-constexpr int EZ = TZ + 3, EX = TX + 3;  // p halo region: rows i0-1..i0+TZ+1, cols j0-1..j0+TX+1
-constexpr int UZ = TZ + 3, UX = TX + 6;  // u region: rows i0-1..i0+TZ+1, cols j0-3..j0+TX+2
-constexpr int WZ = TZ + 6, WX = TX + 3;  // w region: rows i0-3..i0+TZ+2, cols j0-1..j0+TX+1
-constexpr int AZ = TZ + 6, AX = TX + 6;  // union of the u and w regions (adjoint alpha2)
 
 // Explicitly rounded arithmetic (keeps the reference's operation order; no FMA contraction).
 __device__ __forceinline__ float radd(float a, float b) { return __fadd_rn(a, b); }
@@ -93,356 +83,9 @@ __device__ __forceinline__ bool in_window(const Geo<T>& g, int i, int j) {
   return i >= g.nabc && i < g.nabc + g.nz && j >= g.nabc && j < g.nabc + g.nx;
 }
 
-template <typename T>
-struct FwdSmem {
-  T su[UZ][UX];
-  T sw[WZ][WX];
-  T sp[EZ][EX];
-  T sa1[EZ][EX];
-  T sd[EZ][EX];
-  T sa2[TZ][TX];
-  T sou[TZ][TX];
-  T sow[TZ][TX];
-};
-
-// Divergence c1*(u[j]-u[j-1]+w[i]-w[i-1]) + c2*(u[j+1]-u[j-2]+w[i+1]-w[i-2]) in the
-// reference's left-to-right order; (r, c) are p-halo coordinates of (i, j).
-template <typename T>
-__device__ __forceinline__ T divergence(const FwdSmem<T>& s, const Geo<T>& g, int r, int c) {
-  T t1 = rsub(radd(rsub(s.su[r][c + 2], s.su[r][c + 1]), s.sw[r + 2][c]), s.sw[r + 1][c]);
-  T t2 = rsub(radd(rsub(s.su[r][c + 3], s.su[r][c]), s.sw[r + 3][c]), s.sw[r][c]);
-  return radd(rmul(g.c1, t1), rmul(g.c2, t2));
-}
-
-// New pressure at grid cell (i, j) with p-halo coordinates (r, c), before the mirror.
-template <typename T>
-__device__ __forceinline__ T eval_p(const FwdSmem<T>& s, const Geo<T>& g, const T* __restrict__ P0,
-                                    int i, int j, int r, int c, int sz, int sx, T sval) {
-  T v = P0[g.L.off(i, j)];
-  if (in_p(g, i, j)) {
-    T k1 = rmul(s.sd[r][c], g.dt);
-    v = rsub(rmul(rsub(T(1), k1), v), rmul(s.sa1[r][c], divergence(s, g, r, c)));
-  }
-  if (i == sz && j == sx) v = radd(v, sval);
-  return v;
-}
-
-// One forward time step of shots [blockIdx.z*G, ...). Optional outputs may be null.
-template <typename T>
-__global__ void __launch_bounds__(NT) fwd_step(
-    Geo<T> g, int it, int G, int accum_u, const T* __restrict__ a1, const T* __restrict__ a2,
-    const T* __restrict__ damp, const T* __restrict__ wav, const T* __restrict__ p0,
-    const T* __restrict__ u0, const T* __restrict__ w0, T* __restrict__ p1, T* __restrict__ u1,
-    T* __restrict__ w1, T* __restrict__ d1, T* __restrict__ rec_p, T* __restrict__ rec_u,
-    T* __restrict__ rec_w, T* __restrict__ ill_p, T* __restrict__ ill_u) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  FwdSmem<T>& s = *reinterpret_cast<FwdSmem<T>*>(smem_raw);
-  const Layout L = g.L;
-  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
-  const int tile = blockIdx.y * g.tiles_x + blockIdx.x;
-  const int i0 = g.zbeg + blockIdx.y * TZ, j0 = blockIdx.x * TX;
-
-  for (int e = tid; e < EZ * EX; e += NT) {
-    int r = e / EX, c = e - r * EX;
-    int64_t o = L.off(i0 - 1 + r, j0 - 1 + c);
-    s.sa1[r][c] = a1[o];
-    s.sd[r][c] = damp[o];
-  }
-#pragma unroll
-  for (int k = 0; k < RPT; ++k) s.sa2[ty + BY * k][tx] = a2[L.off(i0 + ty + BY * k, j0 + tx)];
-
-  T acc_p[RPT], acc_u[RPT];
-#pragma unroll
-  for (int k = 0; k < RPT; ++k) acc_p[k] = acc_u[k] = T(0);
-
-  const int s_beg = blockIdx.z * G, s_end = min(g.ns, s_beg + G);
-  const int rb = g.tile_rcv_beg[tile], re = g.tile_rcv_beg[tile + 1];
-  for (int sh = s_beg; sh < s_end; ++sh) {
-    const int64_t so = (int64_t)sh * L.plane;
-    const T* P0 = p0 + so;
-    const T* U0 = u0 + so;
-    const T* W0 = w0 + so;
-    for (int e = tid; e < UZ * UX; e += NT) {
-      int r = e / UX, c = e - r * UX;
-      s.su[r][c] = U0[L.off(i0 - 1 + r, j0 - 3 + c)];
-    }
-    for (int e = tid; e < WZ * WX; e += NT) {
-      int r = e / WX, c = e - r * WX;
-      s.sw[r][c] = W0[L.off(i0 - 3 + r, j0 - 1 + c)];
-    }
-    __syncthreads();
-    const int sz = g.src_z[sh], sx = g.src_x[sh];
-    const T sval = rmul(g.dt, wav[(int64_t)sh * g.nt + it]);
-    for (int e = tid; e < EZ * EX; e += NT) {
-      int r = e / EX, c = e - r * EX;
-      int i = i0 - 1 + r, j = j0 - 1 + c;
-      T v = T(0);
-      if (i >= g.zbeg && i < L.nzp && j >= 0 && j < L.nxp) {
-        if (g.fsurf && i == g.fs - 1)  // p[fs-1] = -p[fs+1]  (acoustic_kernels.py:135-136)
-          v = -eval_p(s, g, P0, i + 2, j, r + 2, c, sz, sx, sval);
-        else
-          v = eval_p(s, g, P0, i, j, r, c, sz, sx, sval);
-      }
-      s.sp[r][c] = v;
-    }
-    __syncthreads();
-#pragma unroll
-    for (int k = 0; k < RPT; ++k) {
-      const int li = ty + BY * k;
-      const int i = i0 + li, j = j0 + tx;
-      const int r = li + 1, c = tx + 1;
-      T pv = s.sp[r][c];
-      // u update (acoustic_kernels.py:139-148)
-      T uo = s.su[r][c + 2];
-      T un = uo;
-      if (in_u(g, i, j)) {
-        T k2 = rmul(rmul(T(0.5), radd(s.sd[r][c], s.sd[r][c + 1])), g.dt);
-        T dpx = radd(rmul(g.c1, rsub(s.sp[r][c + 1], s.sp[r][c])),
-                     rmul(g.c2, rsub(s.sp[r][c + 2], s.sp[r][c - 1])));
-        un = rsub(rmul(rsub(T(1), k2), uo), rmul(s.sa2[li][tx], dpx));
-      }
-      // w update (acoustic_kernels.py:151-160); w[fs-1] = w[fs] mirror (163-164)
-      const int ie = (g.fsurf && i == g.fs - 1) ? g.fs : i;
-      const int rr = r + (ie - i);
-      T wo = s.sw[rr + 2][c];
-      T wn = wo;
-      if (in_w(g, ie, j)) {
-        T k3 = rmul(rmul(T(0.5), radd(s.sd[rr][c], s.sd[rr + 1][c])), g.dt);
-        T dpz = radd(rmul(g.c1, rsub(s.sp[rr + 1][c], s.sp[rr][c])),
-                     rmul(g.c2, rsub(s.sp[rr + 2][c], s.sp[rr - 1][c])));
-        wn = rsub(rmul(rsub(T(1), k3), wo), rmul(s.sa2[rr - 1][tx], dpz));
-      }
-      s.sou[li][tx] = un;
-      s.sow[li][tx] = wn;
-      if (i < L.nzp && j < L.nxp) {
-        const int64_t o = so + L.off(i, j);
-        p1[o] = pv;
-        u1[o] = un;
-        w1[o] = wn;
-        if (d1 != nullptr) d1[o] = in_p(g, i, j) ? divergence(s, g, r, c) : T(0);
-        if (in_window(g, i, j)) {
-          acc_p[k] += pv * pv;
-          acc_u[k] += un * un;
-        }
-      }
-    }
-    __syncthreads();
-    if (rec_p != nullptr && ty == 0) {
-      const int64_t rowbase = ((int64_t)sh * g.nt + it) * g.nr;
-      for (int q = rb + tx; q < re; q += TX) {
-        int cell = g.trcv_cell[q];
-        int li = cell >> 16, lj = cell & 0xffff;
-        int64_t o = rowbase + g.trcv_id[q];
-        rec_p[o] = s.sp[li + 1][lj + 1];
-        rec_u[o] = s.sou[li][lj];
-        rec_w[o] = s.sow[li][lj];
-      }
-    }
-  }
-  if (ill_p != nullptr) {
-    const int64_t go = (int64_t)blockIdx.z * L.plane;
-#pragma unroll
-    for (int k = 0; k < RPT; ++k) {
-      const int i = i0 + ty + BY * k, j = j0 + tx;
-      if (i < L.nzp && j < L.nxp && in_window(g, i, j)) {
-        ill_p[go + L.off(i, j)] += acc_p[k];
-        if (accum_u) ill_u[go + L.off(i, j)] += acc_u[k];
-      }
-    }
-  }
-}
-
-template <typename T>
-struct AdjSmem {
-  T qu[UZ][UX];  // -alpha2 * lambda_u on the u region (zero outside the u update region)
-  T qw[WZ][WX];  // -alpha2 * lambda_w on the w region
-  T lp[EZ][EX];  // lambda_p after the u/w transposes and the free-surface fold
-  T ph[EZ][EX];  // forward pressure after this step (history)
-  T sa1[EZ][EX];
-  T sd[EZ][EX];
-  T sa2[AZ][AX];
-  T op[TZ][TX];
-  T ou[TZ][TX];
-  T ow[TZ][TX];
-};
-
-template <typename T>
-__device__ __forceinline__ T adj_lp(const AdjSmem<T>& s, const Geo<T>& g, const T* __restrict__ LP0,
-                                    int i, int j, int r, int c) {
-  // lambda_p + D_x^T(q_u) + D_z^T(q_w): transposes of the forward differences of p used by
-  // the u and w updates (acoustic_kernels.py:143-146, 155-158).
-  T v = LP0[g.L.off(i, j)];
-  v += g.c1 * (s.qu[r][c + 1] - s.qu[r][c + 2]) + g.c2 * (s.qu[r][c] - s.qu[r][c + 3]);
-  v += g.c1 * (s.qw[r + 1][c] - s.qw[r + 2][c]) + g.c2 * (s.qw[r][c] - s.qw[r + 3][c]);
-  return v;
-}
-
-template <typename T>
-__device__ __forceinline__ T qp_at(const AdjSmem<T>& s, const Geo<T>& g, int i, int j, int r, int c) {
-  return in_p(g, i, j) ? -s.sa1[r][c] * s.lp[r][c] : T(0);
-}
-
-// Reverse of forward step `it`. Input lambda = dL/d(state after step it) including the
-// receiver injection of step it and the w-mirror fold; output = the same for step it-1.
-// Accumulates dL/d alpha1 and dL/d alpha2 of this step into per-group partial planes.
-template <typename T>
-__global__ void __launch_bounds__(NT) adj_step(
-    Geo<T> g, int it, int G, const T* __restrict__ a1, const T* __restrict__ a2,
-    const T* __restrict__ damp, const T* __restrict__ lp0, const T* __restrict__ lu0,
-    const T* __restrict__ lw0, T* __restrict__ lp1, T* __restrict__ lu1, T* __restrict__ lw1,
-    const T* __restrict__ phist, const T* __restrict__ dhist, const T* __restrict__ gr_p,
-    const T* __restrict__ gr_u, const T* __restrict__ gr_w, T* __restrict__ g1,
-    T* __restrict__ g2) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  AdjSmem<T>& s = *reinterpret_cast<AdjSmem<T>*>(smem_raw);
-  const Layout L = g.L;
-  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
-  const int tile = blockIdx.y * g.tiles_x + blockIdx.x;
-  const int i0 = g.zbeg + blockIdx.y * TZ, j0 = blockIdx.x * TX;
-
-  for (int e = tid; e < EZ * EX; e += NT) {
-    int r = e / EX, c = e - r * EX;
-    int64_t o = L.off(i0 - 1 + r, j0 - 1 + c);
-    s.sa1[r][c] = a1[o];
-    s.sd[r][c] = damp[o];
-  }
-  for (int e = tid; e < AZ * AX; e += NT) {
-    int r = e / AX, c = e - r * AX;
-    s.sa2[r][c] = a2[L.off(i0 - 3 + r, j0 - 3 + c)];
-  }
-  __syncthreads();
-
-  T ag1[RPT], ag2[RPT];
-#pragma unroll
-  for (int k = 0; k < RPT; ++k) ag1[k] = ag2[k] = T(0);
-
-  const int s_beg = blockIdx.z * G, s_end = min(g.ns, s_beg + G);
-  const int cb = g.tile_cell_beg[tile], ce = g.tile_cell_beg[tile + 1];
-  const bool inject = (it >= 1) && (gr_p != nullptr || gr_u != nullptr || gr_w != nullptr);
-  for (int sh = s_beg; sh < s_end; ++sh) {
-    const int64_t so = (int64_t)sh * L.plane;
-    const T* LP0 = lp0 + so;
-    const T* LU0 = lu0 + so;
-    const T* LW0 = lw0 + so;
-    const T* PH = phist + so;
-    for (int e = tid; e < UZ * UX; e += NT) {
-      int r = e / UX, c = e - r * UX;
-      int i = i0 - 1 + r, j = j0 - 3 + c;
-      s.qu[r][c] = in_u(g, i, j) ? -s.sa2[r + 2][c] * LU0[L.off(i, j)] : T(0);
-    }
-    for (int e = tid; e < WZ * WX; e += NT) {
-      int r = e / WX, c = e - r * WX;
-      int i = i0 - 3 + r, j = j0 - 1 + c;
-      s.qw[r][c] = in_w(g, i, j) ? -s.sa2[r][c + 2] * LW0[L.off(i, j)] : T(0);
-    }
-    for (int e = tid; e < EZ * EX; e += NT) {
-      int r = e / EX, c = e - r * EX;
-      s.ph[r][c] = PH[L.off(i0 - 1 + r, j0 - 1 + c)];
-    }
-    __syncthreads();
-    for (int e = tid; e < EZ * EX; e += NT) {
-      int r = e / EX, c = e - r * EX;
-      int i = i0 - 1 + r, j = j0 - 1 + c;
-      T v = T(0);
-      if (i >= 0 && i < L.nzp && j >= 0 && j < L.nxp) {
-        if (g.fsurf && i == g.fs - 1) {
-          v = T(0);  // adjoint of p[fs-1] = -p[fs+1]: the mirrored row carries no sensitivity
-        } else {
-          v = adj_lp(s, g, LP0, i, j, r, c);
-          if (g.fsurf && i == g.fs + 1 && r >= 2) v -= adj_lp(s, g, LP0, i - 2, j, r - 2, c);
-        }
-      }
-      s.lp[r][c] = v;
-    }
-    __syncthreads();
-    const T* DH = dhist + so;
-#pragma unroll
-    for (int k = 0; k < RPT; ++k) {
-      const int li = ty + BY * k;
-      const int i = i0 + li, j = j0 + tx;
-      const int r = li + 1, c = tx + 1;
-      T lpm = s.lp[r][c];
-      T lpo = lpm;
-      T qc = qp_at(s, g, i, j, r, c);
-      if (in_p(g, i, j)) {
-        lpo = (T(1) - s.sd[r][c] * g.dt) * lpm;
-        ag1[k] -= lpm * DH[L.off(i, j)];
-      }
-      const int64_t oo = L.off(i, j);
-      T luin = (i < L.nzp && j < L.nxp) ? LU0[oo] : T(0);
-      T lwin = (i < L.nzp && j < L.nxp) ? LW0[oo] : T(0);
-      T luo = luin, lwo = lwin;
-      if (in_u(g, i, j)) {
-        T k2 = T(0.5) * (s.sd[r][c] + s.sd[r][c + 1]) * g.dt;
-        luo = (T(1) - k2) * luin;
-        T dpx = g.c1 * (s.ph[r][c + 1] - s.ph[r][c]) + g.c2 * (s.ph[r][c + 2] - s.ph[r][c - 1]);
-        ag2[k] -= luin * dpx;
-      }
-      if (in_w(g, i, j)) {
-        T k3 = T(0.5) * (s.sd[r][c] + s.sd[r + 1][c]) * g.dt;
-        lwo = (T(1) - k3) * lwin;
-        T dpz = g.c1 * (s.ph[r + 1][c] - s.ph[r][c]) + g.c2 * (s.ph[r + 2][c] - s.ph[r - 1][c]);
-        ag2[k] -= lwin * dpz;
-      }
-      // transposes of the p update's differences of u and w (acoustic_kernels.py:119-126)
-      luo += g.c1 * (qc - qp_at(s, g, i, j + 1, r, c + 1)) +
-             g.c2 * (qp_at(s, g, i, j - 1, r, c - 1) - qp_at(s, g, i, j + 2, r, c + 2));
-      lwo += g.c1 * (qc - qp_at(s, g, i + 1, j, r + 1, c)) +
-             g.c2 * (qp_at(s, g, i - 1, j, r - 1, c) - qp_at(s, g, i + 2, j, r + 2, c));
-      s.op[li][tx] = lpo;
-      s.ou[li][tx] = luo;
-      s.ow[li][tx] = lwo;
-    }
-    __syncthreads();
-    if (inject && ty == 0) {
-      // dL/d records of step it-1 enter the state after step it-1 (acoustic_kernels.py:167-169)
-      const int64_t rowbase = ((int64_t)sh * g.nt + (it - 1)) * g.nr;
-      for (int q = cb + tx; q < ce; q += TX) {
-        int cell = g.tcell_cell[q];
-        int li = cell >> 16, lj = cell & 0xffff;
-        T ap = T(0), au = T(0), aw = T(0);
-        for (int m = g.tcell_rbeg[q]; m < g.tcell_rbeg[q + 1]; ++m) {
-          int64_t o = rowbase + g.cell_rcv[m];
-          if (gr_p) ap += gr_p[o];
-          if (gr_u) au += gr_u[o];
-          if (gr_w) aw += gr_w[o];
-        }
-        s.op[li][lj] += ap;
-        s.ou[li][lj] += au;
-        s.ow[li][lj] += aw;
-      }
-    }
-    __syncthreads();
-#pragma unroll
-    for (int k = 0; k < RPT; ++k) {
-      const int li = ty + BY * k;
-      const int i = i0 + li, j = j0 + tx;
-      if (i < L.nzp && j < L.nxp) {
-        const int64_t o = so + L.off(i, j);
-        T wv = s.ow[li][tx];
-        if (g.fsurf && i == g.fs - 1) wv = T(0);                    // adjoint of w[fs-1] = w[fs]
-        if (g.fsurf && i == g.fs && li >= 1) wv += s.ow[li - 1][tx];
-        lp1[o] = s.op[li][tx];
-        lu1[o] = s.ou[li][tx];
-        lw1[o] = wv;
-      }
-    }
-    __syncthreads();
-  }
-  const int64_t go = (int64_t)blockIdx.z * L.plane;
-#pragma unroll
-  for (int k = 0; k < RPT; ++k) {
-    const int i = i0 + ty + BY * k, j = j0 + tx;
-    if (i < L.nzp && j < L.nxp) {
-      g1[go + L.off(i, j)] += ag1[k];
-      g2[go + L.off(i, j)] += ag2[k];
-    }
-  }
-}
-
 // Seed of the reverse pass: lambda = injection of the records of the last step.
 template <typename T>
-__global__ void adj_seed(Geo<T> g, int ntiles, const T* __restrict__ gr_p, const T* __restrict__ gr_u,
+__global__ void adj_seed(Geo<T> g, int ntiles, int tz, int tx, const T* __restrict__ gr_p, const T* __restrict__ gr_u,
                          const T* __restrict__ gr_w, T* lp, T* lu, T* lw) {
   const int sh = blockIdx.y;
   const int64_t rowbase = ((int64_t)sh * g.nt + (g.nt - 1)) * g.nr;
@@ -458,8 +101,8 @@ __global__ void adj_seed(Geo<T> g, int ntiles, const T* __restrict__ gr_p, const
       tile = lo;
     }
     int cell = g.tcell_cell[q];
-    int i = g.zbeg + (tile / g.tiles_x) * TZ + (cell >> 16);
-    int j = (tile % g.tiles_x) * TX + (cell & 0xffff);
+    int i = g.zbeg + (tile / g.tiles_x) * tz + (cell >> 16);
+    int j = (tile % g.tiles_x) * tx + (cell & 0xffff);
     T ap = T(0), au = T(0), aw = T(0);
     for (int m = g.tcell_rbeg[q]; m < g.tcell_rbeg[q + 1]; ++m) {
       int64_t o = rowbase + g.cell_rcv[m];
@@ -521,6 +164,33 @@ __global__ void illum_finalize(Layout L, int groups, int ns, int nabc, int nz, i
   }
 }
 
+// Masked coefficient planes for the branch-free pipelined kernels, computed with the
+// reference's own operations (acoustic_kernels.py:257-265, and 1 - kappa of 115-160):
+//   A1M = alpha1 on the p region, 0 elsewhere;  B1 = 1 - damp*dt on the p region, 1 elsewhere;
+//   A2U / A2W = alpha2 on the u / w regions, 0 elsewhere;
+//   B2 / B3 = 1 - 0.5*(d + d_right)*dt / 1 - 0.5*(d + d_below)*dt on the u / w regions, 1 elsewhere.
+// Ghost cells stay 0. Planes follow the raw a1, a2, damp planes in the coefficient block.
+enum { kA1 = 0, kA2 = 1, kDamp = 2, kA1M = 3, kB1 = 4, kA2U = 5, kA2W = 6, kB2 = 7, kB3 = 8, kNumCoef = 9 };
+
+template <typename T>
+__global__ void mask_coefficients(Geo<T> g, T* cf) {
+  const Layout L = g.L;
+  const int64_t n = (int64_t)L.nzp * L.nxp;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(e / L.nxp), j = (int)(e - (int64_t)i * L.nxp);
+    const int64_t o = L.off(i, j);
+    const T* d = cf + kDamp * L.plane;
+    const T a1 = cf[kA1 * L.plane + o], a2 = cf[kA2 * L.plane + o];
+    const bool pin = in_p(g, i, j), uin = in_u(g, i, j), win = in_w(g, i, j);
+    cf[kA1M * L.plane + o] = pin ? a1 : T(0);
+    cf[kB1 * L.plane + o] = pin ? rsub(T(1), rmul(d[o], g.dt)) : T(1);
+    cf[kA2U * L.plane + o] = uin ? a2 : T(0);
+    cf[kB2 * L.plane + o] = uin ? rsub(T(1), rmul(rmul(T(0.5), radd(d[o], d[o + 1])), g.dt)) : T(1);
+    cf[kA2W * L.plane + o] = win ? a2 : T(0);
+    cf[kB3 * L.plane + o] = win ? rsub(T(1), rmul(rmul(T(0.5), radd(d[o], d[o + L.pitch])), g.dt)) : T(1);
+  }
+}
+
 }  // namespace ac
 }  // namespace adfwi
 
@@ -544,8 +214,7 @@ struct Tiling {
 struct adfwi_acoustic_plan {
   adfwi_acoustic_desc d;
   int nzp, nxp, fs, zbeg;
-  Tiling t1;             // 16 x 32 tiles of the adjoint step
-  Tiling t2;             // 16 x 64 tiles of the TMA forward step
+  Tiling t2;             // 16 x 64 tiles of the pipelined forward and adjoint steps
   int K, nseg;           // snapshot interval and number of segments (gradient mode)
   int last_chunk_start;  // first step of the reference's last checkpoint chunk
   int elem;              // bytes per element
@@ -570,7 +239,7 @@ Carve carve(const adfwi_acoustic_plan* p, bool grad, int K) {
   const int64_t ns = p->d.ns;
   int64_t o = 0;
   auto take = [&](int64_t bytes) { int64_t at = o; o += align256(bytes); return at; };
-  c.coef = take(3 * pl);
+  c.coef = take(ac::kNumCoef * pl);
   c.fa = take(3 * ns * pl);
   c.fb = take(3 * ns * pl);
   c.ilp = take((int64_t)p->t2.ngroups * pl);
@@ -587,8 +256,8 @@ Carve carve(const adfwi_acoustic_plan* p, bool grad, int K) {
     c.hd = take((int64_t)K * ns * pl);
     c.la = take(3 * ns * pl);
     c.lb = take(3 * ns * pl);
-    c.g1 = take((int64_t)p->t1.ngroups * pl);
-    c.g2 = take((int64_t)p->t1.ngroups * pl);
+    c.g1 = take((int64_t)p->t2.ngroups * pl);
+    c.g2 = take((int64_t)p->t2.ngroups * pl);
   }
   c.total = o;
   return c;
@@ -664,48 +333,88 @@ int setup_common(const adfwi_acoustic_plan* p, unsigned char* ws, const Carve& c
                                 p->L, p->nzp, p->nxp, static_cast<const T*>(src[q]),
                                 reinterpret_cast<T*>(reinterpret_cast<unsigned char*>(cf) + q * pl))));
   }
+  ac::Geo<T> g = make_geo<T>(p, ws, c, p->t2);
+  ADFWI_LAUNCH(kAux, st, (ac::mask_coefficients<T><<<grid_blocks(n), 256, 0, st>>>(g, cf)));
   ADFWI_CUDA_TRY(cudaGetLastError());
   return kOk;
 }
 
 template <typename T>
 int tma_stages() {
-  return sizeof(T) == 8 ? 2 : 3;
+  return sizeof(T) == 8 ? 2 : 4;
+}
+template <typename T>
+int tma_adj_stages() {
+  return 2;
+}
+
+template <typename T>
+ac2::StepArgs<T> step_args(const adfwi_acoustic_plan* p, int it, const T* cf, int* flag) {
+  ac2::StepArgs<T> a;
+  memset(&a, 0, sizeof(a));
+  a.it = it;
+  a.G = p->t2.G;
+  a.ngroups = p->t2.ngroups;
+  a.ntiles = p->t2.ntiles;
+  a.cf = cf;
+  a.flag = flag;
+  return a;
 }
 
 template <typename T>
 int launch_fwd(const adfwi_acoustic_plan* p, const ac::Geo<T>& g, int it, int accum_u, const T* cf,
                const T* wav, const T* p0, const T* u0, const T* w0, T* p1, T* u1, T* w1, T* d1, T* rp, T* ru,
                T* rw, T* ilp, T* ilu, int* flag, cudaStream_t st) {
-  const Tiling& t = p->t2;
   const int64_t ns = p->d.ns;
   ac2::Maps maps;
-  int rc = make_plane_map(&maps.u, u0, sizeof(T), p->L, ns, ac2::BOXX, ac2::EZ);
-  if (!rc) rc = make_plane_map(&maps.w, w0, sizeof(T), p->L, ns, ac2::BOXX, ac2::WZ);
-  if (!rc) rc = make_plane_map(&maps.p, p0, sizeof(T), p->L, ns, ac2::BOXX, ac2::EZ);
-  if (!rc) rc = make_plane_map(&maps.coef, cf, sizeof(T), p->L, 3, ac2::BOXX, ac2::EZ);
+  int rc = make_plane_map(&maps.a, u0, sizeof(T), p->L, ns, ac2::BOXX, ac2::EZ);
+  if (!rc) rc = make_plane_map(&maps.b, w0, sizeof(T), p->L, ns, ac2::BOXX, ac2::WZ);
+  if (!rc) rc = make_plane_map(&maps.c, p0, sizeof(T), p->L, ns, ac2::BOXX, ac2::EZ);
   if (rc) return rc;
-  ac2::FwdArgs<T> a;
-  a.it = it;
-  a.G = t.G;
-  a.ngroups = t.ngroups;
-  a.ntiles = t.ntiles;
+  ac2::StepArgs<T> a = step_args<T>(p, it, cf, flag);
   a.accum_u = accum_u;
   a.stages = tma_stages<T>();
   a.wav = wav;
-  a.p1 = p1;
-  a.u1 = u1;
-  a.w1 = w1;
+  a.o0 = p1;
+  a.o1 = u1;
+  a.o2 = w1;
   a.d1 = d1;
   a.rec_p = rp;
   a.rec_u = ru;
   a.rec_w = rw;
-  a.ill_p = ilp;
-  a.ill_u = ilu;
-  a.flag = flag;
+  a.acc0 = ilp;
+  a.acc1 = ilu;
   const int smem = ac2::FwdLayout<T>::bytes(a.stages);
   ADFWI_LAUNCH(kAcFwdStep, st,
-               (ac2::fwd_step_tma<T><<<t.blocks, ac2::NTHREADS, smem, st>>>(maps, g, a)));
+               (ac2::fwd_step_tma<T><<<p->t2.blocks, ac2::NTHREADS, smem, st>>>(maps, g, a)));
+  return kOk;
+}
+
+template <typename T>
+int launch_adj(const adfwi_acoustic_plan* p, const ac::Geo<T>& g, int it, const T* cf, const T* lp0, const T* lu0,
+               const T* lw0, T* lp1, T* lu1, T* lw1, const T* ph, const T* dh, const T* gp, const T* gu, const T* gw,
+               T* g1, T* g2, int* flag, cudaStream_t st) {
+  const int64_t ns = p->d.ns;
+  ac2::Maps maps;
+  int rc = make_plane_map(&maps.a, lu0, sizeof(T), p->L, ns, ac2::BOXX, ac2::EZ);
+  if (!rc) rc = make_plane_map(&maps.b, lw0, sizeof(T), p->L, ns, ac2::BOXX, ac2::WZ);
+  if (!rc) rc = make_plane_map(&maps.c, lp0, sizeof(T), p->L, ns, ac2::BOXX, ac2::EZ);
+  if (!rc) rc = make_plane_map(&maps.d, ph, sizeof(T), p->L, ns, ac2::BOXX, ac2::EZ);
+  if (!rc) rc = make_plane_map(&maps.e, dh, sizeof(T), p->L, ns, ac2::BOXX, ac2::EZ);
+  if (rc) return rc;
+  ac2::StepArgs<T> a = step_args<T>(p, it, cf, flag);
+  a.stages = tma_adj_stages<T>();
+  a.o0 = lp1;
+  a.o1 = lu1;
+  a.o2 = lw1;
+  a.rec_p = gp;
+  a.rec_u = gu;
+  a.rec_w = gw;
+  a.acc0 = g1;
+  a.acc1 = g2;
+  const int smem = ac2::AdjLayout<T>::bytes(a.stages);
+  ADFWI_LAUNCH(kAcAdjStep, st,
+               (ac2::adj_step_tma<T><<<p->t2.blocks, ac2::NTHREADS, smem, st>>>(maps, g, a)));
   return kOk;
 }
 
@@ -713,12 +422,10 @@ template <typename T>
 int set_smem_limits() {
   static bool done = false;
   if (!done) {
-    ADFWI_CUDA_TRY(cudaFuncSetAttribute(ac::fwd_step<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)sizeof(ac::FwdSmem<T>)));
-    ADFWI_CUDA_TRY(cudaFuncSetAttribute(ac::adj_step<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)sizeof(ac::AdjSmem<T>)));
     ADFWI_CUDA_TRY(cudaFuncSetAttribute(ac2::fwd_step_tma<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         ac2::FwdLayout<T>::bytes(tma_stages<T>())));
+    ADFWI_CUDA_TRY(cudaFuncSetAttribute(ac2::adj_step_tma<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        ac2::AdjLayout<T>::bytes(tma_adj_stages<T>())));
     done = true;
   }
   return kOk;
@@ -797,8 +504,7 @@ int backward_impl(const adfwi_acoustic_plan* p, const void* wavelet, const void*
     set_error("workspace too small: %lld bytes given, %lld needed", (long long)ws_bytes, (long long)c.total);
     return kWorkspaceTooSmall;
   }
-  ac::Geo<T> g2 = make_geo<T>(p, ws, c, p->t2);  // recomputation (TMA forward step)
-  ac::Geo<T> g1 = make_geo<T>(p, ws, c, p->t1);  // adjoint step
+  ac::Geo<T> g2 = make_geo<T>(p, ws, c, p->t2);
   const int64_t pl = p->L.plane;
   const int64_t ns = p->d.ns;
   const int nt = p->d.nt;
@@ -820,18 +526,16 @@ int backward_impl(const adfwi_acoustic_plan* p, const void* wavelet, const void*
 
   ADFWI_CUDA_TRY(cudaMemsetAsync(la, 0, 3 * ns * pl * sizeof(T), st));
   ADFWI_CUDA_TRY(cudaMemsetAsync(lb, 0, 3 * ns * pl * sizeof(T), st));
-  ADFWI_CUDA_TRY(cudaMemsetAsync(g1p, 0, (size_t)p->t1.ngroups * pl * sizeof(T), st));
-  ADFWI_CUDA_TRY(cudaMemsetAsync(g2p, 0, (size_t)p->t1.ngroups * pl * sizeof(T), st));
+  ADFWI_CUDA_TRY(cudaMemsetAsync(g1p, 0, (size_t)p->t2.ngroups * pl * sizeof(T), st));
+  ADFWI_CUDA_TRY(cudaMemsetAsync(g2p, 0, (size_t)p->t2.ngroups * pl * sizeof(T), st));
   if (gp || gu || gw) {
-    dim3 sg(std::max(1, std::min(64, (p->t1.ncells + 127) / 128)), p->d.ns);
-    ADFWI_LAUNCH(kAux, st, (ac::adj_seed<T><<<sg, 128, 0, st>>>(g1, p->t1.ntiles, gp, gu, gw, la, la + ns * pl,
-                                                                   la + 2 * ns * pl)));
+    dim3 sg(std::max(1, std::min(64, (p->t2.ncells + 127) / 128)), p->d.ns);
+    ADFWI_LAUNCH(kAux, st, (ac::adj_seed<T><<<sg, 128, 0, st>>>(g2, p->t2.ntiles, ac2::TZ, ac2::TX, gp, gu, gw, la,
+                                                                   la + ns * pl, la + 2 * ns * pl)));
   }
   T* lcur = la;
   T* lnxt = lb;
   const int nseg = full ? 1 : (nt + K - 1) / K;
-  dim3 grid(p->t1.tiles_x, p->t1.tiles_z, p->t1.ngroups);
-  dim3 block(ac::TX, ac::BY);
   for (int seg = nseg - 1; seg >= 0; --seg) {
     const int t0 = full ? 0 : seg * K;
     const int t1 = full ? nt : std::min(nt, t0 + K);
@@ -852,18 +556,18 @@ int backward_impl(const adfwi_acoustic_plan* p, const void* wavelet, const void*
       }
     }
     for (int it = t1 - 1; it >= t0; --it) {
-      ADFWI_LAUNCH(kAcAdjStep, st, (ac::adj_step<T><<<grid, block, sizeof(ac::AdjSmem<T>), st>>>(
-          g1, it, p->t1.G, cf, cf + pl, cf + 2 * pl, lcur, lcur + ns * pl, lcur + 2 * ns * pl, lnxt, lnxt + ns * pl,
-          lnxt + 2 * ns * pl, hp + (int64_t)(it - t0) * ns * pl, hd + (int64_t)(it - t0) * ns * pl, gp, gu, gw, g1p,
-          g2p)));
+      rc = launch_adj<T>(p, g2, it, cf, lcur, lcur + ns * pl, lcur + 2 * ns * pl, lnxt, lnxt + ns * pl,
+                         lnxt + 2 * ns * pl, hp + (int64_t)(it - t0) * ns * pl, hd + (int64_t)(it - t0) * ns * pl, gp,
+                         gu, gw, g1p, g2p, flag, st);
+      if (rc) return rc;
       std::swap(lcur, lnxt);
     }
     ADFWI_CUDA_TRY(cudaGetLastError());
   }
   const int64_t n = (int64_t)p->nzp * p->nxp;
-  ADFWI_LAUNCH(kAux, st, (ac::reduce_planes<T><<<grid_blocks(n), 256, 0, st>>>(p->L, p->t1.ngroups, 0, 0, p->nzp,
+  ADFWI_LAUNCH(kAux, st, (ac::reduce_planes<T><<<grid_blocks(n), 256, 0, st>>>(p->L, p->t2.ngroups, 0, 0, p->nzp,
                                                                                 p->nxp, g1p, static_cast<T*>(ga1))));
-  ADFWI_LAUNCH(kAux, st, (ac::reduce_planes<T><<<grid_blocks(n), 256, 0, st>>>(p->L, p->t1.ngroups, 0, 0, p->nzp,
+  ADFWI_LAUNCH(kAux, st, (ac::reduce_planes<T><<<grid_blocks(n), 256, 0, st>>>(p->L, p->t2.ngroups, 0, 0, p->nzp,
                                                                                 p->nxp, g2p, static_cast<T*>(ga2))));
   ADFWI_CUDA_TRY(cudaGetLastError());
   return kOk;
@@ -1082,17 +786,7 @@ int adfwi_acoustic_plan_create(const adfwi_acoustic_desc* desc, const int32_t* s
       return kBadGeometry;
     }
   }
-  // 16 x 32 tiles (adjoint step): enough blocks to fill the GPU (about 8 resident per SM).
-  int G1 = d.shots_per_block;
-  {
-    const int ntiles = ((p->nxp + ac::TX - 1) / ac::TX) * ((p->nzp - p->zbeg + ac::TZ - 1) / ac::TZ);
-    if (G1 <= 0) {
-      const int groups = std::min(d.ns, std::max(1, (152 * 8 + ntiles - 1) / ntiles));
-      G1 = (d.ns + groups - 1) / groups;
-    }
-  }
-  build_tiling(p, &p->t1, ac::TZ, ac::TX, G1, rcv_z, rcv_x);
-  // 16 x 64 tiles (TMA forward step): units of G shots spread over the resident blocks.
+  // 16 x 64 tiles: units of G shots spread over the resident blocks of the pipelined steps.
   {
     const int ntiles = ((p->nxp + ac2::TX - 1) / ac2::TX) * ((p->nzp - p->zbeg + ac2::TZ - 1) / ac2::TZ);
     const int blocks = p->elem == 8 ? resident_tma_blocks<double>() : resident_tma_blocks<float>();

@@ -29,6 +29,7 @@
 
 #include "../../include/adfwi_gb300.h"
 #include "common.cuh"
+#include "frames.cuh"
 #include "snapshot.cuh"
 #include "tma.cuh"
 
@@ -220,6 +221,7 @@ struct adfwi_acoustic_plan {
   int elem;              // bytes per element
   Layout L;
   std::vector<int32_t> tab;  // geometry tables, uploaded into the workspace
+  PinnedBytes tab_pin;       // page-locked copy of tab, the source of each upload
   int64_t o_srcz, o_srcx;
 };
 
@@ -324,7 +326,7 @@ int setup_common(const adfwi_acoustic_plan* p, unsigned char* ws, const Carve& c
   // Zero coefficient planes (ghosts), field buffers and illumination partials.
   ADFWI_CUDA_TRY(cudaMemsetAsync(ws + c.coef, 0, c.tab - c.coef, st));
   ADFWI_CUDA_TRY(cudaMemsetAsync(ws + c.flag, 0, 256, st));
-  ADFWI_CUDA_TRY(cudaMemcpyAsync(ws + c.tab, p->tab.data(), p->tab.size() * 4, cudaMemcpyHostToDevice, st));
+  ADFWI_CUDA_TRY(cudaMemcpyAsync(ws + c.tab, p->tab_pin.ptr, p->tab.size() * 4, cudaMemcpyHostToDevice, st));
   const int64_t n = (int64_t)p->nzp * p->nxp;
   T* cf = reinterpret_cast<T*>(ws + c.coef);
   const void* src[3] = {alpha1, alpha2, damp};
@@ -458,6 +460,11 @@ int forward_impl(const adfwi_acoustic_plan* p, const void* alpha1, const void* a
   const bool full = grad && K >= p->d.nt;
   T* hp = grad ? reinterpret_cast<T*>(ws + c.hp) : nullptr;
   T* hd = grad ? reinterpret_cast<T*>(ws + c.hd) : nullptr;
+  if (full) {
+    // the pressure history is read with its halo (as the next step's input and by the adjoint)
+    rc = zero_frames<T>(hp, (int64_t)K * ns, p->L, st);
+    if (rc) return rc;
+  }
   T* cur = fa;
   T* nxt = fb;
   for (int it = 0; it < p->d.nt; ++it) {
@@ -528,6 +535,11 @@ int backward_impl(const adfwi_acoustic_plan* p, const void* wavelet, const void*
   ADFWI_CUDA_TRY(cudaMemsetAsync(lb, 0, 3 * ns * pl * sizeof(T), st));
   ADFWI_CUDA_TRY(cudaMemsetAsync(g1p, 0, (size_t)p->t2.ngroups * pl * sizeof(T), st));
   ADFWI_CUDA_TRY(cudaMemsetAsync(g2p, 0, (size_t)p->t2.ngroups * pl * sizeof(T), st));
+  if (!full) {
+    // the recomputed pressure history is read with its halo by the next step and the adjoint
+    rc = zero_frames<T>(hp, (int64_t)K * ns, p->L, st);
+    if (rc) return rc;
+  }
   if (gp || gu || gw) {
     dim3 sg(std::max(1, std::min(64, (p->t2.ncells + 127) / 128)), p->d.ns);
     ADFWI_LAUNCH(kAux, st, (ac::adj_seed<T><<<sg, 128, 0, st>>>(g2, p->t2.ntiles, ac2::TZ, ac2::TX, gp, gu, gw, la,
@@ -797,6 +809,10 @@ int adfwi_acoustic_plan_create(const adfwi_acoustic_desc* desc, const int32_t* s
   }
   if (t.empty()) t.push_back(0);
 
+  if (!p->tab_pin.assign(p->tab.data(), p->tab.size() * 4)) {
+    delete p;
+    return kCudaError;
+  }
   p->K = choose_K(p);
   p->nseg = (d.nt + p->K - 1) / p->K;
   *out = p;

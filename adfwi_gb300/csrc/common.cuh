@@ -60,6 +60,25 @@ enum Status : int {
 // Thread-local last-error text, read through adfwi_last_error().
 void set_error(const char* fmt, ...);
 
+// Host copy of a plan's tables, page-locked when the CUDA runtime can give page-locked
+// memory. Uploading from page-locked memory is a stream-ordered asynchronous copy (a
+// pageable source makes the copy wait for the stream), so a solve enqueues without host
+// stalls and can be captured into a CUDA graph. Without a device (plans built on a host
+// without a GPU, for sizing) the copy is ordinary heap memory.
+struct PinnedBytes {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+  bool pinned = false;
+  PinnedBytes() = default;
+  PinnedBytes(const PinnedBytes&) = delete;
+  PinnedBytes& operator=(const PinnedBytes&) = delete;
+  ~PinnedBytes() { release(); }
+  void release();
+  // Copies n bytes from src; returns false (with the error text set) when no host memory
+  // can be had at all.
+  bool assign(const void* src, size_t n);
+};
+
 }  // namespace adfwi
 
 #define ADFWI_CUDA_TRY(expr)                                                      \

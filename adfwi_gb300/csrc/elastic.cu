@@ -28,6 +28,7 @@
 
 #include "../../include/adfwi_gb300.h"
 #include "common.cuh"
+#include "frames.cuh"
 #include "snapshot.cuh"
 
 namespace adfwi {
@@ -785,6 +786,7 @@ struct adfwi_elastic_plan {
   Layout L;
   std::vector<int32_t> tab;
   std::vector<unsigned char> srcm;  // ns x 3 source weights (xx, zz, xz) in the solve's dtype
+  PinnedBytes tab_pin, srcm_pin;    // page-locked copies of tab and srcm, the sources of each upload
   int64_t o_srcz, o_srcx, o_rcvz, o_rcvx, o_uzx, o_ubeg, o_urcv;
   int ncells;
   std::vector<int> chunk_end;  // last step of each reference checkpoint chunk
@@ -902,8 +904,8 @@ int esetup(const adfwi_elastic_plan* p, unsigned char* ws, const ECarve& c, cons
            const int32_t* shapes, cudaStream_t st) {
   const int64_t pl = p->L.plane * p->elem;
   ADFWI_CUDA_TRY(cudaMemsetAsync(ws, 0, c.srcm, st));  // coefficient ghosts, state, totals
-  ADFWI_CUDA_TRY(cudaMemcpyAsync(ws + c.tab, p->tab.data(), p->tab.size() * 4, cudaMemcpyHostToDevice, st));
-  ADFWI_CUDA_TRY(cudaMemcpyAsync(ws + c.srcm, p->srcm.data(), p->srcm.size(), cudaMemcpyHostToDevice, st));
+  ADFWI_CUDA_TRY(cudaMemcpyAsync(ws + c.tab, p->tab_pin.ptr, p->tab.size() * 4, cudaMemcpyHostToDevice, st));
+  ADFWI_CUDA_TRY(cudaMemcpyAsync(ws + c.srcm, p->srcm_pin.ptr, p->srcm.size(), cudaMemcpyHostToDevice, st));
   for (int q = 0; q < ncoef(p); ++q) {
     const int h = shapes[2 * q], w = shapes[2 * q + 1];
     if (h < 1 || w < 1 || h > p->nzp || w > p->nxp) {
@@ -983,6 +985,12 @@ int eforward(const adfwi_elastic_plan* p, const void* const* coef, const int32_t
   T* ht = grad ? reinterpret_cast<T*>(ws + c.ht) : nullptr;
   const int nt = p->d.nt;
   if (fw) ADFWI_CUDA_TRY(cudaMemsetAsync(fw, 0, 5 * (int64_t)p->d.nz * p->d.nx * sizeof(T), s));
+  if (full) {
+    // the histories double as the state and are read with their halos
+    int rc0 = zero_frames<T>(hv, (int64_t)K * 2 * p->d.ns, p->L, s);
+    if (!rc0 && p->d.pml) rc0 = zero_frames<T>(ht, (int64_t)K * 3 * p->d.ns, p->L, s);
+    if (rc0) return rc0;
+  }
   size_t chunk = 0;
   for (int it = 0; it < nt; ++it) {
     if (grad && !full && it % K == 0) {
@@ -1053,6 +1061,13 @@ int ebackward(const adfwi_elastic_plan* p, const void* wavelet, const void* grec
   ADFWI_CUDA_TRY(cudaMemsetAsync(lt, 0, 3 * NSP * sizeof(T), s));
   ADFWI_CUDA_TRY(cudaMemsetAsync(lv, 0, 2 * NSP * sizeof(T), s));
   ADFWI_CUDA_TRY(cudaMemsetAsync(gcp, 0, 8 * PL * sizeof(T), s));
+  ADFWI_CUDA_TRY(cudaMemsetAsync(lv2, 0, 2 * NSP * sizeof(T), s));
+  if (!full) {
+    // recomputed histories are read with their halos
+    int rc0 = zero_frames<T>(hv, (int64_t)K * 2 * ns, p->L, s);
+    if (!rc0 && p->d.pml) rc0 = zero_frames<T>(ht, (int64_t)K * 3 * ns, p->L, s);
+    if (rc0) return rc0;
+  }
   const dim3 gcs = cells_grid(p, ns), gc1 = cells_grid(p, 1), b(256);
   const dim3 gcol((unsigned)((p->nxp + 127) / 128), ns);
   const dim3 ginj((unsigned)std::max(1, (p->ncells + 127) / 128), ns);
@@ -1210,6 +1225,10 @@ int adfwi_elastic_plan_create(const adfwi_elastic_desc* desc, const int32_t* src
   const int chunk = (d.nt + d.checkpoint_segments - 1) / d.checkpoint_segments;
   for (int e = chunk - 1; e < d.nt; e += chunk) p->chunk_end.push_back(e);
   if (p->chunk_end.empty() || p->chunk_end.back() != d.nt - 1) p->chunk_end.push_back(d.nt - 1);
+  if (!p->tab_pin.assign(p->tab.data(), p->tab.size() * 4) || !p->srcm_pin.assign(p->srcm.data(), p->srcm.size())) {
+    delete p;
+    return kCudaError;
+  }
   p->K = echoose_K(p);
   p->nseg = (d.nt + p->K - 1) / p->K;
   *out = p;

@@ -1,5 +1,6 @@
 // Error reporting and build information of the C ABI.
 #include <stdarg.h>
+#include <stdlib.h>
 #include <stdio.h>
 #include <string.h>
 
@@ -17,6 +18,36 @@ void set_error(const char* fmt, ...) {
   va_start(ap, fmt);
   vsnprintf(g_last_error, sizeof(g_last_error), fmt, ap);
   va_end(ap);
+}
+
+void PinnedBytes::release() {
+  if (ptr) {
+    if (pinned)
+      cudaFreeHost(ptr);
+    else
+      free(ptr);
+  }
+  ptr = nullptr;
+  bytes = 0;
+  pinned = false;
+}
+
+bool PinnedBytes::assign(const void* src, size_t n) {
+  release();
+  if (n == 0) return true;
+  if (cudaMallocHost(&ptr, n) == cudaSuccess) {
+    pinned = true;
+  } else {
+    (void)cudaGetLastError();  // no usable device here: keep a pageable copy
+    ptr = malloc(n);
+    if (ptr == nullptr) {
+      set_error("host allocation of %zu bytes for plan tables failed", n);
+      return false;
+    }
+  }
+  memcpy(ptr, src, n);
+  bytes = n;
+  return true;
 }
 
 }  // namespace adfwi

@@ -98,10 +98,12 @@ class ElasticPlan(object):
         shapes = (ctypes.c_int32 * (2 * len(ts)))(*[d for t in ts for d in t.shape])
         return ts, ptrs, shapes
 
-    def run_forward(self, coefs, wavelet, with_gradient):
+    def run_forward(self, coefs, wavelet, with_gradient, workspace=None):
         ts, ptrs, shapes = self._coef_arrays(coefs)
         dev = ts[0].device
-        ws = torch.empty(self.workspace_bytes(with_gradient), dtype=torch.uint8, device=dev)
+        ws = workspace
+        if ws is None:
+            ws = torch.empty(self.workspace_bytes(with_gradient), dtype=torch.uint8, device=dev)
         rec = torch.empty((5, self.ns, self.nt, self.nr), dtype=self.dtype, device=dev)
         fw = torch.empty((5, self.nz, self.nx), dtype=self.dtype, device=dev)
         wavelet = wavelet.contiguous()

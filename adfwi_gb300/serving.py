@@ -1,0 +1,533 @@
+"""Continuous-batching server for iso-acoustic forward and gradient solves of mixed sizes.
+
+Requests (a model, its shots and, for a gradient solve, its observed data) arrive at any
+time. The server admits a request as soon as a solve slot is free and its device memory fits
+the HBM budget, runs every admitted solve on its own CUDA stream so that the solves of
+different requests overlap on the GPU (the persistent stencil kernels of a small grid fill
+only part of the 152 SMs, and one request's host-side preparation hides behind the others'
+kernels), and reports per-request latency (arrival to result) beside throughput.
+
+Memory. The budget is one device arena allocated once. Each admitted request takes one
+contiguous, 256-byte aligned range of it (first fit) holding everything of its solve that
+scales with the problem: the snapshot workspace, the three record arrays, the observed data
+and its adjoint source, and the coefficient, damping, wavelet and gradient planes. The range
+stays resident until the request completes. Admission is therefore exact (a request starts
+only when its range can be carved), and no solve allocates or frees its large buffers through
+a caching allocator (which synchronises the whole device when it runs out of cached blocks).
+Short-lived temporaries of the misfit go through PyTorch's allocator and are covered by the
+reserve left outside the arena.
+
+Scheduling is first-come-first-served with backfill: a waiting request that fits may start
+before an older one that does not fit yet, until the oldest has waited ``max_wait_s``; from
+then on requests start strictly in arrival order so large requests cannot starve. A request
+larger than the whole arena is rejected at submission.
+
+Determinism. A request's snapshot interval depends only on its own shape (every plan gets
+the same ``per_request_budget``), the kernels are deterministic (fixed-order reductions, no
+atomics), and the misfit uses fixed-order reductions, so a request returns bit-identical
+records, loss and gradient whether it runs alone or in a mix.
+"""
+import threading
+import time
+from concurrent.futures import Future
+from dataclasses import dataclass, field
+from typing import List, Optional
+
+import numpy as np
+import torch
+
+from .acoustic import AcousticPlan
+from .boundary import bc_pml
+from .utils import wavelet as _wavelet
+
+_ALIGN = 256
+
+
+def _aligned(n):
+    return (int(n) + _ALIGN - 1) // _ALIGN * _ALIGN
+
+
+@dataclass
+class SolveRequest:
+    """One iso-acoustic solve: records of ``vp`` (forward) or loss and dL/dvp (gradient).
+
+    ``vp`` (nz, nx) in m/s on a square grid of spacing ``dx``; rho follows Gardner
+    (310 vp^0.25, not differentiated) as ``AcousticModel.forward`` does; PML damping of
+    ``nabc`` cells built from max(vp); sources ``(src_z, src_x)`` and receivers
+    ``(rcv_z, rcv_x)`` are model cells; every shot fires the same Ricker wavelet of peak
+    frequency ``f0``. ``obs`` (ns, nt, nr) makes it a gradient solve: the misfit is the L2
+    trace misfit on max-normalised traces.
+    """
+    vp: np.ndarray
+    dx: float
+    nt: int
+    dt: float
+    f0: float
+    src_z: np.ndarray
+    src_x: np.ndarray
+    rcv_z: np.ndarray
+    rcv_x: np.ndarray
+    obs: Optional[np.ndarray] = None
+    nabc: int = 50
+    free_surface: bool = False
+    rid: int = -1
+    meta: dict = field(default_factory=dict)
+
+
+@dataclass
+class SolveResult:
+    rid: int
+    loss: Optional[float]
+    grad: Optional[np.ndarray]
+    records: Optional[np.ndarray]
+    t_arrival: float
+    t_admit: float
+    t_done: float
+    cell_updates: int
+    arena_bytes: int
+    snapshot_every: int
+
+    @property
+    def latency(self):
+        return self.t_done - self.t_arrival
+
+
+# ------------------------------------------------------------------------------------------
+# misfit and chain rule (explicit, so that no solve goes through the shared autograd thread)
+# ------------------------------------------------------------------------------------------
+def _live_traces(m, silent_rel):
+    """Traces (rows of the per-trace peaks ``m``, shape (ns, nr)) that carry signal: peak > 0
+    and above ``silent_rel`` times the peak of their shot gather."""
+    return (m > 0) & (m > silent_rel * m.amax(dim=1, keepdim=True))
+
+
+def normalise_traces(d, silent_rel=0.0):
+    """Divide every trace (dim 1 = time) by its max |value| (acoustic_fwi.py:149-150).
+    Traces that are silent (zero everywhere, or with a peak at most ``silent_rel`` times
+    their shot gather's peak) are set to zero; the reference divides them by their own tiny
+    or zero peak."""
+    m = torch.max(torch.abs(d), dim=1).values
+    live = _live_traces(m, silent_rel)
+    return d / torch.where(live, m, torch.ones_like(m))[:, None, :] * live[:, None, :]
+
+
+def l2_misfit_grad(syn, obs_n, dt, silent_rel=0.0):
+    """Loss and dLoss/dsyn of ``Misfit_waveform_L2`` (fwi/misfit/L2.py:26-29) applied to
+    max-normalised synthetic traces: L = sum_{s,r} sqrt(sum_t (obs_n - syn/m)^2 dt) with
+    m = max_t |syn|. The sums over time and traces are taken in FP64; the gradient follows
+    the reference's autograd (the max routes its share to the arg-max sample).
+
+    Silent synthetic traces (zero everywhere, or with a peak at most ``silent_rel`` times
+    their shot gather's peak: only the stencil's numerical precursor ahead of the first
+    arrival reaches them) are taken as zero: they add their observed trace's norm to the
+    loss and nothing to the gradient. The reference normalises them by their own peak, which
+    turns a precursor of ~1e-38 into an adjoint source of ~1e35 (overflow, NaN gradients).
+    Returns (loss as a 0-d FP64 tensor, gradient in syn's dtype)."""
+    mx, imx = syn.max(dim=1)
+    mn, imn = syn.min(dim=1)
+    use_min = (-mn) > mx
+    m = torch.where(use_min, -mn, mx)                     # (ns, nr), >= 0
+    idx = torch.where(use_min, imn, imx)
+    sgn = torch.where(use_min, -torch.ones_like(m), torch.ones_like(m))
+    live = _live_traces(m, silent_rel)
+    syn_n = syn / torch.where(live, m, torch.ones_like(m))[:, None, :] * live[:, None, :]
+    rsd = (obs_n - syn_n).double()                        # (ns, nt, nr)
+    nrm = torch.sqrt(torch.sum(rsd * rsd, dim=1) * dt)    # (ns, nr)
+    loss = nrm.sum()
+    live = live & (nrm > 0)
+    inv = torch.where(live, 1.0 / torch.where(live, nrm, torch.ones_like(nrm)), torch.zeros_like(nrm))
+    g_n = rsd * (-dt) * inv[:, None, :]                   # dL / d(syn/m), zero on silent traces
+    m64 = torch.where(live, m, torch.ones_like(m)).double()
+    g = g_n / m64[:, None, :]
+    corr = -(g_n * syn.double()).sum(dim=1) / (m64 * m64) * sgn.double()
+    g.scatter_add_(1, idx[:, None, :], corr[:, None, :])
+    return loss, g.to(syn.dtype)
+
+
+def fold_replicate_pad(g, n):
+    """Adjoint of edge-replicate padding by n cells (acoustic_kernels.py:16-37): the padded
+    strips fold into the edge rows / columns and the corner blocks into the corner cells."""
+    if n == 0:
+        return g.clone()
+    out = g[n:-n, n:-n].clone()
+    out[0, :] += g[:n, n:-n].sum(0)
+    out[-1, :] += g[-n:, n:-n].sum(0)
+    out[:, 0] += g[n:-n, :n].sum(1)
+    out[:, -1] += g[n:-n, -n:].sum(1)
+    out[0, 0] += g[:n, :n].sum()
+    out[0, -1] += g[:n, -n:].sum()
+    out[-1, 0] += g[-n:, :n].sum()
+    out[-1, -1] += g[-n:, -n:].sum()
+    return out
+
+
+def _pad(v, n):
+    return torch.nn.functional.pad(v[None, None], (n, n, n, n), mode="replicate")[0, 0]
+
+
+# ------------------------------------------------------------------------------------------
+# device arena
+# ------------------------------------------------------------------------------------------
+class ArenaBook(object):
+    """First-fit bookkeeping of 256-byte aligned ranges in ``capacity`` bytes (host only).
+    Not thread-safe by itself: the server calls it under its lock."""
+
+    def __init__(self, capacity):
+        self.capacity = int(capacity) // _ALIGN * _ALIGN
+        self.free_ranges = [(0, self.capacity)] if self.capacity else []  # sorted, coalesced
+        self.used = 0
+        self.peak = 0
+
+    def alloc(self, nbytes):
+        n = _aligned(nbytes)
+        for k, (off, size) in enumerate(self.free_ranges):
+            if size >= n:
+                if size == n:
+                    del self.free_ranges[k]
+                else:
+                    self.free_ranges[k] = (off + n, size - n)
+                self.used += n
+                self.peak = max(self.peak, self.used)
+                return off, n
+        return None
+
+    def free(self, off, n):
+        fr = self.free_ranges
+        k = 0
+        while k < len(fr) and fr[k][0] < off:
+            k += 1
+        if (k < len(fr) and off + n > fr[k][0]) or (k > 0 and fr[k - 1][0] + fr[k - 1][1] > off):
+            raise RuntimeError("arena range (%d, %d) overlaps a free range: double free" % (off, n))
+        fr.insert(k, (off, n))
+        if k + 1 < len(fr) and fr[k][0] + fr[k][1] == fr[k + 1][0]:
+            fr[k] = (fr[k][0], fr[k][1] + fr[k + 1][1])
+            del fr[k + 1]
+        if k > 0 and fr[k - 1][0] + fr[k - 1][1] == fr[k][0]:
+            fr[k - 1] = (fr[k - 1][0], fr[k - 1][1] + fr[k][1])
+            del fr[k]
+        self.used -= n
+
+    def largest_free(self):
+        return max((s for _, s in self.free_ranges), default=0)
+
+
+def admit(queue, book, free_slots, now, max_wait_s, size=lambda e: e[1].nbytes):
+    """Admission step: carve ``book`` ranges for entries of ``queue`` (arrival-ordered
+    tuples whose first item is the arrival time) into at most ``free_slots`` slots, first
+    come first served with backfill; once the oldest entry has waited more than
+    ``max_wait_s`` nothing may pass it. Removes the admitted entries from ``queue`` and
+    returns [(entry, offset, bytes)]."""
+    out = []
+    strict = bool(queue) and now - queue[0][0] > max_wait_s
+    i = 0
+    while i < len(queue) and len(out) < free_slots:
+        got = book.alloc(size(queue[i]))
+        if got is not None:
+            out.append((queue.pop(i),) + got)
+            continue
+        if strict:
+            break
+        i += 1
+    return out
+
+
+class _Carver(object):
+    """Hands out typed views of consecutive 256-byte aligned pieces of an arena range."""
+
+    def __init__(self, buf, off, end):
+        self.buf, self.off, self.end = buf, off, end
+
+    def take(self, shape, dtype):
+        n = int(np.prod(shape)) * torch.empty((), dtype=dtype).element_size()
+        if self.off + n > self.end:
+            raise RuntimeError("solve footprint exceeds its arena range")
+        v = self.buf[self.off:self.off + n].view(dtype).view(*shape)
+        self.off += _aligned(n)
+        return v
+
+
+# ------------------------------------------------------------------------------------------
+# one solve
+# ------------------------------------------------------------------------------------------
+class _Solve(object):
+    """A request with its plan and its arena footprint."""
+
+    def __init__(self, req, snapshot_precision, per_request_budget, silent_rel=1e-6):
+        self.req = req
+        self.silent_rel = silent_rel
+        vp = np.asarray(req.vp, dtype=np.float32)
+        if vp.ndim != 2:
+            raise ValueError("vp must be a 2-D (nz, nx) array")
+        self.nz, self.nx = vp.shape
+        self.ns, self.nr = len(req.src_x), len(req.rcv_x)
+        if req.obs is not None and tuple(np.shape(req.obs)) != (self.ns, req.nt, self.nr):
+            raise ValueError("obs has shape %s, expected %s" % (np.shape(req.obs), (self.ns, req.nt, self.nr)))
+        self.grad = req.obs is not None
+        self.plan = AcousticPlan(nz=self.nz, nx=self.nx, nabc=req.nabc, free_surface=req.free_surface,
+                                 src_z=req.src_z, src_x=req.src_x, rcv_z=req.rcv_z, rcv_x=req.rcv_x, nt=req.nt,
+                                 dt=req.dt, dtype=torch.float32, snapshot_precision=snapshot_precision,
+                                 memory_budget=per_request_budget)
+        self.ws_bytes = self.plan.workspace_bytes(self.grad)
+        self.nzp, self.nxp = self.plan.grid_shape()
+        rec = self.ns * req.nt * self.nr * 4
+        grid = self.nzp * self.nxp * 4
+        self.nbytes = (_aligned(self.ws_bytes) + 3 * _aligned(rec) + (2 * _aligned(rec) if self.grad else 0)
+                       + 4 * _aligned(grid) + 4 * _aligned(self.nz * self.nx * 4) + _aligned(self.ns * req.nt * 4))
+        self.cells = self.ns * self.nzp * self.nxp * req.nt
+
+    def run(self, arena, off, n, stream, device):
+        """Enqueue the whole solve on ``stream`` inside the arena range [off, off + n) and
+        wait for it. Returns (loss, grad, records)."""
+        r = self.req
+        cv = _Carver(arena, off, off + n)
+        ws = cv.take((self.ws_bytes,), torch.uint8)
+        shp = (self.ns, r.nt, self.nr)
+        recs = tuple(cv.take(shp, torch.float32) for _ in range(3))
+        a1, a2, damp, ga_buf = (cv.take((self.nzp, self.nxp), torch.float32) for _ in range(4))
+        fw = tuple(cv.take((self.nz, self.nx), torch.float32) for _ in range(3))
+        vp_d = cv.take((self.nz, self.nx), torch.float32)
+        wav = cv.take((self.ns, r.nt), torch.float32)
+        h = stream.cuda_stream
+        with torch.cuda.stream(stream):
+            vp = np.ascontiguousarray(r.vp, dtype=np.float32)
+            vp_d.copy_(torch.from_numpy(vp))
+            rho = torch.from_numpy(np.power(vp, 0.25) * 310).to(device)
+            damp.copy_(torch.from_numpy(np.ascontiguousarray(
+                bc_pml(self.nx, self.nz, r.dx, r.dx, r.nabc, vp.max(), free_surface=False), dtype=np.float32)))
+            _, w = _wavelet(r.nt, r.dt, r.f0)
+            wav.copy_(torch.from_numpy(np.ascontiguousarray(np.tile(w, (self.ns, 1)), dtype=np.float32)))
+            nb = r.nabc
+            c, den = _pad(vp_d, nb), _pad(rho, nb)
+            t1 = den * c
+            a1.copy_(t1 * c * r.dt / r.dx)
+            a2.copy_(r.dt / (den * r.dx))
+            self.plan.run_forward(a1, a2, damp, wav, self.grad, workspace=ws, records=recs, fw=fw, stream=h)
+            if not self.grad:
+                out = recs[0].cpu()
+                code = self.plan.status(ws, False, stream=h)
+                if code != 0:
+                    raise RuntimeError("solve %d: a pipeline wait timed out on the GPU (status %d)" % (r.rid, code))
+                return None, None, out.numpy()
+            obs = cv.take(shp, torch.float32)
+            obs.copy_(torch.from_numpy(np.ascontiguousarray(r.obs, dtype=np.float32)))
+            loss, g_rec = l2_misfit_grad(recs[0], normalise_traces(obs, self.silent_rel), r.dt, self.silent_rel)
+            adj = cv.take(shp, torch.float32)
+            adj.copy_(g_rec)
+            del g_rec
+            ga1, _ = self.plan.run_backward(a1, a2, damp, wav, (adj, None, None), ws, stream=h)
+            code = self.plan.status(ws, True, stream=h)
+            if code != 0:
+                raise RuntimeError("solve %d: a pipeline wait timed out on the GPU (status %d)" % (r.rid, code))
+            # alpha1 = ((den c) c) dt / dx; alpha2 and rho do not depend on vp
+            g_t2 = ga1 * (r.dt / r.dx)
+            torch.add(g_t2 * t1, g_t2 * c * den, out=ga_buf)
+            grad = fold_replicate_pad(ga_buf, nb).cpu().numpy()
+            return float(loss.cpu()), grad, None
+
+
+# ------------------------------------------------------------------------------------------
+# server
+# ------------------------------------------------------------------------------------------
+class SolveServer(object):
+    """Admit, overlap and complete solves under an HBM budget (module docstring)."""
+
+    def __init__(self, device="cuda:0", hbm_budget=150 << 30, slots=4, snapshot_precision="bf16",
+                 per_request_budget=None, max_wait_s=2.0, reserve=None, silent_rel=1e-6):
+        if not torch.cuda.is_available():
+            raise RuntimeError("SolveServer needs a CUDA device (adfwi_gb300 has no CPU implementation)")
+        self.device = torch.device(device)
+        self.budget = int(hbm_budget)
+        reserve = int(reserve if reserve is not None else min(self.budget // 10, 16 << 30))
+        self.book = ArenaBook(self.budget - reserve)
+        self.arena = torch.empty(self.book.capacity, dtype=torch.uint8, device=self.device)
+        self.slots = int(slots)
+        self.snapshot_precision = snapshot_precision
+        self.per_request_budget = int(per_request_budget if per_request_budget is not None
+                                      else max(1 << 30, self.book.capacity // max(1, self.slots)))
+        self.max_wait_s = float(max_wait_s)
+        self.silent_rel = float(silent_rel)
+        self._cv = threading.Condition()
+        self._queue = []      # (t_arrival, solve, future), arrival order
+        self._ready = []      # (t_arrival, solve, future, t_admit, off, n)
+        self._running = 0
+        self._closed = False
+        self._next_id = 0
+        self.completed: List[SolveResult] = []
+        self.failed = 0
+        self.peak_running = 0
+        self._streams = [torch.cuda.Stream(device=self.device) for _ in range(self.slots)]
+        self._workers = [threading.Thread(target=self._worker, args=(k,), daemon=True, name="adfwi-solve-%d" % k)
+                         for k in range(self.slots)]
+        for w in self._workers:
+            w.start()
+
+    # -------------------------------------------------------------- client side
+    def submit(self, req: SolveRequest, t_arrival=None) -> Future:
+        """Queue a request; the future resolves to a SolveResult (or raises the solve's error)."""
+        fut = Future()
+        t = time.perf_counter() if t_arrival is None else t_arrival
+        try:
+            solve = _Solve(req, self.snapshot_precision, self.per_request_budget, self.silent_rel)
+        except Exception as e:
+            fut.set_exception(e)
+            return fut
+        if solve.nbytes > self.book.capacity:
+            fut.set_exception(MemoryError("request %d needs %d bytes of device memory, more than the %d-byte arena"
+                                          % (req.rid, solve.nbytes, self.book.capacity)))
+            return fut
+        with self._cv:
+            if self._closed:
+                raise RuntimeError("the server is closed")
+            if req.rid < 0:
+                req.rid = self._next_id
+            self._next_id += 1
+            self._queue.append((t, solve, fut))
+            self._admit_locked()
+            self._cv.notify_all()
+        return fut
+
+    def close(self, wait=True):
+        with self._cv:
+            self._closed = True
+            self._cv.notify_all()
+        if wait:
+            for w in self._workers:
+                w.join()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def reset_stats(self):
+        with self._cv:
+            self.completed = []
+            self.failed = 0
+            self.peak_running = self._running
+            self.book.peak = self.book.used
+
+    def stats(self):
+        done = list(self.completed)
+        if not done:
+            return {}
+        lat = np.array([r.latency for r in done])
+        t0 = min(r.t_arrival for r in done)
+        t1 = max(r.t_done for r in done)
+        cells = sum(r.cell_updates for r in done)
+        return {"requests": len(done), "failed": self.failed, "p50_s": float(np.percentile(lat, 50)),
+                "p99_s": float(np.percentile(lat, 99)), "mean_s": float(lat.mean()), "makespan_s": t1 - t0,
+                "gcell_per_s": cells / (t1 - t0) / 1e9, "peak_arena_bytes": self.book.peak,
+                "arena_bytes": self.book.capacity, "peak_concurrency": self.peak_running}
+
+    # -------------------------------------------------------------- scheduling
+    def _admit_locked(self):
+        now = time.perf_counter()
+        free = self.slots - self._running - len(self._ready)
+        for (t, solve, fut), off, n in admit(self._queue, self.book, free, now, self.max_wait_s):
+            self._ready.append((t, solve, fut, now, off, n))
+
+    def _worker(self, k):
+        stream = self._streams[k]
+        while True:
+            with self._cv:
+                while True:
+                    self._admit_locked()
+                    if self._ready:
+                        break
+                    if self._closed and not self._queue:
+                        return
+                    self._cv.wait(timeout=0.05)
+                t_arr, solve, fut, t_admit, off, n = self._ready.pop(0)
+                self._running += 1
+                self.peak_running = max(self.peak_running, self._running)
+            res = err = None
+            try:
+                loss, grad, rec = solve.run(self.arena, off, n, stream, self.device)
+                res = SolveResult(solve.req.rid, loss, grad, rec, t_arr, t_admit, time.perf_counter(), solve.cells,
+                                  n, solve.plan.snapshot_every)
+            except Exception as e:  # the others keep running; the future carries the error
+                err = e
+            try:
+                stream.synchronize()  # the range may be reused only once this solve's work is done
+            except Exception as e:
+                err = err or e
+            with self._cv:
+                self._running -= 1
+                self.book.free(off, n)
+                if res is not None and err is None:
+                    self.completed.append(res)
+                else:
+                    self.failed += 1
+                self._admit_locked()
+                self._cv.notify_all()
+            if err is None:
+                fut.set_result(res)
+            else:
+                fut.set_exception(err)
+
+
+def replay(server, timed_requests):
+    """Submit ``[(t_offset_s, SolveRequest), ...]`` at their arrival offsets from now and
+    wait for all; returns the results in submission order."""
+    t0 = time.perf_counter()
+    futs = []
+    for t, req in timed_requests:
+        delay = t0 + t - time.perf_counter()
+        if delay > 0:
+            time.sleep(delay)
+        futs.append(server.submit(req, t_arrival=t0 + t))
+    return [f.result() for f in futs]
+
+
+# ------------------------------------------------------------------------------------------
+# synthetic request streams
+# ------------------------------------------------------------------------------------------
+GRIDS = ((100, 300), (200, 600), (300, 900), (500, 1500))
+
+
+def random_layered_vp(rng, nz, nx, vmin=1500.0, vmax=4500.0):
+    """Random layered model: 4-11 dipping interfaces and 0-2 normal faults, velocities
+    uniform in [vmin, vmax] sorted to increase with depth."""
+    from .synthetic import layered_faulted
+    return layered_faulted(nz, nx, rng, n_interfaces=int(rng.integers(4, 12)), vmin=vmin, vmax=vmax,
+                           n_faults=int(rng.integers(0, 3))).astype(np.float32)
+
+
+def synthetic_stream(n, rate, seed=0, grids=GRIDS, shots=(1, 16), nts=(1000, 2000, 4000), dt=1e-3, f0=10.0,
+                     nabc=50):
+    """``n`` seeded requests with Poisson arrivals of ``rate`` per second: grid uniform over
+    ``grids``, shot count uniform in ``shots`` (evenly spaced at z=2), nt uniform over
+    ``nts``, a receiver at every column (z=2), PML of ``nabc`` cells. Returns
+    [(t_offset, true_vp, request)]; the request's ``vp`` is the Gaussian-smoothed (sigma 10
+    cells) true model and its ``obs`` is left for ``observed_data`` to fill."""
+    from .synthetic import smooth
+    rng = np.random.default_rng(seed)
+    t = 0.0
+    out = []
+    for k in range(n):
+        t += rng.exponential(1.0 / rate)
+        nz, nx = grids[int(rng.integers(len(grids)))]
+        ns = int(rng.integers(shots[0], shots[1] + 1))
+        nt = int(nts[int(rng.integers(len(nts)))])
+        true_vp = random_layered_vp(rng, nz, nx)
+        dx = 12.5 if nz >= 300 else 10.0
+        sx = np.linspace(0, nx - 1, ns + 2)[1:-1].round().astype(int) if ns > 1 else np.array([nx // 2])
+        req = SolveRequest(vp=smooth(true_vp, 10.0).astype(np.float32), dx=dx, nt=nt, dt=dt, f0=f0,
+                           src_z=np.full(len(sx), 2), src_x=sx, rcv_z=np.full(nx, 2), rcv_x=np.arange(nx),
+                           nabc=nabc, rid=k, meta={"shape": (nz, nx), "shots": ns, "nt": nt})
+        out.append((t, true_vp, req))
+    return out
+
+
+def observed_data(server, stream):
+    """Fill each request's ``obs`` with the records of its true model, served as forward
+    solves by ``server`` (all submitted at once)."""
+    futs = []
+    for _, true_vp, req in stream:
+        fwd = SolveRequest(vp=true_vp, dx=req.dx, nt=req.nt, dt=req.dt, f0=req.f0, src_z=req.src_z, src_x=req.src_x,
+                           rcv_z=req.rcv_z, rcv_x=req.rcv_x, nabc=req.nabc, free_surface=req.free_surface)
+        futs.append(server.submit(fwd))
+    for (_, _, req), f in zip(stream, futs):
+        req.obs = f.result().records
+    return stream

@@ -279,6 +279,42 @@ def gpu_arm(args, world, rank, local):
     return line
 
 
+def serving_arm(args, dev):
+    """Served stream of mixed-size forward+gradient requests (Poisson arrivals, grids from
+    {100x300, 200x600, 300x900, 500x1500}, 1-16 shots, nt in {1000, 2000, 4000}, random layered
+    vp, FP32 stencils with BF16 snapshots, PML 50, 150 GB HBM admission budget): the
+    continuous-batching server against the same stream solved one request at a time."""
+    from adfwi_gb300 import serving as S
+    stream = S.synthetic_stream(args.serve_requests, args.serve_rate, seed=0)
+    timed = [(t, req) for t, _, req in stream]
+    budget = 150 << 30
+    out = {}
+    results = {}
+    per_req = None
+    for name, slots in (("served", args.serve_slots), ("one_at_a_time", 1)):
+        with S.SolveServer(device=dev, hbm_budget=budget, slots=slots, snapshot_precision="bf16",
+                           per_request_budget=per_req) as srv:
+            per_req = srv.per_request_budget
+            if not results:
+                S.observed_data(srv, stream)  # observed data of the true models (setup, untimed)
+                srv.reset_stats()
+            results[name] = S.replay(srv, timed)
+            st = srv.stats()
+        out[name] = {"p50_s": round(st["p50_s"], 4), "p99_s": round(st["p99_s"], 4), "mean_s": round(st["mean_s"], 4),
+                     "throughput_gcell_per_s": round(st["gcell_per_s"], 3),
+                     "requests_per_s": round(st["requests"] / st["makespan_s"], 3), "slots": slots,
+                     "peak_concurrency": st["peak_concurrency"], "peak_arena_gb": round(st["peak_arena_bytes"] / 2 ** 30, 2)}
+    same = all(a.loss == b.loss and np.array_equal(a.grad, b.grad)
+               for a, b in zip(results["served"], results["one_at_a_time"]))
+    out.update({"requests": len(timed), "arrival_rate_per_s": args.serve_rate, "hbm_budget_gb": budget / 2 ** 30,
+                "arena_gb": round(srv.book.capacity / 2 ** 30, 2), "per_request_budget_gb": round(per_req / 2 ** 30, 2),
+                "bit_identical_alone_vs_mix": bool(same),
+                "speedup_vs_one_at_a_time": round(out["served"]["throughput_gcell_per_s"]
+                                                  / out["one_at_a_time"]["throughput_gcell_per_s"], 3),
+                "sample": "first %d requests of the seeded 2000-request stream" % len(timed)})
+    return out
+
+
 def cpu_sample(n_steps, threads):
     """Time the CPU oracle on a bounded sample: 1 shot of the gradient workload, n_steps steps,
     forward + autograd backward (the reference's own gradient mechanism)."""
@@ -339,6 +375,10 @@ def main():
                     help="share of free HBM the gradient workspace may use (snapshot / history sizing)")
     ap.add_argument("--cpu-sample-steps", type=int, default=300)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--serve-requests", type=int, default=48,
+                    help="requests of the served mixed-size stream (0 skips the serving measurement)")
+    ap.add_argument("--serve-rate", type=float, default=50.0, help="Poisson arrival rate of the served stream (1/s)")
+    ap.add_argument("--serve-slots", type=int, default=4, help="concurrent solves of the server")
     args = ap.parse_args()
     world, rank, local = dist_setup()
     if args.impl == "reference":
@@ -346,6 +386,9 @@ def main():
             print(json.dumps(reference_arm(args)), flush=True)
         return
     line = gpu_arm(args, world, rank, local)
+    if world == 1 and args.serve_requests > 0:
+        torch.cuda.empty_cache()
+        line["serving"] = serving_arm(args, torch.device("cuda", local))
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         # bounded sample: repeat a 1-shot slice of the workload until >= 10 s of CPU work
         threads = os.cpu_count() or 1

@@ -1,0 +1,119 @@
+"""Solve server on the GPU: results equal the drop-in propagator's, each request's result
+is bit-identical alone and in a mix, and admission keeps to the HBM budget."""
+import numpy as np
+import pytest
+import torch
+
+import adfwi_gb300 as A
+from adfwi_gb300 import serving as S
+from adfwi_gb300.synthetic import smooth
+
+from _cases import layered_vp, rel
+
+pytestmark = pytest.mark.gpu
+
+
+def _request(seed, nz, nx, ns, nt, nabc=16, dx=10.0, dt=1e-3, f0=18.0, true=False):
+    rng = np.random.default_rng(seed)
+    vp_true = layered_vp(nz, nx, rng, vmin=1600.0, vmax=3200.0).astype(np.float32)
+    vp = vp_true if true else smooth(vp_true, 3.0).astype(np.float32)
+    sx = np.linspace(3, nx - 4, ns).round().astype(int)
+    req = S.SolveRequest(vp=vp, dx=dx, nt=nt, dt=dt, f0=f0, src_z=np.full(ns, 2), src_x=sx,
+                         rcv_z=np.full(nx, 2), rcv_x=np.arange(nx), nabc=nabc, rid=seed)
+    return req, vp_true
+
+
+def _with_obs(server, req, vp_true):
+    fwd = S.SolveRequest(vp=vp_true, dx=req.dx, nt=req.nt, dt=req.dt, f0=req.f0, src_z=req.src_z,
+                         src_x=req.src_x, rcv_z=req.rcv_z, rcv_x=req.rcv_x, nabc=req.nabc)
+    req.obs = server.submit(fwd).result().records
+    return req
+
+
+def test_server_matches_the_drop_in_propagator(native_lib):
+    req, vp_true = _request(11, 48, 72, 3, 400)
+    with S.SolveServer(hbm_budget=2 << 30, slots=2, snapshot_precision="native", silent_rel=0.0) as srv:
+        _with_obs(srv, req, vp_true)
+        res = srv.submit(req).result()
+    # the same solve through AcousticModel / AcousticPropagator and autograd
+    nz, nx = req.vp.shape
+    model = A.AcousticModel(0, 0, nx, nz, req.dx, req.dx, vp=req.vp.copy(),
+                            rho=(np.power(req.vp, 0.25) * 310).astype(np.float32), vp_grad=True,
+                            nabc=req.nabc, device="cuda:0")
+    src = A.Source(nt=req.nt, dt=req.dt, f0=req.f0)
+    _, wav = A.wavelet(req.nt, req.dt, req.f0)
+    src.add_sources(src_x=req.src_x, src_z=req.src_z, src_wavelet=wav)
+    rcv = A.Receiver(nt=req.nt, dt=req.dt)
+    rcv.add_receivers(rcv_x=req.rcv_x, rcv_z=req.rcv_z, rcv_type="pr")
+    prop = A.AcousticPropagator(model, A.Survey(src, rcv), device="cuda:0")
+    syn = prop.forward()["p"]
+    obs = torch.tensor(req.obs, device="cuda:0")
+    syn_n = syn / torch.max(torch.abs(syn), dim=1, keepdim=True).values
+    obs_n = obs / torch.max(torch.abs(obs), dim=1, keepdim=True).values
+    loss = torch.sum(torch.sqrt(torch.sum((obs_n - syn_n) ** 2 * req.dt, dim=1)))
+    loss.backward()
+    assert abs(res.loss - loss.item()) <= 1e-5 * abs(loss.item())
+    assert rel(res.grad, model.vp.grad) <= 1e-5
+
+
+def test_forward_records_match_the_drop_in_propagator(native_lib):
+    req, vp_true = _request(5, 40, 64, 2, 300, true=True)
+    with S.SolveServer(hbm_budget=1 << 30, slots=1) as srv:
+        rec = srv.submit(req).result().records
+    nz, nx = req.vp.shape
+    model = A.AcousticModel(0, 0, nx, nz, req.dx, req.dx, vp=req.vp.copy(),
+                            rho=(np.power(req.vp, 0.25) * 310).astype(np.float32), nabc=req.nabc, device="cuda:0")
+    src = A.Source(nt=req.nt, dt=req.dt, f0=req.f0)
+    _, wav = A.wavelet(req.nt, req.dt, req.f0)
+    src.add_sources(src_x=req.src_x, src_z=req.src_z, src_wavelet=wav)
+    rcv = A.Receiver(nt=req.nt, dt=req.dt)
+    rcv.add_receivers(rcv_x=req.rcv_x, rcv_z=req.rcv_z, rcv_type="pr")
+    prop = A.AcousticPropagator(model, A.Survey(src, rcv), device="cuda:0")
+    with torch.no_grad():
+        ref = prop.forward()["p"].cpu().numpy()
+    assert np.array_equal(rec, ref)
+
+
+SHAPES = [(48, 80, 2, 300), (64, 128, 3, 500), (40, 64, 1, 400), (80, 96, 4, 300), (56, 100, 2, 600)]
+
+
+def test_each_result_is_the_same_alone_and_in_the_mix(native_lib):
+    budget = 256 << 20  # small per-solve budget: the longer solves keep BF16 snapshots
+    reqs = [_request(100 + k, *shape) for k, shape in enumerate(SHAPES)]
+    with S.SolveServer(hbm_budget=2 << 30, slots=1, per_request_budget=budget) as srv:
+        for req, vp_true in reqs:
+            _with_obs(srv, req, vp_true)
+        alone = [srv.submit(req).result() for req, _ in reqs]
+    with S.SolveServer(hbm_budget=2 << 30, slots=3, per_request_budget=budget) as srv:
+        futs = [srv.submit(req) for req, _ in reqs]
+        mix = [f.result() for f in futs]
+        st = srv.stats()
+    assert st["peak_concurrency"] >= 2  # the solves really overlapped
+    assert any(r.snapshot_every < r_req.nt for r, (r_req, _) in zip(alone, reqs))
+    for a, m in zip(alone, mix):
+        assert a.rid == m.rid and a.snapshot_every == m.snapshot_every
+        assert a.loss == m.loss
+        assert np.array_equal(a.grad, m.grad)
+        assert np.isfinite(a.grad).all() and np.abs(a.grad).max() > 0
+
+
+def test_admission_keeps_to_the_budget(native_lib):
+    req, vp_true = _request(7, 48, 80, 2, 300)
+    with S.SolveServer(hbm_budget=1 << 30, slots=1) as srv:
+        _with_obs(srv, req, vp_true)
+    need = S._Solve(req, "bf16", 64 << 20).nbytes
+    # room for one solve at a time: the second waits for the first to free its range
+    with S.SolveServer(hbm_budget=int(need * 1.5), reserve=0, slots=2, per_request_budget=64 << 20) as srv:
+        futs = [srv.submit(req) for _ in range(3)]
+        res = [f.result() for f in futs]
+        st = srv.stats()
+    assert st["peak_concurrency"] == 1 and st["peak_arena_bytes"] <= st["arena_bytes"]
+    assert all(np.array_equal(r.grad, res[0].grad) for r in res)
+    # a request larger than the whole arena is refused; the server keeps serving
+    with S.SolveServer(hbm_budget=need // 2, reserve=0, slots=1, per_request_budget=64 << 20) as srv:
+        with pytest.raises(MemoryError):
+            srv.submit(req).result()
+        bad = S.SolveRequest(vp=req.vp, dx=req.dx, nt=10, dt=req.dt, f0=req.f0, src_z=np.array([2]),
+                             src_x=np.array([10 ** 6]), rcv_z=req.rcv_z, rcv_x=req.rcv_x, nabc=req.nabc)
+        with pytest.raises(RuntimeError):
+            srv.submit(bad).result()

@@ -21,6 +21,11 @@ FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", 
          "--expt-relaxed-constexpr"]
 
 
+# Extra nvcc arguments for tuning builds (for example -DADFWI_VEC_GROUPS=2); build(force=True)
+# after changing them.
+EXTRA = os.environ.get("ADFWI_NVCC_EXTRA", "").split()
+
+
 def nvcc_path():
     cand = shutil.which("nvcc")
     if cand:
@@ -63,7 +68,7 @@ def build(force=False, verbose=False):
 
     def compile_one(job):
         src, obj = job
-        cmd = [nvcc, *ARCH, *FLAGS, "-I", os.path.join(ROOT, "include"), "-c", src, "-o", obj]
+        cmd = [nvcc, *ARCH, *FLAGS, *EXTRA, "-I", os.path.join(ROOT, "include"), "-c", src, "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("nvcc failed for %s:\n%s\n%s" % (src, r.stdout, r.stderr))

@@ -8,12 +8,12 @@
 //   ADFWI/propagator/acoustic_kernels.py:252-265  alpha / kappa coefficient definitions
 //   ADFWI/propagator/acoustic_kernels.py:268-301  chunked time loop and the record dict
 //
-// One launch advances one time step of all shots (acoustic_tma.cuh): persistent, warp-
-// specialised blocks stream (tile, shot) items through a TMA / mbarrier pipeline; per item
-// the consumers compute the new pressure on a 16 x 64 tile plus its halo (1 row / column
-// before, 2 after) and then the new u and w on the tile, so p, u and w each cross HBM once
-// per step (ping-pong buffers keep the Jacobi semantics of the reference's slice
-// assignments). The forward arithmetic uses explicitly rounded operations (no FMA
+// One launch advances one time step of all shots (acoustic_tma.cuh, acoustic_vec.cuh):
+// persistent, warp-specialised blocks stream (tile, shot) items through a TMA / mbarrier
+// pipeline; per item the consumers compute the new pressure on a 16 x 64 tile plus its halo
+// (1 row / column before, 2 after) and then the new u and w on the tile, four adjacent
+// columns per thread, so p, u and w each cross HBM once per step (ping-pong buffers keep the
+// Jacobi semantics of the reference's slice assignments). The forward arithmetic uses explicitly rounded operations (no FMA
 // contraction) in the reference's evaluation order, so float32 records reproduce the
 // reference's PyTorch CPU results bit for bit. The adjoint step is the exact transpose of
 // the forward step, in reverse operation order.
@@ -196,6 +196,7 @@ __global__ void mask_coefficients(Geo<T> g, T* cf) {
 }  // namespace adfwi
 
 #include "acoustic_tma.cuh"
+#include "acoustic_vec.cuh"
 
 // ----------------------------------------------------------------------------------------
 // Plan, workspace and drivers.
@@ -207,7 +208,8 @@ struct Tiling {
   int tz, tx;
   int tiles_x, tiles_z, ntiles;
   int G, ngroups;  // shots per unit / units per tile
-  int blocks;      // launch width (persistent kernels)
+  int blocks;      // launch width of the adjoint step (persistent kernel)
+  int fwd_blocks;  // launch width of the forward step (persistent kernel)
   int64_t o_trb, o_trc, o_tri, o_tcb, o_tcc, o_tcr, o_cr;
   int ncells;
 };
@@ -342,12 +344,12 @@ int setup_common(const adfwi_acoustic_plan* p, unsigned char* ws, const Carve& c
 }
 
 template <typename T>
-int tma_stages() {
-  return sizeof(T) == 8 ? 2 : 4;
+int vec_adj_stages() {
+  return sizeof(T) == 8 ? 2 : (ac2::VAMINB >= 3 ? 2 : 3);
 }
 template <typename T>
-int tma_adj_stages() {
-  return 2;
+int vec_stages() {
+  return sizeof(T) == 8 ? 2 : (ac2::VMINB >= 3 ? 3 : 4);
 }
 
 template <typename T>
@@ -375,7 +377,7 @@ int launch_fwd(const adfwi_acoustic_plan* p, const ac::Geo<T>& g, int it, int ac
   if (rc) return rc;
   ac2::StepArgs<T> a = step_args<T>(p, it, cf, flag);
   a.accum_u = accum_u;
-  a.stages = tma_stages<T>();
+  a.stages = vec_stages<T>();
   a.wav = wav;
   a.o0 = p1;
   a.o1 = u1;
@@ -386,9 +388,9 @@ int launch_fwd(const adfwi_acoustic_plan* p, const ac::Geo<T>& g, int it, int ac
   a.rec_w = rw;
   a.acc0 = ilp;
   a.acc1 = ilu;
-  const int smem = ac2::FwdLayout<T>::bytes(a.stages);
+  const int smem = ac2::VecFwdLayout<T>::bytes(a.stages);
   ADFWI_LAUNCH(kAcFwdStep, st,
-               (ac2::fwd_step_tma<T><<<p->t2.blocks, ac2::NTHREADS, smem, st>>>(maps, g, a)));
+               (ac2::fwd_step_vec<T><<<p->t2.fwd_blocks, ac2::VTHREADS, smem, st>>>(maps, g, a)));
   return kOk;
 }
 
@@ -405,7 +407,7 @@ int launch_adj(const adfwi_acoustic_plan* p, const ac::Geo<T>& g, int it, const 
   if (!rc) rc = make_plane_map(&maps.e, dh, sizeof(T), p->L, ns, ac2::BOXX, ac2::EZ);
   if (rc) return rc;
   ac2::StepArgs<T> a = step_args<T>(p, it, cf, flag);
-  a.stages = tma_adj_stages<T>();
+  a.stages = vec_adj_stages<T>();
   a.o0 = lp1;
   a.o1 = lu1;
   a.o2 = lw1;
@@ -414,9 +416,9 @@ int launch_adj(const adfwi_acoustic_plan* p, const ac::Geo<T>& g, int it, const 
   a.rec_w = gw;
   a.acc0 = g1;
   a.acc1 = g2;
-  const int smem = ac2::AdjLayout<T>::bytes(a.stages);
+  const int smem = ac2::VecAdjLayout<T>::bytes(a.stages);
   ADFWI_LAUNCH(kAcAdjStep, st,
-               (ac2::adj_step_tma<T><<<p->t2.blocks, ac2::NTHREADS, smem, st>>>(maps, g, a)));
+               (ac2::adj_step_vec<T><<<p->t2.blocks, ac2::VTHREADS, smem, st>>>(maps, g, a)));
   return kOk;
 }
 
@@ -424,10 +426,10 @@ template <typename T>
 int set_smem_limits() {
   static bool done = false;
   if (!done) {
-    ADFWI_CUDA_TRY(cudaFuncSetAttribute(ac2::fwd_step_tma<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        ac2::FwdLayout<T>::bytes(tma_stages<T>())));
-    ADFWI_CUDA_TRY(cudaFuncSetAttribute(ac2::adj_step_tma<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        ac2::AdjLayout<T>::bytes(tma_adj_stages<T>())));
+    ADFWI_CUDA_TRY(cudaFuncSetAttribute(ac2::fwd_step_vec<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        ac2::VecFwdLayout<T>::bytes(vec_stages<T>())));
+    ADFWI_CUDA_TRY(cudaFuncSetAttribute(ac2::adj_step_vec<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        ac2::VecAdjLayout<T>::bytes(vec_adj_stages<T>())));
     done = true;
   }
   return kOk;
@@ -585,35 +587,46 @@ int backward_impl(const adfwi_acoustic_plan* p, const void* wavelet, const void*
   return kOk;
 }
 
-// Resident blocks of the TMA forward step on the current device (152 SMs x 2 without a GPU).
-template <typename T>
-int resident_tma_blocks() {
+// Resident blocks of a persistent step kernel on the current device (`fallback` per SM x 152
+// without a GPU).
+template <typename K>
+int resident_blocks(K kernel, int threads, int smem, int fallback) {
   int dev = 0, sms = 0, occ = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
     cudaGetLastError();
-    return 152 * (sizeof(T) == 8 ? 1 : 2);
+    return 152 * fallback;
   }
-  const int smem = ac2::FwdLayout<T>::bytes(tma_stages<T>());
-  if (cudaFuncSetAttribute(ac2::fwd_step_tma<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess ||
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, ac2::fwd_step_tma<T>, ac2::NTHREADS, smem) != cudaSuccess ||
-      occ < 1) {
+  if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, threads, smem) != cudaSuccess || occ < 1) {
     cudaGetLastError();
-    return 152 * (sizeof(T) == 8 ? 1 : 2);
+    return 152 * fallback;
   }
   return sms * occ;
+}
+
+template <typename T>
+int resident_adj_blocks() {
+  return resident_blocks(ac2::adj_step_vec<T>, ac2::VTHREADS, ac2::VecAdjLayout<T>::bytes(vec_adj_stages<T>()),
+                         sizeof(T) == 8 ? 1 : ac2::VAMINB);
+}
+template <typename T>
+int resident_fwd_blocks() {
+  return resident_blocks(ac2::fwd_step_vec<T>, ac2::VTHREADS, ac2::VecFwdLayout<T>::bytes(vec_stages<T>()),
+                         sizeof(T) == 8 ? 1 : ac2::VMINB);
 }
 
 // Shots per unit for the persistent TMA kernels: balance the units over the resident blocks
 // (the block with the most units sets the time) against the per-unit flush of the partial
 // accumulator planes (about half an item's worth of traffic).
-int pick_unit_shots(int ns, int ntiles, int blocks) {
+int pick_unit_shots(int ns, int ntiles, int blocks_fwd, int blocks_adj) {
   int best = 1;
   double best_cost = 1e30;
   for (int G = 1; G <= ns; ++G) {
     const int groups = (ns + G - 1) / G;
     const long long units = (long long)ntiles * groups;
-    const long long per = (units + blocks - 1) / blocks;
-    const double cost = (double)per * (G + 0.5);
+    const long long pf = (units + blocks_fwd - 1) / blocks_fwd;
+    const long long pa = (units + blocks_adj - 1) / blocks_adj;
+    const double cost = (double)(pf + 2 * pa) * (G + 0.5);  // the adjoint step takes about twice as long
     if (cost < best_cost - 1e-9) {
       best_cost = cost;
       best = G;
@@ -801,11 +814,13 @@ int adfwi_acoustic_plan_create(const adfwi_acoustic_desc* desc, const int32_t* s
   // 16 x 64 tiles: units of G shots spread over the resident blocks of the pipelined steps.
   {
     const int ntiles = ((p->nxp + ac2::TX - 1) / ac2::TX) * ((p->nzp - p->zbeg + ac2::TZ - 1) / ac2::TZ);
-    const int blocks = p->elem == 8 ? resident_tma_blocks<double>() : resident_tma_blocks<float>();
+    const int blocks = p->elem == 8 ? resident_adj_blocks<double>() : resident_adj_blocks<float>();
+    const int fblocks = p->elem == 8 ? resident_fwd_blocks<double>() : resident_fwd_blocks<float>();
     int G2 = d.shots_per_block;
-    if (G2 <= 0) G2 = pick_unit_shots(d.ns, ntiles, blocks);
+    if (G2 <= 0) G2 = pick_unit_shots(d.ns, ntiles, fblocks, blocks);
     build_tiling(p, &p->t2, ac2::TZ, ac2::TX, G2, rcv_z, rcv_x);
     p->t2.blocks = std::max(1, std::min(blocks, p->t2.ntiles * p->t2.ngroups));
+    p->t2.fwd_blocks = std::max(1, std::min(fblocks, p->t2.ntiles * p->t2.ngroups));
   }
   if (t.empty()) t.push_back(0);
 

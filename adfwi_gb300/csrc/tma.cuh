@@ -27,7 +27,16 @@ int make_plane_map(CUtensorMap* map, const void* base, int elem_bytes, const Lay
                    int box_x, int box_y);
 
 // ---------------------------------------------------------------------------- device side
-constexpr unsigned kWaitLimit = 1u << 26;  // bounded spin (far beyond any legitimate wait)
+// Bounded spin: a wait gives up after kWaitNs nanoseconds of the global timer (far beyond any
+// legitimate wait; one try_wait may itself suspend the thread for a while, so the bound is
+// on elapsed time, not on the number of polls).
+constexpr unsigned long long kWaitNs = 2000000000ull;  // 2 s
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -50,10 +59,11 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
-// Wait for the phase with the given parity to complete. Returns false after kWaitLimit polls.
+// Wait for the phase with the given parity to complete. Returns false once kWaitNs have passed.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
   const uint32_t a = smem_u32(bar);
-  for (unsigned n = 0; n < kWaitLimit; ++n) {
+  unsigned long long t0 = 0;
+  for (unsigned n = 0;; ++n) {
     uint32_t done;
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
@@ -63,8 +73,14 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
         : "r"(a), "r"(parity)
         : "memory");
     if (done) return true;
+    if ((n & 63) == 63) {
+      const unsigned long long t = global_ns();
+      if (t0 == 0)
+        t0 = t;
+      else if (t - t0 > kWaitNs)
+        return false;
+    }
   }
-  return false;
 }
 
 // One 3-D tile load into shared memory, completing on `bar` (complete_tx in bytes).

@@ -65,6 +65,17 @@ __device__ __forceinline__ void st4(double* p, const double (&r)[4]) {
   *reinterpret_cast<double2*>(p + 2) = make_double2(r[2], r[3]);
 }
 
+// read-only (non-coherent path) loads of data that no thread writes during the launch
+__device__ __forceinline__ void ldg4(const float* p, float (&r)[4]) {
+  const float4 q = __ldg(reinterpret_cast<const float4*>(p));
+  r[0] = q.x, r[1] = q.y, r[2] = q.z, r[3] = q.w;
+}
+__device__ __forceinline__ void ldg4(const double* p, double (&r)[4]) {
+  const double2 a = __ldg(reinterpret_cast<const double2*>(p));
+  const double2 b = __ldg(reinterpret_cast<const double2*>(p + 2));
+  r[0] = a.x, r[1] = a.y, r[2] = b.x, r[3] = b.y;
+}
+
 // twelve consecutive values (three 16-byte groups)
 template <typename T>
 __device__ __forceinline__ void ld12(const T* p, T (&r)[12]) {
@@ -203,13 +214,11 @@ __global__ void __launch_bounds__(VTHREADS, VMINB)
     const int rb = g.tile_rcv_beg[tile], re_ = g.tile_rcv_beg[tile + 1];
     const int64_t go = (int64_t)sgrp * PL;
     const int64_t ot = L.off(i0 + tli, j0 + 4 * tcg);  // this thread's tile cells
-    // the unit's running sums start from zero; the partial planes' values, loaded now, are
-    // added at the end so their load latency hides behind the unit's items
+    // the unit's illumination sums continue the partial planes' running sums
     T accp[4] = {T(0), T(0), T(0), T(0)}, accu[4] = {T(0), T(0), T(0), T(0)};
-    T pre_p[4] = {T(0), T(0), T(0), T(0)}, pre_u[4] = {T(0), T(0), T(0), T(0)};
     if (a.acc0 != nullptr && twin) {
-      ld4(a.acc0 + go + ot, pre_p);
-      if (a.accum_u) ld4(a.acc1 + go + ot, pre_u);
+      ld4(a.acc0 + go + ot, accp);
+      if (a.accum_u) ld4(a.acc1 + go + ot, accu);
     }
     for (int sh = s_beg; sh < s_end; ++sh, ++k) {
       const int st = k % S;
@@ -328,11 +337,6 @@ __global__ void __launch_bounds__(VTHREADS, VMINB)
       sel ^= 1;
     }
     if (a.acc0 != nullptr && twin) {
-#pragma unroll
-      for (int c = 0; c < 4; ++c) {
-        accp[c] = pre_p[c] + accp[c];
-        accu[c] = pre_u[c] + accu[c];
-      }
       st4(a.acc0 + go + ot, accp);
       if (a.accum_u) st4(a.acc1 + go + ot, accu);
     }
@@ -432,11 +436,8 @@ __global__ void __launch_bounds__(VTHREADS, VAMINB)
   const int erp = gt / CGE, ecg = gt - erp * CGE;
   const int tli = gt / CGT, tcg = gt - tli * CGT;
 
-  T cq[Q_ROUNDS][4];       // -alpha2 (masked) of this thread's q tasks
-  T ca1[2][4], cb1[2][4];  // alpha1 (masked), 1 - kappa1 (masked) at the halo task's cells
   unsigned evalid[2];      // halo cells inside the grid (and at or below zbeg)
   int ekind[2];            // 0: ordinary row, 1: row fs-1 (no sensitivity), 2: row fs+1 (fold of fs-1), -1: none
-  T b2[4], b3[4];
   unsigned tin = 0, tu = 0, tw = 0;  // tile cells inside the grid / the u region / the w region
   bool trow = false, special = false;
   int prev_tile = -1, k = 0;
@@ -448,19 +449,6 @@ __global__ void __launch_bounds__(VTHREADS, VAMINB)
     const int cb = g.tile_cell_beg[tile], ce = g.tile_cell_beg[tile + 1];
     if (tile != prev_tile) {
 #pragma unroll
-      for (int q = 0; q < Q_ROUNDS; ++q) {
-        const int t = gt + q * VG;
-        if (t < QU_TASKS) {
-          const int r = t / CGE, cg = t - r * CGE;
-          ld4(cf + ac::kA2U * PL + L.off(i0 - 1 + r, j0 - 4 + 4 * cg), cq[q]);
-        } else if (t < Q_TASKS) {
-          const int tt = t - QU_TASKS, r = tt / CGE, cg = tt - r * CGE;
-          ld4(cf + ac::kA2W * PL + L.off(i0 - 3 + r, j0 - 4 + 4 * cg), cq[q]);
-        }
-#pragma unroll
-        for (int c = 0; c < 4; ++c) cq[q][c] = -cq[q][c];
-      }
-#pragma unroll
       for (int q = 0; q < 2; ++q) {
         const int r = 2 * erp + q;
         ekind[q] = -1;
@@ -468,8 +456,6 @@ __global__ void __launch_bounds__(VTHREADS, VAMINB)
         if (!has_ext || r >= EZ) continue;
         const int i = i0 - 1 + r, jb = j0 - 4 + 4 * ecg;
         ekind[q] = (g.fsurf && i == g.fs - 1) ? 1 : ((g.fsurf && i == g.fs + 1 && r >= 2) ? 2 : 0);
-        ld4(cf + ac::kA1M * PL + L.off(i, jb), ca1[q]);
-        ld4(cf + ac::kB1 * PL + L.off(i, jb), cb1[q]);
 #pragma unroll
         for (int c = 0; c < 4; ++c)
           if (i >= g.zbeg && i < L.nzp && jb + c >= 0 && jb + c < L.nxp) evalid[q] |= 1u << c;
@@ -477,8 +463,6 @@ __global__ void __launch_bounds__(VTHREADS, VAMINB)
       {
         const int i = i0 + tli, jb = j0 + 4 * tcg;
         trow = i < L.nzp;
-        ld4(cf + ac::kB2 * PL + L.off(i, jb), b2);
-        ld4(cf + ac::kB3 * PL + L.off(i, jb), b3);
         tin = tu = tw = 0;
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
@@ -513,6 +497,20 @@ __global__ void __launch_bounds__(VTHREADS, VAMINB)
     const bool inject = a.it >= 1 && (a.rec_p != nullptr || a.rec_u != nullptr || a.rec_w != nullptr) && ce > cb;
     for (int sh = s_beg; sh < s_end; ++sh, ++k) {
       const int st = k % S;
+      // the coefficients of A (re-read per item through the read-only path, so they need no
+      // registers across items) are requested before the stage wait
+      T cq[Q_ROUNDS][4];
+#pragma unroll
+      for (int q = 0; q < Q_ROUNDS; ++q) {
+        const int t = gt + q * VG;
+        if (t < QU_TASKS) {
+          const int r = t / CGE, cg = t - r * CGE;
+          ldg4(cf + ac::kA2U * PL + L.off(i0 - 1 + r, j0 - 4 + 4 * cg), cq[q]);
+        } else if (t < Q_TASKS) {
+          const int tt = t - QU_TASKS, r = tt / CGE, cg = tt - r * CGE;
+          ldg4(cf + ac::kA2W * PL + L.off(i0 - 3 + r, j0 - 4 + 4 * cg), cq[q]);
+        }
+      }
       bool ready = !aborted(h);
       if (ready && !mbar_wait(&h->full[st], (k / S) & 1)) {
         set_abort(h, a.flag);
@@ -538,7 +536,7 @@ __global__ void __launch_bounds__(VTHREADS, VAMINB)
             T x[4];
             ld4((isu ? LU : LW) + o, x);
 #pragma unroll
-            for (int c = 0; c < 4; ++c) x[c] = cq[q][c] * x[c];
+            for (int c = 0; c < 4; ++c) x[c] = -cq[q][c] * x[c];
             st4((isu ? QU : QW) + o, x);
           }
         }
@@ -565,6 +563,10 @@ __global__ void __launch_bounds__(VTHREADS, VAMINB)
           const int kind = ekind[q];
           if (kind < 0) continue;
           const int r = 2 * erp + q;
+          const int64_t oc = L.off(i0 - 1 + r, j0 - 4 + 4 * ecg);
+          T ca1[4], cb1[4];
+          ldg4(cf + ac::kA1M * PL + oc, ca1);
+          ldg4(cf + ac::kB1 * PL + oc, cb1);
           T v[4] = {T(0), T(0), T(0), T(0)};
           if (kind != 1) {  // the mirrored row fs-1 carries no sensitivity
             lp_mid(r, v);
@@ -583,7 +585,7 @@ __global__ void __launch_bounds__(VTHREADS, VAMINB)
             ld4(DH + r * BOXX + 4 * ecg, dh);
 #pragma unroll
             for (int c = 0; c < 4; ++c) {
-              lpo[c] = cb1[q][c] * v[c];
+              lpo[c] = cb1[c] * v[c];
               if ((evalid[q] >> c) & 1u) ag1[q][c] -= v[c] * dh[c];
             }
             if (special)
@@ -593,7 +595,7 @@ __global__ void __launch_bounds__(VTHREADS, VAMINB)
           }
           T qp[4];
 #pragma unroll
-          for (int c = 0; c < 4; ++c) qp[c] = -ca1[q][c] * v[c];
+          for (int c = 0; c < 4; ++c) qp[c] = -ca1[c] * v[c];
           st4(QP + r * BOXX + 4 * ecg, qp);
         }
       }
@@ -601,7 +603,12 @@ __global__ void __launch_bounds__(VTHREADS, VAMINB)
       // ---- C: lambda_u, lambda_w, dL/d alpha2
       if (ready && trow) {
         const int r = tli + 1, b = 4 * tcg + 4;
-        T lu[4], lw[4], luo[4], lwo[4];
+        T lu[4], lw[4], luo[4], lwo[4], b2[4], b3[4];
+        {
+          const int64_t oc = L.off(i0 + tli, j0 + 4 * tcg);
+          ldg4(cf + ac::kB2 * PL + oc, b2);
+          ldg4(cf + ac::kB3 * PL + oc, b3);
+        }
         ld4(LU + r * BOXX + b, lu);
         ld4(LW + (r + 2) * BOXX + b, lw);
         {

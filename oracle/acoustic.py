@@ -20,7 +20,11 @@ C1 = 9.0 / 8.0
 C2 = -1.0 / 24.0
 
 
-def _cpu_only(*ts):
+def _cpu_only(*ts, allow_gpu=False):
+    """The oracle checks results on the CPU. ``allow_gpu`` lets a timing test run the same
+    PyTorch loop on CUDA tensors as the plain (reference-shaped) GPU path it is compared to."""
+    if allow_gpu:
+        return
     for t in ts:
         if torch.is_tensor(t) and t.device.type != "cpu":
             raise RuntimeError("oracle runs on the CPU only")
@@ -45,7 +49,7 @@ def _step(p, u, w, it, co, src, rcv, fs, free_surface, dt, nabc, nz, nx):
               + w[:, fs + 1:nzp - 2, xi] - w[:, fs:nzp - 3, xi])
         + C2 * (u[:, zi, 3:nxp - 1] - u[:, zi, 0:nxp - 4]
                 + w[:, fs + 2:nzp - 1, xi] - w[:, fs - 1:nzp - 4, xi])))
-    shots = torch.arange(ns)
+    shots = torch.arange(ns, device=p.device)
     pn[shots, sz, sx] = pn[shots, sz, sx] + dt * wav[:, it]
     if free_surface:
         pn[:, fs - 1, :] = -pn[:, fs + 1, :]
@@ -72,35 +76,37 @@ def _step(p, u, w, it, co, src, rcv, fs, free_surface, dt, nabc, nz, nx):
 
 
 def acoustic_forward(vp, rho, damp, src_x, src_z, wavelet, rcv_x, rcv_z, *, nabc, free_surface,
-                     dx, dz, dt, checkpoint_segments=1):
+                     dx, dz, dt, checkpoint_segments=1, allow_gpu=False):
     """Records of the reference acoustic propagator (acoustic_kernels.py:179-301).
 
     ``vp``, ``rho``: (nz, nx); ``damp``: (nz+2nabc, nx+2nabc); ``src_*``: int (ns,);
     ``wavelet``: (ns, nt); ``rcv_*``: int (nr,). Returns the reference's record dict.
     Differentiable w.r.t. ``vp`` and ``rho`` through autograd.
     """
-    _cpu_only(vp, rho, damp, wavelet)
+    _cpu_only(vp, rho, damp, wavelet, allow_gpu=allow_gpu)
     c = pad_edge(vp, nabc)
     den = pad_edge(rho, nabc)
     alpha1 = den * c * c * dt / dz
     alpha2 = dt / (den * dz)
     return acoustic_forward_coef(alpha1, alpha2, damp, src_x, src_z, wavelet, rcv_x, rcv_z, nabc=nabc,
-                                 free_surface=free_surface, dt=dt, checkpoint_segments=checkpoint_segments)
+                                 free_surface=free_surface, dt=dt, checkpoint_segments=checkpoint_segments,
+                                 allow_gpu=allow_gpu)
 
 
 def acoustic_forward_coef(alpha1, alpha2, damp, src_x, src_z, wavelet, rcv_x, rcv_z, *, nabc, free_surface, dt,
-                          checkpoint_segments=1):
+                          checkpoint_segments=1, allow_gpu=False):
     """The time loop of acoustic_kernels.py:239-301 given alpha1 = rho c^2 dt/dz and
     alpha2 = dt/(rho dz) on the padded grid (differentiable w.r.t. both)."""
-    _cpu_only(alpha1, alpha2, damp, wavelet)
+    _cpu_only(alpha1, alpha2, damp, wavelet, allow_gpu=allow_gpu)
     nzp, nxp = alpha1.shape
     nz, nx = nzp - 2 * nabc, nxp - 2 * nabc
     dtype = alpha1.dtype
+    dev = alpha1.device
     fs = nabc if free_surface else 1
-    sx = torch.as_tensor(src_x, dtype=torch.long) + nabc
-    sz = torch.as_tensor(src_z, dtype=torch.long) + nabc
-    rx = torch.as_tensor(rcv_x, dtype=torch.long) + nabc
-    rz = torch.as_tensor(rcv_z, dtype=torch.long) + nabc
+    sx = torch.as_tensor(src_x, dtype=torch.long, device=dev) + nabc
+    sz = torch.as_tensor(src_z, dtype=torch.long, device=dev) + nabc
+    rx = torch.as_tensor(rcv_x, dtype=torch.long, device=dev) + nabc
+    rz = torch.as_tensor(rcv_z, dtype=torch.long, device=dev) + nabc
     ns = sx.numel()
     damp = damp.to(dtype)
     kappa1 = damp * dt
@@ -109,17 +115,17 @@ def acoustic_forward_coef(alpha1, alpha2, damp, src_x, src_z, wavelet, rcv_x, rc
     kappa3 = torch.zeros_like(damp)
     kappa3[fs:nzp - 2, :] = 0.5 * (damp[fs:nzp - 2, :] + damp[fs + 1:nzp - 1, :]) * dt
     co = (alpha1, kappa1, alpha2, kappa2, kappa3)
-    p = torch.zeros((ns, nzp, nxp), dtype=dtype)
-    u = torch.zeros((ns, nzp, nxp - 1), dtype=dtype)
-    w = torch.zeros((ns, nzp - 1, nxp), dtype=dtype)
-    fwp = torch.zeros((nz, nx), dtype=dtype)
-    fwu = torch.zeros((nz, nx), dtype=dtype)
-    fww = torch.zeros((nz, nx), dtype=dtype)
+    p = torch.zeros((ns, nzp, nxp), dtype=dtype, device=dev)
+    u = torch.zeros((ns, nzp, nxp - 1), dtype=dtype, device=dev)
+    w = torch.zeros((ns, nzp - 1, nxp), dtype=dtype, device=dev)
+    fwp = torch.zeros((nz, nx), dtype=dtype, device=dev)
+    fwu = torch.zeros((nz, nx), dtype=dtype, device=dev)
+    fww = torch.zeros((nz, nx), dtype=dtype, device=dev)
     recs = ([], [], [])
     for chunk in torch.chunk(wavelet, checkpoint_segments, dim=-1):
-        seg_p = torch.zeros((nz, nx), dtype=dtype)
-        seg_u = torch.zeros((nz, nx), dtype=dtype)
-        seg_w = torch.zeros((nz, nx), dtype=dtype)
+        seg_p = torch.zeros((nz, nx), dtype=dtype, device=dev)
+        seg_u = torch.zeros((nz, nx), dtype=dtype, device=dev)
+        seg_w = torch.zeros((nz, nx), dtype=dtype, device=dev)
         for it in range(chunk.shape[-1]):
             p, u, w, rec, sq = _step(p, u, w, it, co, (sz, sx, chunk), (rz, rx), fs, free_surface,
                                      dt, nabc, nz, nx)

@@ -172,7 +172,7 @@ def gpu_arm(args, world, rank, local):
 
     dev = torch.device("cuda", local)
     torch.cuda.set_device(dev)
-    model, survey, vp_true, vp_init = acoustic_gradient_case(seed=0, device=str(dev))
+    model, survey, vp_true, vp_init = acoustic_gradient_case(seed=0, device=str(dev), nt=args.nt)
     free, _ = torch.cuda.mem_get_info(dev)
     prop = A.AcousticPropagator(model, survey, device=str(dev), memory_budget=int(args.memory_fraction * free))
     nt, dt, ns = prop.nt, prop.dt, prop.src_n
@@ -315,6 +315,88 @@ def serving_arm(args, dev):
     return out
 
 
+def elastic_arm(args, dev):
+    """VTI-elastic velocity-stress gradient (200 x 400, dx = 10 m, PML 40 + free surface -> 242 x 480
+    padded cells, 4th order, nt = 2000, dt = 0.8 ms, 15 Hz Ricker explosive sources, 20 shots,
+    400 receivers; vx / vz records weighted by fixed random traces; gradients for vp, vs, rho,
+    eps and delta through the hand-written adjoint)."""
+    import adfwi_gb300 as A
+    from adfwi_gb300.synthetic import vti_gradient_case
+    model, survey = vti_gradient_case(seed=0, device=str(dev))
+    prop = A.ElasticPropagator(model, survey, device=str(dev))
+    nt, ns = prop.nt, prop.src_n
+    gen = torch.Generator().manual_seed(0)
+    w = {k: torch.randn((ns, nt, prop.rcv_n), generator=gen).to(dev) for k in ("vx", "vz")}
+
+    def step():
+        for par in ("vp", "vs", "rho", "eps", "delta"):
+            getattr(model, par).grad = None
+        rec = prop.forward(fd_order=4)
+        loss = (rec["vx"] * w["vx"]).sum() + (rec["vz"] * w["vz"]).sum()
+        loss.backward()
+        return rec
+
+    rec = step()
+    nzp, nxp = prop.padded_coefficients(model, 4)[0][0].shape
+    cells = ns * nzp * nxp * nt
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = max(1, min(args.steps, 3))
+    e0.record()
+    for _ in range(reps):
+        step()
+    e1.record()
+    torch.cuda.synchronize(dev)
+    ms = e0.elapsed_time(e1) / reps
+    _, plan = prop.plan(None, 4)
+    return {"workload": "VTI elastic gradient (vp, vs, rho, eps, delta): 200x400, PML 40 + free surface "
+                        "(242x480 padded), 4th order, nt=2000, dt=0.8 ms, 20 shots, 400 receivers, FP32",
+            "value": round(cells / (ms * 1e-3) / 1e9, 3), "unit": UNIT, "ms_per_gradient": round(ms, 2),
+            "steps": reps, "snapshot_every": plan.snapshot_every, "grid_padded": [int(nzp), int(nxp)]}
+
+
+def precision_study(args):
+    """Snapshot precision against the FP64 instance of the same scheme on the 500 x 1500 model
+    (linear 1500 -> 3000 m/s with a +300 m/s Gaussian anomaly, dx = 12.5 m, PML 50, nt = 6000,
+    dt = 1 ms, 10 Hz Ricker): FP32 stencils with checkpoints every 50 steps kept in FP32, BF16 and
+    FP16 (per-snapshot max-abs scale), against FP64 stencils and FP64 checkpoints. Shots: every
+    8th of the 64 evenly spaced surface shots. Errors: relative L2 of the pressure records and of
+    dL/dvp for L = sum(records x fixed random traces)."""
+    import adfwi_gb300 as A
+    from adfwi_gb300.synthetic import linear_gradient_with_anomaly, surface_acquisition
+    dev = torch.device("cuda", 0)
+    nz, nx, dx, nt, dt, f0 = 500, 1500, 12.5, args.precision_nt, 1e-3, 10.0
+    vp = linear_gradient_with_anomaly(nz, nx)
+    sv64 = surface_acquisition(nx, nt, dt, f0, 64)
+    idx = np.arange(0, 64, 8)
+    gen = torch.Generator().manual_seed(0)
+    wts = torch.randn((len(idx), nt, nx), generator=gen, dtype=torch.float64)
+    out = {}
+    runs = [("fp64", torch.float64, "native"), ("fp32", torch.float32, "native"), ("fp32_bf16", torch.float32, "bf16"),
+            ("fp32_fp16", torch.float32, "fp16")]
+    for name, dtype, prec in runs:
+        npdt = np.float64 if dtype == torch.float64 else np.float32
+        model = A.AcousticModel(0, 0, nx, nz, dx, dx, vp=vp.astype(npdt), rho=(np.power(vp, 0.25) * 310).astype(npdt),
+                                vp_grad=True, nabc=50, device=str(dev), dtype=dtype)
+        prop = A.AcousticPropagator(model, sv64, device=str(dev), dtype=dtype, snapshot_precision=prec,
+                                    snapshot_every=50)
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        rec = prop.forward(shot_index=idx)
+        (rec["p"] * wts.to(dev, dtype)).sum().backward()
+        torch.cuda.synchronize(dev)
+        out[name] = {"rec": rec["p"].detach().double().cpu(), "grad": model.vp.grad.detach().double().cpu(),
+                     "s": time.perf_counter() - t0}
+        del model, prop, rec
+        torch.cuda.empty_cache()
+    ref = out["fp64"]
+    rel = lambda a, b: float((a - b).norm() / b.norm())  # noqa: E731
+    res = {name: {"records_rel_l2": rel(v["rec"], ref["rec"]), "grad_vp_rel_l2": rel(v["grad"], ref["grad"]),
+                  "seconds": round(v["s"], 2)} for name, v in out.items() if name != "fp64"}
+    return {"study": "snapshot precision vs FP64 GPU run", "grid": [nz, nx], "dx": dx, "nt": nt, "shots": len(idx),
+            "snapshot_every": 50, "fp64_seconds": round(ref["s"], 2), "results": res}
+
+
 def cpu_sample(n_steps, threads):
     """Time the CPU oracle on a bounded sample: 1 shot of the gradient workload, n_steps steps,
     forward + autograd backward (the reference's own gradient mechanism)."""
@@ -374,18 +456,32 @@ def main():
     ap.add_argument("--memory-fraction", type=float, default=0.7,
                     help="share of free HBM the gradient workspace may use (snapshot / history sizing)")
     ap.add_argument("--cpu-sample-steps", type=int, default=300)
+    ap.add_argument("--nt", type=int, default=3000,
+                    help="time steps of the gradient workload (the measured configuration has 3000; fewer steps "
+                         "keep the same per-launch shapes for small profiling captures)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--serve-requests", type=int, default=48,
                     help="requests of the served mixed-size stream (0 skips the serving measurement)")
     ap.add_argument("--serve-rate", type=float, default=50.0, help="Poisson arrival rate of the served stream (1/s)")
     ap.add_argument("--serve-slots", type=int, default=4, help="concurrent solves of the server")
+    ap.add_argument("--no-elastic", action="store_true", help="skip the VTI-elastic gradient measurement")
+    ap.add_argument("--precision", action="store_true",
+                    help="run only the snapshot-precision study (BF16 / FP16 / FP32 checkpoints vs FP64)")
+    ap.add_argument("--precision-nt", type=int, default=6000)
     args = ap.parse_args()
     world, rank, local = dist_setup()
+    if args.precision:
+        if rank == 0:
+            print(json.dumps(precision_study(args)), flush=True)
+        return
     if args.impl == "reference":
         if rank == 0:
             print(json.dumps(reference_arm(args)), flush=True)
         return
     line = gpu_arm(args, world, rank, local)
+    if world == 1 and not args.no_elastic:
+        torch.cuda.empty_cache()
+        line["elastic"] = elastic_arm(args, torch.device("cuda", local))
     if world == 1 and args.serve_requests > 0:
         torch.cuda.empty_cache()
         line["serving"] = serving_arm(args, torch.device("cuda", local))

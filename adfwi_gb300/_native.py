@@ -73,6 +73,9 @@ def _bind(lib):
         "adfwi_elastic_snapshot_every": (c_int32, [P, ctypes.POINTER(c_int32)]),
         "adfwi_elastic_forward": (c_int32, [P, P, P, P, P, P, c_int32, P, c_int64, P]),
         "adfwi_elastic_backward": (c_int32, [P, P, P, P, P, P, c_int64, P]),
+        "adfwi_l2_misfit_workspace_bytes": (c_int32, [c_int32, c_int32, c_int32, ctypes.POINTER(c_int64)]),
+        "adfwi_l2_misfit": (c_int32, [c_int32, c_int32, c_int32, c_int32, ctypes.c_double, ctypes.c_double, c_int32,
+                                      P, P, P, P, P, c_int64, P]),
     })
     for name, (res, args) in list(sig.items()) + list(optional.items()):
         fn = getattr(lib, name, None)

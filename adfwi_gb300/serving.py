@@ -38,6 +38,7 @@ import torch
 
 from .acoustic import AcousticPlan
 from .boundary import bc_pml
+from .misfit import l2_misfit_and_adjoint
 from .utils import wavelet as _wavelet
 
 _ALIGN = 256
@@ -93,7 +94,9 @@ class SolveResult:
 
 
 # ------------------------------------------------------------------------------------------
-# misfit and chain rule (explicit, so that no solve goes through the shared autograd thread)
+# misfit and chain rule without autograd (no solve goes through the shared autograd thread);
+# the server itself calls the fused CUDA misfit (adfwi_gb300.misfit), these PyTorch forms
+# state the same arithmetic and check it
 # ------------------------------------------------------------------------------------------
 def _live_traces(m, silent_rel):
     """Traces (rows of the per-trace peaks ``m``, shape (ns, nr)) that carry signal: peak > 0
@@ -310,10 +313,8 @@ class _Solve(object):
                 return None, None, out.numpy()
             obs = cv.take(shp, torch.float32)
             obs.copy_(torch.from_numpy(np.ascontiguousarray(r.obs, dtype=np.float32)))
-            loss, g_rec = l2_misfit_grad(recs[0], normalise_traces(obs, self.silent_rel), r.dt, self.silent_rel)
-            adj = cv.take(shp, torch.float32)
-            adj.copy_(g_rec)
-            del g_rec
+            loss, adj = l2_misfit_and_adjoint(recs[0], obs, r.dt, silent_rel=self.silent_rel, stream=h,
+                                              adj=cv.take(shp, torch.float32))
             ga1, _ = self.plan.run_backward(a1, a2, damp, wav, (adj, None, None), ws, stream=h)
             code = self.plan.status(ws, True, stream=h)
             if code != 0:

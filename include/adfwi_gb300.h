@@ -159,6 +159,25 @@ int adfwi_acoustic_status(const adfwi_acoustic_plan* plan, const void* workspace
                           int64_t workspace_bytes, int32_t with_gradient, int32_t* status,
                           void* stream);
 
+/* ------------------------------------------------------------------------- */
+/* Normalised L2 trace misfit and its adjoint source.                          */
+/* ------------------------------------------------------------------------- */
+
+/* Workspace bytes of adfwi_l2_misfit for ns shots and nr receivers. */
+int adfwi_l2_misfit_workspace_bytes(int32_t dtype, int32_t ns, int32_t nr, int64_t* bytes);
+
+/* loss = sum over traces (s, r) of sqrt(sum_t (obs/max|obs| - syn/max|syn|)^2 dt) and
+ * adj = dL/dsyn, for records syn, obs of shape (ns, nt, nr). Replaces the reference's
+ * misfit evaluation ADFWI/fwi/misfit/L2.py:26-29 on the traces normalised at
+ * ADFWI/fwi/acoustic_fwi.py:149-150, and its autograd backward. `loss` is ONE device double;
+ * every sum is FP64 in a fixed order (deterministic). flags bit 0: normalise obs (else obs is
+ * used as given). Traces whose peak is at most silent_rel times their gather's peak count as
+ * zero (silent_rel = 0 keeps the reference's rule, under which an all-zero trace divides by
+ * zero). Stream-ordered; allocates nothing. */
+int adfwi_l2_misfit(int32_t dtype, int32_t ns, int32_t nt, int32_t nr, double dt, double silent_rel,
+                    int32_t flags, const void* syn, const void* obs, void* adj, double* loss,
+                    void* workspace, int64_t workspace_bytes, void* stream);
+
 /* Forward solve that allocates nothing, for callers that cannot call cudaMalloc: hosts whose
  * device memory is entirely owned by another allocator or pool, sandboxed plug-ins that may
  * not grow their footprint after start-up, or code running where an allocation would break

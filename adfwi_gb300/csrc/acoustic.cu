@@ -352,6 +352,24 @@ int vec_stages() {
   return sizeof(T) == 8 ? 2 : (ac2::VMINB >= 3 ? 3 : 4);
 }
 
+// Launch of a persistent step kernel with programmatic stream serialisation (the kernel
+// calls griddepcontrol.wait before touching data of the previous launch).
+template <typename T>
+cudaError_t launch_pdl(void (*kernel)(ac2::Maps, ac::Geo<T>, ac2::StepArgs<T>), int blocks, int smem, cudaStream_t st,
+                       const ac2::Maps& maps, const ac::Geo<T>& g, const ac2::StepArgs<T>& a) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)blocks);
+  cfg.blockDim = dim3(ac2::VTHREADS);
+  cfg.dynamicSmemBytes = (size_t)smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, maps, g, a);
+}
+
 template <typename T>
 ac2::StepArgs<T> step_args(const adfwi_acoustic_plan* p, int it, const T* cf, int* flag) {
   ac2::StepArgs<T> a;
@@ -389,8 +407,7 @@ int launch_fwd(const adfwi_acoustic_plan* p, const ac::Geo<T>& g, int it, int ac
   a.acc0 = ilp;
   a.acc1 = ilu;
   const int smem = ac2::VecFwdLayout<T>::bytes(a.stages);
-  ADFWI_LAUNCH(kAcFwdStep, st,
-               (ac2::fwd_step_vec<T><<<p->t2.fwd_blocks, ac2::VTHREADS, smem, st>>>(maps, g, a)));
+  ADFWI_LAUNCH(kAcFwdStep, st, ADFWI_CUDA_TRY(launch_pdl(ac2::fwd_step_vec<T>, p->t2.fwd_blocks, smem, st, maps, g, a)));
   return kOk;
 }
 
@@ -417,8 +434,7 @@ int launch_adj(const adfwi_acoustic_plan* p, const ac::Geo<T>& g, int it, const 
   a.acc0 = g1;
   a.acc1 = g2;
   const int smem = ac2::VecAdjLayout<T>::bytes(a.stages);
-  ADFWI_LAUNCH(kAcAdjStep, st,
-               (ac2::adj_step_vec<T><<<p->t2.blocks, ac2::VTHREADS, smem, st>>>(maps, g, a)));
+  ADFWI_LAUNCH(kAcAdjStep, st, ADFWI_CUDA_TRY(launch_pdl(ac2::adj_step_vec<T>, p->t2.blocks, smem, st, maps, g, a)));
   return kOk;
 }
 

@@ -123,6 +123,8 @@ __global__ void __launch_bounds__(VTHREADS, VMINB)
     fence_barrier_init();
   }
   __syncthreads();
+  griddep_launch_dependents();
+  griddep_wait();
   const int nunits = a.ntiles * a.ngroups;
   const int per = (nunits + gridDim.x - 1) / gridDim.x;
   const int u_beg = blockIdx.x * per, u_end = min(nunits, u_beg + per);
@@ -404,6 +406,8 @@ __global__ void __launch_bounds__(VTHREADS, VAMINB)
     fence_barrier_init();
   }
   __syncthreads();
+  griddep_launch_dependents();
+  griddep_wait();
   const int nunits = a.ntiles * a.ngroups;
   const int per = (nunits + gridDim.x - 1) / gridDim.x;
   const int u_beg = blockIdx.x * per, u_end = min(nunits, u_beg + per);

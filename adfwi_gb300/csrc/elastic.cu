@@ -151,6 +151,13 @@ __device__ __forceinline__ T dzb_t(const Geo<T>& g, const Q& q, int i, int j) {
   const int64_t PL = g.L.plane, NSP = (int64_t)g.ns * PL;                            \
   const int64_t oc = g.L.off(i, j);
 
+// Gradient kernels: blockIdx.y picks a group of `eg` consecutive shots; the group's gradient
+// partials (8 planes) start at gpart + blockIdx.y * 8 * PL and are summed over the groups in a
+// fixed order at the end of the backward pass (deterministic).
+#define EL_SHOT_GROUP                                                                \
+  const int s_beg = blockIdx.y * eg, s_end = min(g.ns, s_beg + eg);                  \
+  T* gbase = gpart + (int64_t)blockIdx.y * 8 * PL;
+
 // ======================================================================= forward, PML
 // Split stresses in I (elastic_kernels.py:351-356), then the moment-tensor source on both
 // split parts (359-372). ts: 6 fields; v: vx, vz totals at the start of the step.
@@ -507,25 +514,56 @@ __global__ void adj_vfs_pml(Geo<T> g, const T* __restrict__ cf, const T* __restr
   lvs[VZ_Z * NSP + o] = sz * lvs[VZ_Z * NSP + o] + az;
 }
 
+// One plane of a (field, shot) block read at grid cells; the block's ghost frame is zero.
+template <typename T>
+struct PlaneQ {
+  const T* base;
+  Layout L;
+  __device__ __forceinline__ T operator()(int ii, int jj) const { return base[L.off(ii, jj)]; }
+};
+
+// (B3q) the velocity update's adjoint sources, once per cell and shot (zero outside I):
+// q = lambda(v split) * dt * b / (d * pml_d) for (vx_x, vx_z, vz_x, vz_z); PMLM = 0 uses the
+// absorbing-layer velocities (no pml_d).
+template <typename T, bool PMLM>
+__global__ void adj_tq(Geo<T> g, const T* __restrict__ cf, const T* __restrict__ lvv, T* __restrict__ q4) {
+  EL_CELL_SHOT
+  T a = T(0), b = T(0), c = T(0), d = T(0);
+  if (in_I(g, i, j)) {
+    const int64_t c0 = g.L.off(i, j);
+    const T bx = cf[BX * PL + c0], bz = cf[BZ * PL + c0];
+    if (PMLM) {
+      const Pml<T> p = pml_at(g, cf, c0, PL);
+      a = lvv[VX_X * NSP + o] * (g.dt * bx) / (g.dx * p.xd);
+      b = lvv[VX_Z * NSP + o] * (g.dt * bx) / (g.dz * p.zd);
+      c = lvv[VZ_X * NSP + o] * (g.dt * bz) / (g.dx * p.xd);
+      d = lvv[VZ_Z * NSP + o] * (g.dt * bz) / (g.dz * p.zd);
+    } else {
+      a = lvv[VX * NSP + o] * (g.dt * bx) / g.dx;
+      b = lvv[VX * NSP + o] * (g.dt * bx) / g.dz;
+      c = lvv[VZ * NSP + o] * (g.dt * bz) / g.dx;
+      d = lvv[VZ * NSP + o] * (g.dt * bz) / g.dz;
+    }
+  }
+  q4[0 * NSP + o] = a;
+  q4[1 * NSP + o] = b;
+  q4[2 * NSP + o] = c;
+  q4[3 * NSP + o] = d;
+}
+
 // (B3a) lt += transposes of the velocity update's stress differences; bx, bz gradients.
 template <typename T, int NN>
-__global__ void adj_t_pml(Geo<T> g, const T* __restrict__ cf, const T* __restrict__ lvs, T* lt,
-                          const T* __restrict__ tt_hist, T* gbx, T* gbz) {
+__global__ void adj_t_pml(Geo<T> g, const T* __restrict__ cf, const T* __restrict__ lvs,
+                          const T* __restrict__ q4, T* lt, const T* __restrict__ tt_hist, T* gpart, int eg) {
   EL_CELL
+  EL_SHOT_GROUP
+  T* gbx = gbase + 6 * PL;
+  T* gbz = gbase + 7 * PL;
   T gx = T(0), gz = T(0);
-  for (int s = 0; s < g.ns; ++s) {
+  for (int s = s_beg; s < s_end; ++s) {
     const int64_t so = (int64_t)s * PL;
-    auto qf = [&](int comp, bool xdir, int ii, int jj) -> T {
-      if (!in_I(g, ii, jj)) return T(0);
-      const int64_t c = g.L.off(ii, jj);
-      const T bcoef = cf[(comp < 2 ? BX : BZ) * PL + c];
-      const Pml<T> p = pml_at(g, cf, c, PL);
-      return lvs[comp * NSP + so + c] * (g.dt * bcoef) / (xdir ? g.dx * p.xd : g.dz * p.zd);
-    };
-    auto q_vxx = [&](int ii, int jj) { return qf(VX_X, true, ii, jj); };
-    auto q_vxz = [&](int ii, int jj) { return qf(VX_Z, false, ii, jj); };
-    auto q_vzx = [&](int ii, int jj) { return qf(VZ_X, true, ii, jj); };
-    auto q_vzz = [&](int ii, int jj) { return qf(VZ_Z, false, ii, jj); };
+    const PlaneQ<T> q_vxx{q4 + 0 * NSP + so, g.L}, q_vxz{q4 + 1 * NSP + so, g.L};
+    const PlaneQ<T> q_vzx{q4 + 2 * NSP + so, g.L}, q_vzz{q4 + 3 * NSP + so, g.L};
     const int64_t o = so + oc;
     lt[TXX * NSP + o] += dxf_t<NN>(g, q_vxx, i, j);
     lt[TXZ * NSP + o] += dzb_t<NN>(g, q_vxz, i, j) + dxb_t<NN>(g, q_vzx, i, j);
@@ -575,54 +613,75 @@ struct StressQ {
   T a, b, c, d, e, f;  // xx_x, xx_z, zz_x, zz_z, xz_x, xz_z
 };
 
+// Coefficient-weighted adjoint sources of the stress update at cell (i, j) of one shot.
+template <typename T, bool PMLM>
+__device__ __forceinline__ StressQ<T> stress_q(const Geo<T>& g, const T* __restrict__ cf,
+                                               const T* __restrict__ lts, int64_t c0, int64_t oo, int64_t PL,
+                                               int64_t NSP) {
+  StressQ<T> r;
+  if (PMLM) {
+    const Pml<T> p = pml_at(g, cf, c0, PL);
+    const T kx = g.dt_dx / p.xd, kz = g.dt_dz / p.zd;
+    r.a = lts[TXX_X * NSP + oo] * kx;
+    r.b = lts[TXX_Z * NSP + oo] * kz;
+    r.c = lts[TZZ_X * NSP + oo] * kx;
+    r.d = lts[TZZ_Z * NSP + oo] * kz;
+    r.e = lts[TXZ_X * NSP + oo] * kx;
+    r.f = lts[TXZ_Z * NSP + oo] * kz;
+  } else {
+    const T kx = g.dt / g.dx, kz = g.dt / g.dz;
+    r.a = lts[TXX * NSP + oo] * kx;
+    r.b = lts[TXX * NSP + oo] * kz;
+    r.c = lts[TZZ * NSP + oo] * kx;
+    r.d = lts[TZZ * NSP + oo] * kz;
+    r.e = lts[TXZ * NSP + oo] * kx;
+    r.f = lts[TXZ * NSP + oo] * kz;
+  }
+  return r;
+}
+
+// (B1q) the stress update's adjoint sources for the velocity transposes, once per cell and
+// shot (zero outside I): sx_b, sx_zb, sx_f, sx_zf, sz_b, sz_zb, sz_f, sz_zf.
+template <typename T, bool PMLM>
+__global__ void adj_vq(Geo<T> g, const T* __restrict__ cf, const T* __restrict__ lts, T* __restrict__ q8) {
+  EL_CELL_SHOT
+  T v[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) v[k] = T(0);
+  if (in_I(g, i, j)) {
+    const int64_t c0 = g.L.off(i, j);
+    const StressQ<T> r = stress_q<T, PMLM>(g, cf, lts, c0, o, PL, NSP);
+    const T c11 = cf[C11 * PL + c0], c13 = cf[C13 * PL + c0], c15 = cf[C15 * PL + c0];
+    const T c33 = cf[C33 * PL + c0], c35 = cf[C35 * PL + c0], c55 = cf[C55 * PL + c0];
+    v[0] = c11 * r.a + c13 * r.c;
+    v[1] = c15 * r.b + c35 * r.d;
+    v[2] = c15 * r.e;
+    v[3] = c55 * r.f;
+    v[4] = c15 * r.a + c35 * r.c;
+    v[5] = c13 * r.b + c33 * r.d;
+    v[6] = c55 * r.e;
+    v[7] = c35 * r.f;
+  }
+#pragma unroll
+  for (int k = 0; k < 8; ++k) q8[k * NSP + o] = v[k];
+}
+
 // (B1a) lambda of the velocity totals at the start of the step (overwrite) and the C gradients.
 // pml = 1: split-field update; pml = 0: absorbing-layer update (lts then holds txx, tzz, txz,
 // and lv is accumulated instead of overwritten because v' = v + ...).
 template <typename T, int NN, bool PMLM>
-__global__ void adj_v(Geo<T> g, const T* __restrict__ cf, const T* __restrict__ lts, T* lv,
-                      const T* __restrict__ v_hist, T* gc) {
+__global__ void adj_v(Geo<T> g, const T* __restrict__ cf, const T* __restrict__ lts, const T* __restrict__ q8,
+                      T* lv, const T* __restrict__ v_hist, T* gpart, int eg) {
   EL_CELL
+  EL_SHOT_GROUP
+  T* gc = gbase;
   T g11 = T(0), g13 = T(0), g15 = T(0), g33 = T(0), g35 = T(0), g55 = T(0);
-  for (int s = 0; s < g.ns; ++s) {
+  for (int s = s_beg; s < s_end; ++s) {
     const int64_t so = (int64_t)s * PL;
-    auto q = [&](int ii, int jj) -> StressQ<T> {
-      StressQ<T> r;
-      if (!in_I(g, ii, jj)) {
-        r.a = r.b = r.c = r.d = r.e = r.f = T(0);
-        return r;
-      }
-      const int64_t c = g.L.off(ii, jj), oo = so + c;
-      if (PMLM) {
-        const Pml<T> p = pml_at(g, cf, c, PL);
-        const T kx = g.dt_dx / p.xd, kz = g.dt_dz / p.zd;
-        r.a = lts[TXX_X * NSP + oo] * kx;
-        r.b = lts[TXX_Z * NSP + oo] * kz;
-        r.c = lts[TZZ_X * NSP + oo] * kx;
-        r.d = lts[TZZ_Z * NSP + oo] * kz;
-        r.e = lts[TXZ_X * NSP + oo] * kx;
-        r.f = lts[TXZ_Z * NSP + oo] * kz;
-      } else {
-        const T kx = g.dt / g.dx, kz = g.dt / g.dz;
-        r.a = lts[TXX * NSP + oo] * kx;
-        r.b = lts[TXX * NSP + oo] * kz;
-        r.c = lts[TZZ * NSP + oo] * kx;
-        r.d = lts[TZZ * NSP + oo] * kz;
-        r.e = lts[TXZ * NSP + oo] * kx;
-        r.f = lts[TXZ * NSP + oo] * kz;
-      }
-      return r;
-    };
-    auto C = [&](int k, int ii, int jj) { return cf[k * PL + g.L.off(ii, jj)]; };
-    // velocity-x sources
-    auto sx_b = [&](int ii, int jj) { StressQ<T> r = q(ii, jj); return C(C11, ii, jj) * r.a + C(C13, ii, jj) * r.c; };
-    auto sx_zb = [&](int ii, int jj) { StressQ<T> r = q(ii, jj); return C(C15, ii, jj) * r.b + C(C35, ii, jj) * r.d; };
-    auto sx_f = [&](int ii, int jj) { StressQ<T> r = q(ii, jj); return C(C15, ii, jj) * r.e; };
-    auto sx_zf = [&](int ii, int jj) { StressQ<T> r = q(ii, jj); return C(C55, ii, jj) * r.f; };
-    // velocity-z sources
-    auto sz_b = [&](int ii, int jj) { StressQ<T> r = q(ii, jj); return C(C15, ii, jj) * r.a + C(C35, ii, jj) * r.c; };
-    auto sz_zb = [&](int ii, int jj) { StressQ<T> r = q(ii, jj); return C(C13, ii, jj) * r.b + C(C33, ii, jj) * r.d; };
-    auto sz_f = [&](int ii, int jj) { StressQ<T> r = q(ii, jj); return C(C55, ii, jj) * r.e; };
-    auto sz_zf = [&](int ii, int jj) { StressQ<T> r = q(ii, jj); return C(C35, ii, jj) * r.f; };
+    const PlaneQ<T> sx_b{q8 + 0 * NSP + so, g.L}, sx_zb{q8 + 1 * NSP + so, g.L};
+    const PlaneQ<T> sx_f{q8 + 2 * NSP + so, g.L}, sx_zf{q8 + 3 * NSP + so, g.L};
+    const PlaneQ<T> sz_b{q8 + 4 * NSP + so, g.L}, sz_zb{q8 + 5 * NSP + so, g.L};
+    const PlaneQ<T> sz_f{q8 + 6 * NSP + so, g.L}, sz_zf{q8 + 7 * NSP + so, g.L};
     const T avx = dxb_t<NN>(g, sx_b, i, j) + dzb_t<NN>(g, sx_zb, i, j) + dxf_t<NN>(g, sx_f, i, j) +
                   dzf_t<NN>(g, sx_zf, i, j);
     const T avz = dxb_t<NN>(g, sz_b, i, j) + dzb_t<NN>(g, sz_zb, i, j) + dxf_t<NN>(g, sz_f, i, j) +
@@ -636,7 +695,7 @@ __global__ void adj_v(Geo<T> g, const T* __restrict__ cf, const T* __restrict__ 
       lv[VZ * NSP + o] += avz;
     }
     if (in_I(g, i, j)) {
-      const StressQ<T> r = q(i, j);
+      const StressQ<T> r = stress_q<T, PMLM>(g, cf, lts, oc, o, PL, NSP);
       const T* vx = v_hist + VX * NSP;
       const T* vz = v_hist + VZ * NSP;
       const T dxb_vx = dxb<NN>(g, vx, o), dxb_vz = dxb<NN>(g, vz, o);
@@ -700,22 +759,17 @@ __global__ void adj_vfs_abl(Geo<T> g, const T* __restrict__ cf, const T* __restr
 
 // ABL: lt += transposes of the velocity update's stress differences; bx, bz gradients.
 template <typename T, int NN>
-__global__ void adj_t_abl(Geo<T> g, const T* __restrict__ cf, const T* __restrict__ lv, T* lt,
-                          const T* __restrict__ tt_hist, T* gbx, T* gbz) {
+__global__ void adj_t_abl(Geo<T> g, const T* __restrict__ cf, const T* __restrict__ lv,
+                          const T* __restrict__ qv, T* lt, const T* __restrict__ tt_hist, T* gpart, int eg) {
   EL_CELL
+  EL_SHOT_GROUP
+  T* gbx = gbase + 6 * PL;
+  T* gbz = gbase + 7 * PL;
   T gx = T(0), gz = T(0);
-  for (int s = 0; s < g.ns; ++s) {
+  for (int s = s_beg; s < s_end; ++s) {
     const int64_t so = (int64_t)s * PL;
-    auto qf = [&](int comp, T den, int ii, int jj) -> T {
-      if (!in_I(g, ii, jj)) return T(0);
-      const int64_t c = g.L.off(ii, jj);
-      const T b = cf[(comp == VX ? BX : BZ) * PL + c];
-      return lv[comp * NSP + so + c] * (g.dt * b) / den;
-    };
-    auto q1 = [&](int ii, int jj) { return qf(VX, g.dx, ii, jj); };
-    auto q2 = [&](int ii, int jj) { return qf(VX, g.dz, ii, jj); };
-    auto q3 = [&](int ii, int jj) { return qf(VZ, g.dx, ii, jj); };
-    auto q4 = [&](int ii, int jj) { return qf(VZ, g.dz, ii, jj); };
+    const PlaneQ<T> q1{qv + 0 * NSP + so, g.L}, q2{qv + 1 * NSP + so, g.L};
+    const PlaneQ<T> q3{qv + 2 * NSP + so, g.L}, q4{qv + 3 * NSP + so, g.L};
     const int64_t o = so + oc;
     lt[TXX * NSP + o] += dxf_t<NN>(g, q1, i, j);
     lt[TXZ * NSP + o] += dzb_t<NN>(g, q2, i, j) + dxb_t<NN>(g, q3, i, j);
@@ -749,6 +803,21 @@ __global__ void adj_tfs_abl(Geo<T> g, T* lt) {
   zz[o0] -= zz[o2];
   zz[o2] = T(0);
   zz[o1] = T(0);
+}
+
+// Sum the shot groups' gradient partials (8 planes each) into the first group, in group order.
+template <typename T>
+__global__ void sum_groups(Layout L, int groups, T* part) {
+  const int64_t n = (int64_t)L.nzp * L.nxp;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(e / L.nxp), j = (int)(e - (int64_t)i * L.nxp);
+    const int64_t o = L.off(i, j);
+    for (int q = 0; q < 8; ++q) {
+      T acc = part[q * L.plane + o];
+      for (int gr = 1; gr < groups; ++gr) acc += part[((int64_t)gr * 8 + q) * L.plane + o];
+      part[q * L.plane + o] = acc;
+    }
+  }
 }
 
 template <typename T>
@@ -798,12 +867,26 @@ int64_t al256(int64_t x) { return (x + 255) / 256 * 256; }
 
 struct ECarve {
   int64_t coef, st, tt, vtmp, srcm, tab;       // forward
-  int64_t snap, snap_scale, hv, ht, lst, lt, lv, lv2, gc;  // gradient
+  int64_t snap, snap_scale, hv, ht, lst, lt, lv, lv2, qsrc, gc;  // gradient
   int64_t total;
 };
 
 // Coefficient planes: C11 C13 C15 C33 C35 C55 bx bz + (bcx bcz | damp)
 int ncoef(const adfwi_elastic_plan* p) { return p->d.pml ? 10 : 9; }
+
+// Shot groups of the gradient kernels: enough (cell, group) threads to fill the GPU (about
+// 600 k), at most one group per shot.
+int egroups(const adfwi_elastic_plan* p) {
+  const int64_t cells = (int64_t)p->nzp * p->nxp;
+  const int64_t want = (600000 + cells - 1) / cells;
+  const int g = (int)std::max<int64_t>(1, std::min<int64_t>(p->d.ns, want));
+  const int eg = (p->d.ns + g - 1) / g;
+  return (p->d.ns + eg - 1) / eg;
+}
+int eshots_per_group(const adfwi_elastic_plan* p) {
+  const int g = egroups(p);
+  return (p->d.ns + g - 1) / g;
+}
 
 ECarve ecarve(const adfwi_elastic_plan* p, bool grad, int K) {
   ECarve c{};
@@ -831,7 +914,8 @@ ECarve ecarve(const adfwi_elastic_plan* p, bool grad, int K) {
     c.lt = take(3 * ns * pl);
     c.lv = take(2 * ns * pl);
     c.lv2 = take(2 * ns * pl);
-    c.gc = take(8 * pl);
+    c.qsrc = take(8 * ns * pl);  // adjoint sources of the step transposes (8 planes per shot)
+    c.gc = take(8 * pl * egroups(p));
   }
   c.total = o;
   return c;
@@ -1055,12 +1139,19 @@ int ebackward(const adfwi_elastic_plan* p, const void* wavelet, const void* grec
   T* lv = reinterpret_cast<T*>(ws + c.lv);
   T* lv2 = reinterpret_cast<T*>(ws + c.lv2);
   T* gcp = reinterpret_cast<T*>(ws + c.gc);
+  T* qsrc = reinterpret_cast<T*>(ws + c.qsrc);
   const T* gr = static_cast<const T*>(grec);
   const int nsf = p->d.pml ? 10 : 3;
   ADFWI_CUDA_TRY(cudaMemsetAsync(lst, 0, nsf * NSP * sizeof(T), s));
   ADFWI_CUDA_TRY(cudaMemsetAsync(lt, 0, 3 * NSP * sizeof(T), s));
   ADFWI_CUDA_TRY(cudaMemsetAsync(lv, 0, 2 * NSP * sizeof(T), s));
-  ADFWI_CUDA_TRY(cudaMemsetAsync(gcp, 0, 8 * PL * sizeof(T), s));
+  const int egr = egroups(p), eg = eshots_per_group(p);
+  ADFWI_CUDA_TRY(cudaMemsetAsync(gcp, 0, (int64_t)egr * 8 * PL * sizeof(T), s));
+  {
+    // the source planes are read with their halos by the transposed stencils
+    int rc0 = zero_frames<T>(qsrc, (int64_t)8 * ns, p->L, s);
+    if (rc0) return rc0;
+  }
   ADFWI_CUDA_TRY(cudaMemsetAsync(lv2, 0, 2 * NSP * sizeof(T), s));
   if (!full) {
     // recomputed histories are read with their halos
@@ -1068,7 +1159,7 @@ int ebackward(const adfwi_elastic_plan* p, const void* wavelet, const void* grec
     if (!rc0 && p->d.pml) rc0 = zero_frames<T>(ht, (int64_t)K * 3 * ns, p->L, s);
     if (rc0) return rc0;
   }
-  const dim3 gcs = cells_grid(p, ns), gc1 = cells_grid(p, 1), b(256);
+  const dim3 gcs = cells_grid(p, ns), gcg = cells_grid(p, egroups(p)), b(256);
   const dim3 gcol((unsigned)((p->nxp + 127) / 128), ns);
   const dim3 ginj((unsigned)std::max(1, (p->ncells + 127) / 128), ns);
   const int nseg = full ? 1 : (nt + K - 1) / K;
@@ -1098,21 +1189,29 @@ int ebackward(const adfwi_elastic_plan* p, const void* wavelet, const void* grec
         ADFWI_CUDA_TRY(cudaMemsetAsync(lt, 0, 3 * NSP * sizeof(T), s));
         if (gr) ADFWI_LAUNCH(kAux, s, (el::adj_inject<T><<<ginj, 128, 0, s>>>(g, it, gr, lt, lv, 1)));
         ADFWI_LAUNCH(kElAdjStep, s, (el::adj_vfs_pml<T><<<gcs, b, 0, s>>>(g, cf, lv, lst + 6 * NSP)));
-        ADFWI_LAUNCH(kElAdjStep, s, (el::adj_t_pml<T, NN><<<gc1, b, 0, s>>>(g, cf, lst + 6 * NSP, lt, th,
-                                                                            gcp + 6 * PL, gcp + 7 * PL)));
+        ADFWI_LAUNCH(kElAdjStep, s, (el::adj_tq<T, true><<<gcs, b, 0, s>>>(g, cf, lst + 6 * NSP, qsrc)));
+        ADFWI_LAUNCH(kElAdjStep, s, (el::adj_t_pml<T, NN><<<gcg, b, 0, s>>>(g, cf, lst + 6 * NSP, qsrc, lt, th, gcp,
+                                                                            eg)));
         ADFWI_LAUNCH(kElAdjStep, s, (el::adj_tfs_pml<T><<<gcs, b, 0, s>>>(g, cf, lt, lst)));
-        ADFWI_LAUNCH(kElAdjStep, s, (el::adj_v<T, NN, true><<<gc1, b, 0, s>>>(g, cf, lst, lv, vh, gcp)));
+        ADFWI_LAUNCH(kElAdjStep, s, (el::adj_vq<T, true><<<gcs, b, 0, s>>>(g, cf, lst, qsrc)));
+        ADFWI_LAUNCH(kElAdjStep, s, (el::adj_v<T, NN, true><<<gcg, b, 0, s>>>(g, cf, lst, qsrc, lv, vh, gcp, eg)));
       } else {
         if (gr) ADFWI_LAUNCH(kAux, s, (el::adj_inject<T><<<ginj, 128, 0, s>>>(g, it, gr, lst, lv, 1)));
         ADFWI_LAUNCH(kElAdjStep, s, (el::adj_vfs_abl<T><<<gcs, b, 0, s>>>(g, cf, lv, lv2, nullptr)));
         std::swap(lv, lv2);
-        ADFWI_LAUNCH(kElAdjStep, s, (el::adj_t_abl<T, NN><<<gc1, b, 0, s>>>(g, cf, lv, lst, th, gcp + 6 * PL,
-                                                                            gcp + 7 * PL)));
+        ADFWI_LAUNCH(kElAdjStep, s, (el::adj_tq<T, false><<<gcs, b, 0, s>>>(g, cf, lv, qsrc)));
+        ADFWI_LAUNCH(kElAdjStep, s, (el::adj_t_abl<T, NN><<<gcg, b, 0, s>>>(g, cf, lv, qsrc, lst, th, gcp, eg)));
         if (p->d.free_surface) ADFWI_LAUNCH(kElAdjStep, s, (el::adj_tfs_abl<T><<<gcol, 128, 0, s>>>(g, lst)));
-        ADFWI_LAUNCH(kElAdjStep, s, (el::adj_v<T, NN, false><<<gc1, b, 0, s>>>(g, cf, lst, lv, vh, gcp)));
+        ADFWI_LAUNCH(kElAdjStep, s, (el::adj_vq<T, false><<<gcs, b, 0, s>>>(g, cf, lst, qsrc)));
+        ADFWI_LAUNCH(kElAdjStep, s, (el::adj_v<T, NN, false><<<gcg, b, 0, s>>>(g, cf, lst, qsrc, lv, vh, gcp, eg)));
       }
     }
     ADFWI_CUDA_TRY(cudaGetLastError());
+  }
+  if (egr > 1) {
+    const int64_t n = (int64_t)p->nzp * p->nxp;
+    ADFWI_LAUNCH(kAux, s, (el::sum_groups<T><<<(unsigned)std::min<int64_t>((n + 255) / 256, 4096), 256, 0, s>>>(
+                              p->L, egr, gcp)));
   }
   // gradients out: C11 C13 C15 C33 C35 C55 bx bz, each cropped to its input shape
   for (int q = 0; q < 8; ++q) {

@@ -74,6 +74,8 @@ def _bind(lib):
         "adfwi_elastic_forward": (c_int32, [P, P, P, P, P, P, c_int32, P, c_int64, P]),
         "adfwi_elastic_backward": (c_int32, [P, P, P, P, P, P, c_int64, P]),
         "adfwi_l2_misfit_workspace_bytes": (c_int32, [c_int32, c_int32, c_int32, ctypes.POINTER(c_int64)]),
+        "adfwi_smooth2d_workspace_bytes": (c_int32, [c_int32, c_int32, c_int32, ctypes.POINTER(c_int64)]),
+        "adfwi_smooth2d": (c_int32, [c_int32, c_int32, c_int32, P, P, P, c_int64, P]),
         "adfwi_l2_misfit": (c_int32, [c_int32, c_int32, c_int32, c_int32, ctypes.c_double, ctypes.c_double, c_int32,
                                       P, P, P, P, P, c_int64, P]),
     })

@@ -178,6 +178,21 @@ int adfwi_l2_misfit(int32_t dtype, int32_t ns, int32_t nt, int32_t nr, double dt
                     int32_t flags, const void* syn, const void* obs, void* adj, double* loss,
                     void* workspace, int64_t workspace_bytes, void* stream);
 
+/* ------------------------------------------------------------------------- */
+/* Gaussian smoothing of model planes (gradient processor).                    */
+/* ------------------------------------------------------------------------- */
+
+/* Workspace bytes of adfwi_smooth2d for an (nz, nx) plane. */
+int adfwi_smooth2d_workspace_bytes(int32_t nz, int32_t nx, int32_t span, int64_t* bytes);
+
+/* out = smooth2d(in, span) of ADFWI/propagator/gradient_process.py:32-49 (used by
+ * GradProcessor.forward, 91-134): 'same'-size convolution of the FP64 (nz, nx) plane `in` with a
+ * normalised Gaussian of standard deviation `span` sampled every 2 cells over [-2 span,
+ * 2 span], divided by the convolution of a plane of ones. Device arrays; stream-ordered;
+ * allocates nothing. */
+int adfwi_smooth2d(int32_t nz, int32_t nx, int32_t span, const double* in, double* out, void* workspace,
+                   int64_t workspace_bytes, void* stream);
+
 /* Forward solve that allocates nothing, for callers that cannot call cudaMalloc: hosts whose
  * device memory is entirely owned by another allocator or pool, sandboxed plug-ins that may
  * not grow their footprint after start-up, or code running where an allocation would break

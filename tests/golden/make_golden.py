@@ -7,7 +7,8 @@ None of those stubs touch the propagator arithmetic:
 ``ADFWI/propagator/acoustic_kernels.py`` and ``elastic_kernels.py`` only need
 torch and numpy.
 
-Each fixture holds the inputs of one small case, the reference's record dict
+``gradproc.npz`` holds the reference's ``smooth2d`` and ``GradProcessor.forward`` outputs on
+seeded inputs. Each propagator fixture holds the inputs of one small case, the reference's record dict
 (``AcousticPropagator.forward`` / ``ElasticPropagator.forward``), its damping
 arrays, and autograd gradients of a fixed linear functional of the records
 (``sum_k <W_k, rec_k>`` with seeded weights), so that gradient parity does
@@ -188,11 +189,59 @@ def elastic_case(R, name, *, nz, nx, nabc, nt, dt, dx, f0, ns, nr, free_surface,
     print(name, {k: np.asarray(v).shape for k, v in out.items() if isinstance(v, np.ndarray)})
 
 
+def gradproc_cases(ref_root):
+    """Fixtures of the reference's GradProcessor (gradient_process.py:74-134) and smooth2d.
+
+    scipy 1.13 removed ``scipy.signal.hamming`` (the window lives in ``scipy.signal.windows``);
+    the land taper of the reference calls the old name, so this script points the old name at
+    the window before calling it. Nothing else is changed."""
+    import scipy.signal
+    if not hasattr(scipy.signal, "hamming"):
+        scipy.signal.hamming = scipy.signal.windows.hamming
+    from ADFWI.propagator import gradient_process as G
+    rng = np.random.default_rng(31)
+    out = {"kind": "gradproc"}
+    z = rng.standard_normal((37, 53))
+    for span in (3, 10, 40):
+        out["smooth_in"] = z
+        out["smooth_%d" % span] = G.smooth2d(z, span=span)
+    cases = [
+        ("land_mute_smooth", dict(grad_mute=6, grad_smooth=3, norm_grad=True, forw_illumination=True,
+                                  marine_or_land="land"), (48, 64), True, False),
+        ("marine_mute_smooth_mask", dict(grad_mute=5, grad_smooth=2, norm_grad=True, forw_illumination=True,
+                                         marine_or_land="marine"), (36, 50), True, True),
+        ("plain_no_forw", dict(grad_mute=0, grad_smooth=0, norm_grad=False, forw_illumination=True,
+                               marine_or_land="land"), (30, 44), False, False),
+        ("marine_no_forw_f32", dict(grad_mute=4, grad_smooth=3, norm_grad=True, forw_illumination=True,
+                                    marine_or_land="marine"), (40, 45), False, False),
+    ]
+    for name, kw, (nz, nx), with_forw, with_mask in cases:
+        grad = rng.standard_normal((nz, nx)).astype(np.float32)
+        forw = (rng.random((nz, nx)) ** 3).astype(np.float32) if with_forw else None
+        mask = (rng.random((nz, nx)) > 0.2).astype(np.float32) if with_mask else None
+        gp = G.GradProcessor(grad_mask=mask, **kw)
+        res = gp.forward(nx=nx, nz=nz, vmax=3000.0, grad=grad.copy(), forw=None if forw is None else forw.copy())
+        out[name + "_grad"] = grad
+        if forw is not None:
+            out[name + "_forw"] = forw
+        if mask is not None:
+            out[name + "_mask"] = mask
+        out[name + "_out"] = np.asarray(res)
+        for k, v in kw.items():
+            out[name + "_" + k] = v
+    np.savez_compressed(os.path.join(HERE, "gradproc.npz"), **out)
+    print("gradproc", sorted(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--only", choices=["gradproc"], default=None, help="regenerate one fixture family only")
     args = ap.parse_args()
     R = import_reference(args.ref)
+    if args.only == "gradproc":
+        gradproc_cases(args.ref)
+        return
     import torch
     torch.set_num_threads(min(8, os.cpu_count() or 1))
     ac = dict(nz=24, nx=32, nabc=8, dt=1e-3, dx=10.0, f0=25.0, ns=3, nr=12)
@@ -211,6 +260,7 @@ def main():
                  abc_type="gerjan", iso=False, segments=1, dtype_name="f32", seed=14, **el)
     elastic_case(R, "elastic_vti_o6_sincos_fs_f32", nt=70, free_surface=True, fd_order=6,
                  abc_type="sincos", iso=False, segments=1, dtype_name="f32", seed=15, **el)
+    gradproc_cases(args.ref)
     # No FP64 elastic fixture: the reference's DiffCoef (elastic_kernels.py:37-56) builds its
     # right-hand side in the default dtype and its matrix in float32, so the elastic propagator
     # raises "expected scalar type Float but found Double" under a float64 default dtype.

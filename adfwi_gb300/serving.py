@@ -27,6 +27,7 @@ the same ``per_request_budget``), the kernels are deterministic (fixed-order red
 atomics), and the misfit uses fixed-order reductions, so a request returns bit-identical
 records, loss and gradient whether it runs alone or in a mix.
 """
+import collections
 import threading
 import time
 from concurrent.futures import Future
@@ -250,90 +251,148 @@ class _Carver(object):
 
 
 # ------------------------------------------------------------------------------------------
-# one solve
+# one solve shape: plan, arena buffers, and (after its second use) a captured CUDA graph
 # ------------------------------------------------------------------------------------------
-class _Solve(object):
-    """A request with its plan and its arena footprint."""
+def _shape_key(req, grad, snapshot_precision, per_request_budget, silent_rel):
+    i64 = lambda a: np.asarray(a, dtype=np.int64).tobytes()  # noqa: E731
+    return (bool(grad), tuple(np.shape(req.vp)), float(req.dx), int(req.nt), float(req.dt), float(req.f0),
+            int(req.nabc), bool(req.free_surface), i64(req.src_z), i64(req.src_x), i64(req.rcv_z), i64(req.rcv_x),
+            str(snapshot_precision), int(per_request_budget), float(silent_rel))
 
-    def __init__(self, req, snapshot_precision, per_request_budget, silent_rel=1e-6):
-        self.req = req
-        self.silent_rel = silent_rel
+
+class _Shape(object):
+    """Everything of a solve that depends only on its shape (grid, geometry, nt, dt, f0, mode):
+    the plan, the arena range with its buffers, the wavelet and damping geometry, and the CUDA
+    graph of the whole device-side solve once the shape has been solved twice.
+
+    The device-side solve (``_enqueue``) takes the model, its density, its damping frame and
+    the observed data from fixed buffers (the host computes density and damping exactly as
+    AcousticModel / AcousticPropagator do) and does every other step on the GPU -- the padded
+    coefficients, forward, misfit, adjoint and the chain rule to dL/dvp -- so one captured graph
+    replays it for any model of the shape."""
+
+    def __init__(self, req, snapshot_precision, per_request_budget, silent_rel):
         vp = np.asarray(req.vp, dtype=np.float32)
         if vp.ndim != 2:
             raise ValueError("vp must be a 2-D (nz, nx) array")
         self.nz, self.nx = vp.shape
         self.ns, self.nr = len(req.src_x), len(req.rcv_x)
-        if req.obs is not None and tuple(np.shape(req.obs)) != (self.ns, req.nt, self.nr):
-            raise ValueError("obs has shape %s, expected %s" % (np.shape(req.obs), (self.ns, req.nt, self.nr)))
         self.grad = req.obs is not None
+        if self.grad and tuple(np.shape(req.obs)) != (self.ns, req.nt, self.nr):
+            raise ValueError("obs has shape %s, expected %s" % (np.shape(req.obs), (self.ns, req.nt, self.nr)))
+        self.nt, self.dt, self.dx, self.f0, self.nabc = int(req.nt), float(req.dt), float(req.dx), float(req.f0), \
+            int(req.nabc)
+        self.silent_rel = float(silent_rel)
+        self.key = _shape_key(req, self.grad, snapshot_precision, per_request_budget, silent_rel)
         self.plan = AcousticPlan(nz=self.nz, nx=self.nx, nabc=req.nabc, free_surface=req.free_surface,
                                  src_z=req.src_z, src_x=req.src_x, rcv_z=req.rcv_z, rcv_x=req.rcv_x, nt=req.nt,
                                  dt=req.dt, dtype=torch.float32, snapshot_precision=snapshot_precision,
                                  memory_budget=per_request_budget)
         self.ws_bytes = self.plan.workspace_bytes(self.grad)
         self.nzp, self.nxp = self.plan.grid_shape()
-        rec = self.ns * req.nt * self.nr * 4
+        rec = self.ns * self.nt * self.nr * 4
         grid = self.nzp * self.nxp * 4
         self.nbytes = (_aligned(self.ws_bytes) + 3 * _aligned(rec) + (2 * _aligned(rec) if self.grad else 0)
-                       + 4 * _aligned(grid) + 4 * _aligned(self.nz * self.nx * 4) + _aligned(self.ns * req.nt * 4))
-        self.cells = self.ns * self.nzp * self.nxp * req.nt
+                       + 3 * _aligned(grid) + 5 * _aligned(self.nz * self.nx * 4) + _aligned(self.ns * self.nt * 4))
+        self.cells = self.ns * self.nzp * self.nxp * self.nt
+        self.off = self.n = None
+        self.bound = False
+        self.graph = None
+        self.uses = 0
 
-    def run(self, arena, off, n, stream, device):
-        """Enqueue the whole solve on ``stream`` inside the arena range [off, off + n) and
-        wait for it. Returns (loss, grad, records)."""
-        r = self.req
-        cv = _Carver(arena, off, off + n)
-        ws = cv.take((self.ws_bytes,), torch.uint8)
-        shp = (self.ns, r.nt, self.nr)
-        recs = tuple(cv.take(shp, torch.float32) for _ in range(3))
-        a1, a2, damp, ga_buf = (cv.take((self.nzp, self.nxp), torch.float32) for _ in range(4))
-        fw = tuple(cv.take((self.nz, self.nx), torch.float32) for _ in range(3))
-        vp_d = cv.take((self.nz, self.nx), torch.float32)
-        wav = cv.take((self.ns, r.nt), torch.float32)
-        h = stream.cuda_stream
+    # -- arena buffers and the shape's constant data (once per arena range)
+    def _bind(self, arena, device):
+        cv = _Carver(arena, self.off, self.off + self.n)
+        shp = (self.ns, self.nt, self.nr)
+        self.ws = cv.take((self.ws_bytes,), torch.uint8)
+        self.recs = tuple(cv.take(shp, torch.float32) for _ in range(3))
+        self.a1, self.a2, self.damp = (cv.take((self.nzp, self.nxp), torch.float32) for _ in range(3))
+        self.fw = tuple(cv.take((self.nz, self.nx), torch.float32) for _ in range(3))
+        self.vp_d = cv.take((self.nz, self.nx), torch.float32)
+        self.rho_d = cv.take((self.nz, self.nx), torch.float32)
+        self.wav = cv.take((self.ns, self.nt), torch.float32)
+        if self.grad:
+            self.obs = cv.take(shp, torch.float32)
+            self.adj = cv.take(shp, torch.float32)
+        _, w = _wavelet(self.nt, self.dt, self.f0)
+        self.wav.copy_(torch.from_numpy(np.ascontiguousarray(np.tile(w, (self.ns, 1)), dtype=np.float32)))
+        self.bound = True
+
+    def _load(self, req):
+        """Copy this request's model, its Gardner density (310 vp^0.25, evaluated on the host in
+        float32 as AcousticModel.forward does) and its observed data into the fixed buffers."""
+        vp = np.ascontiguousarray(req.vp, dtype=np.float32)
+        self.vp_d.copy_(torch.from_numpy(vp))
+        self.rho_d.copy_(torch.from_numpy(np.power(vp, 0.25) * 310))
+        self.damp.copy_(torch.from_numpy(np.ascontiguousarray(
+            bc_pml(self.nx, self.nz, self.dx, self.dx, self.nabc, vp.max(), free_surface=False), dtype=np.float32)))
+        if self.grad:
+            self.obs.copy_(torch.from_numpy(np.ascontiguousarray(req.obs, dtype=np.float32)))
+
+    def _enqueue(self, h):
+        """The whole solve on the current stream (handle h): device work only, no host sync."""
+        nb = self.nabc
+        c, den = _pad(self.vp_d, nb), _pad(self.rho_d, nb)
+        t1 = den * c
+        self.a1.copy_(t1 * c * self.dt / self.dx)
+        self.a2.copy_(self.dt / (den * self.dx))
+        self.plan.run_forward(self.a1, self.a2, self.damp, self.wav, self.grad, workspace=self.ws, records=self.recs,
+                              fw=self.fw, stream=h)
+        if not self.grad:
+            return
+        self.out_loss, _ = l2_misfit_and_adjoint(self.recs[0], self.obs, self.dt, silent_rel=self.silent_rel, stream=h,
+                                                 adj=self.adj)
+        ga1, _ = self.plan.run_backward(self.a1, self.a2, self.damp, self.wav, (self.adj, None, None), self.ws,
+                                        stream=h)
+        # alpha1 = ((den c) c) dt / dx; alpha2 and rho do not depend on vp
+        g_t2 = ga1 * (self.dt / self.dx)
+        self.out_grad = fold_replicate_pad(g_t2 * t1 + g_t2 * c * den, nb)
+
+    def run(self, req, arena, stream, capture_stream, device, use_graphs):
+        """Solve ``req`` in this shape's arena range and wait for it; returns (loss, grad, records)."""
+        if not self.bound:
+            self._bind(arena, device)
         with torch.cuda.stream(stream):
-            vp = np.ascontiguousarray(r.vp, dtype=np.float32)
-            vp_d.copy_(torch.from_numpy(vp))
-            rho = torch.from_numpy(np.power(vp, 0.25) * 310).to(device)
-            damp.copy_(torch.from_numpy(np.ascontiguousarray(
-                bc_pml(self.nx, self.nz, r.dx, r.dx, r.nabc, vp.max(), free_surface=False), dtype=np.float32)))
-            _, w = _wavelet(r.nt, r.dt, r.f0)
-            wav.copy_(torch.from_numpy(np.ascontiguousarray(np.tile(w, (self.ns, 1)), dtype=np.float32)))
-            nb = r.nabc
-            c, den = _pad(vp_d, nb), _pad(rho, nb)
-            t1 = den * c
-            a1.copy_(t1 * c * r.dt / r.dx)
-            a2.copy_(r.dt / (den * r.dx))
-            self.plan.run_forward(a1, a2, damp, wav, self.grad, workspace=ws, records=recs, fw=fw, stream=h)
-            if not self.grad:
-                out = recs[0].cpu()
-                code = self.plan.status(ws, False, stream=h)
-                if code != 0:
-                    raise RuntimeError("solve %d: a pipeline wait timed out on the GPU (status %d)" % (r.rid, code))
-                return None, None, out.numpy()
-            obs = cv.take(shp, torch.float32)
-            obs.copy_(torch.from_numpy(np.ascontiguousarray(r.obs, dtype=np.float32)))
-            loss, adj = l2_misfit_and_adjoint(recs[0], obs, r.dt, silent_rel=self.silent_rel, stream=h,
-                                              adj=cv.take(shp, torch.float32))
-            ga1, _ = self.plan.run_backward(a1, a2, damp, wav, (adj, None, None), ws, stream=h)
-            code = self.plan.status(ws, True, stream=h)
+            self._load(req)
+        if use_graphs and self.graph is None and self.uses >= 1:
+            # second solve of this shape: capture the device-side solve once, replay it from now on
+            capture_stream.wait_stream(stream)
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.stream(capture_stream):
+                g.capture_begin(capture_error_mode="thread_local")
+                try:
+                    self._enqueue(capture_stream.cuda_stream)
+                finally:
+                    g.capture_end()
+            self.graph = g
+            stream.wait_stream(capture_stream)
+        with torch.cuda.stream(stream):
+            if self.graph is not None:
+                self.graph.replay()
+            else:
+                self._enqueue(stream.cuda_stream)
+            code = self.plan.status(self.ws, self.grad, stream=stream.cuda_stream)
             if code != 0:
-                raise RuntimeError("solve %d: a pipeline wait timed out on the GPU (status %d)" % (r.rid, code))
-            # alpha1 = ((den c) c) dt / dx; alpha2 and rho do not depend on vp
-            g_t2 = ga1 * (r.dt / r.dx)
-            torch.add(g_t2 * t1, g_t2 * c * den, out=ga_buf)
-            grad = fold_replicate_pad(ga_buf, nb).cpu().numpy()
-            return float(loss.cpu()), grad, None
+                raise RuntimeError("solve %d: a pipeline wait timed out on the GPU (status %d)" % (req.rid, code))
+            self.uses += 1
+            if not self.grad:
+                return None, None, self.recs[0].cpu().numpy()
+            return float(self.out_loss.cpu()), self.out_grad.cpu().numpy(), None
 
 
 # ------------------------------------------------------------------------------------------
 # server
 # ------------------------------------------------------------------------------------------
 class SolveServer(object):
-    """Admit, overlap and complete solves under an HBM budget (module docstring)."""
+    """Admit, overlap and complete solves under an HBM budget (module docstring).
+
+    ``graphs``: keep each solved shape (plan, arena range, buffers) after its request completes
+    and capture the device-side solve in a CUDA graph at its second use; later requests of the
+    same shape copy in their model and data and replay the graph. Idle shapes keep their arena
+    ranges until admission needs the room (least recently used first)."""
 
     def __init__(self, device="cuda:0", hbm_budget=150 << 30, slots=4, snapshot_precision="bf16",
-                 per_request_budget=None, max_wait_s=2.0, reserve=None, silent_rel=1e-6):
+                 per_request_budget=None, max_wait_s=2.0, reserve=None, silent_rel=1e-6, graphs=True):
         if not torch.cuda.is_available():
             raise RuntimeError("SolveServer needs a CUDA device (adfwi_gb300 has no CPU implementation)")
         self.device = torch.device(device)
@@ -347,16 +406,20 @@ class SolveServer(object):
                                       else max(1 << 30, self.book.capacity // max(1, self.slots)))
         self.max_wait_s = float(max_wait_s)
         self.silent_rel = float(silent_rel)
+        self.graphs = bool(graphs)
         self._cv = threading.Condition()
-        self._queue = []      # (t_arrival, solve, future), arrival order
-        self._ready = []      # (t_arrival, solve, future, t_admit, off, n)
+        self._queue = []      # (t_arrival, (shape, request), future), arrival order
+        self._ready = []      # (t_arrival, shape, request, future, t_admit)
+        self._idle = collections.OrderedDict()  # id(shape) -> shape, least recently used first
         self._running = 0
         self._closed = False
         self._next_id = 0
         self.completed: List[SolveResult] = []
         self.failed = 0
         self.peak_running = 0
+        self.graph_replays = 0
         self._streams = [torch.cuda.Stream(device=self.device) for _ in range(self.slots)]
+        self._capture_streams = [torch.cuda.Stream(device=self.device) for _ in range(self.slots)]
         self._workers = [threading.Thread(target=self._worker, args=(k,), daemon=True, name="adfwi-solve-%d" % k)
                          for k in range(self.slots)]
         for w in self._workers:
@@ -368,13 +431,13 @@ class SolveServer(object):
         fut = Future()
         t = time.perf_counter() if t_arrival is None else t_arrival
         try:
-            solve = _Solve(req, self.snapshot_precision, self.per_request_budget, self.silent_rel)
+            shape = _Shape(req, self.snapshot_precision, self.per_request_budget, self.silent_rel)
         except Exception as e:
             fut.set_exception(e)
             return fut
-        if solve.nbytes > self.book.capacity:
+        if shape.nbytes > self.book.capacity:
             fut.set_exception(MemoryError("request %d needs %d bytes of device memory, more than the %d-byte arena"
-                                          % (req.rid, solve.nbytes, self.book.capacity)))
+                                          % (req.rid, shape.nbytes, self.book.capacity)))
             return fut
         with self._cv:
             if self._closed:
@@ -382,7 +445,7 @@ class SolveServer(object):
             if req.rid < 0:
                 req.rid = self._next_id
             self._next_id += 1
-            self._queue.append((t, solve, fut))
+            self._queue.append((t, (shape, req), fut))
             self._admit_locked()
             self._cv.notify_all()
         return fut
@@ -394,6 +457,10 @@ class SolveServer(object):
         if wait:
             for w in self._workers:
                 w.join()
+        with self._cv:
+            for shape in list(self._idle.values()):
+                self.book.free(shape.off, shape.n)
+            self._idle.clear()
 
     def __enter__(self):
         return self
@@ -405,6 +472,7 @@ class SolveServer(object):
         with self._cv:
             self.completed = []
             self.failed = 0
+            self.graph_replays = 0
             self.peak_running = self._running
             self.book.peak = self.book.used
 
@@ -419,17 +487,50 @@ class SolveServer(object):
         return {"requests": len(done), "failed": self.failed, "p50_s": float(np.percentile(lat, 50)),
                 "p99_s": float(np.percentile(lat, 99)), "mean_s": float(lat.mean()), "makespan_s": t1 - t0,
                 "gcell_per_s": cells / (t1 - t0) / 1e9, "peak_arena_bytes": self.book.peak,
-                "arena_bytes": self.book.capacity, "peak_concurrency": self.peak_running}
+                "arena_bytes": self.book.capacity, "peak_concurrency": self.peak_running,
+                "graph_replays": self.graph_replays}
 
     # -------------------------------------------------------------- scheduling
+    def _take_idle(self, key):
+        for sid, shape in self._idle.items():
+            if shape.key == key:
+                del self._idle[sid]
+                return shape
+        return None
+
+    def _alloc_evicting(self, nbytes):
+        got = self.book.alloc(nbytes)
+        while got is None and self._idle:
+            _, old = self._idle.popitem(last=False)  # least recently used idle shape
+            self.book.free(old.off, old.n)
+            got = self.book.alloc(nbytes)
+        return got
+
     def _admit_locked(self):
         now = time.perf_counter()
         free = self.slots - self._running - len(self._ready)
-        for (t, solve, fut), off, n in admit(self._queue, self.book, free, now, self.max_wait_s):
-            self._ready.append((t, solve, fut, now, off, n))
+        q = self._queue
+        strict = bool(q) and now - q[0][0] > self.max_wait_s
+        i = 0
+        while i < len(q) and free > 0:
+            t, (shape, req), fut = q[i]
+            cached = self._take_idle(shape.key)
+            if cached is not None:
+                shape = cached
+            else:
+                got = self._alloc_evicting(shape.nbytes)
+                if got is None:
+                    if strict:
+                        break  # the oldest request has waited too long: nothing may pass it
+                    i += 1
+                    continue
+                shape.off, shape.n = got
+            del q[i]
+            self._ready.append((t, shape, req, fut, now))
+            free -= 1
 
     def _worker(self, k):
-        stream = self._streams[k]
+        stream, cstream = self._streams[k], self._capture_streams[k]
         while True:
             with self._cv:
                 while True:
@@ -439,14 +540,15 @@ class SolveServer(object):
                     if self._closed and not self._queue:
                         return
                     self._cv.wait(timeout=0.05)
-                t_arr, solve, fut, t_admit, off, n = self._ready.pop(0)
+                t_arr, shape, req, fut, t_admit = self._ready.pop(0)
                 self._running += 1
                 self.peak_running = max(self.peak_running, self._running)
             res = err = None
+            replayed = shape.graph is not None
             try:
-                loss, grad, rec = solve.run(self.arena, off, n, stream, self.device)
-                res = SolveResult(solve.req.rid, loss, grad, rec, t_arr, t_admit, time.perf_counter(), solve.cells,
-                                  n, solve.plan.snapshot_every)
+                loss, grad, rec = shape.run(req, self.arena, stream, cstream, self.device, self.graphs)
+                res = SolveResult(req.rid, loss, grad, rec, t_arr, t_admit, time.perf_counter(), shape.cells,
+                                  shape.n, shape.plan.snapshot_every)
             except Exception as e:  # the others keep running; the future carries the error
                 err = e
             try:
@@ -455,9 +557,13 @@ class SolveServer(object):
                 err = err or e
             with self._cv:
                 self._running -= 1
-                self.book.free(off, n)
+                if self.graphs and err is None:
+                    self._idle[id(shape)] = shape  # keep the shape (and its graph) for the next request like it
+                else:
+                    self.book.free(shape.off, shape.n)
                 if res is not None and err is None:
                     self.completed.append(res)
+                    self.graph_replays += int(replayed)
                 else:
                     self.failed += 1
                 self._admit_locked()

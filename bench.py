@@ -303,7 +303,8 @@ def serving_arm(args, dev):
         out[name] = {"p50_s": round(st["p50_s"], 4), "p99_s": round(st["p99_s"], 4), "mean_s": round(st["mean_s"], 4),
                      "throughput_gcell_per_s": round(st["gcell_per_s"], 3),
                      "requests_per_s": round(st["requests"] / st["makespan_s"], 3), "slots": slots,
-                     "peak_concurrency": st["peak_concurrency"], "peak_arena_gb": round(st["peak_arena_bytes"] / 2 ** 30, 2)}
+                     "peak_concurrency": st["peak_concurrency"], "peak_arena_gb": round(st["peak_arena_bytes"] / 2 ** 30, 2),
+                     "graph_replays": st["graph_replays"]}
     same = all(a.loss == b.loss and np.array_equal(a.grad, b.grad)
                for a, b in zip(results["served"], results["one_at_a_time"]))
     out.update({"requests": len(timed), "arrival_rate_per_s": args.serve_rate, "hbm_budget_gb": budget / 2 ** 30,

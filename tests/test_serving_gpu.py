@@ -101,7 +101,7 @@ def test_admission_keeps_to_the_budget(native_lib):
     req, vp_true = _request(7, 48, 80, 2, 300)
     with S.SolveServer(hbm_budget=1 << 30, slots=1) as srv:
         _with_obs(srv, req, vp_true)
-    need = S._Solve(req, "bf16", 64 << 20).nbytes
+    need = S._Shape(req, "bf16", 64 << 20, 1e-6).nbytes
     # room for one solve at a time: the second waits for the first to free its range
     with S.SolveServer(hbm_budget=int(need * 1.5), reserve=0, slots=2, per_request_budget=64 << 20) as srv:
         futs = [srv.submit(req) for _ in range(3)]
@@ -117,3 +117,38 @@ def test_admission_keeps_to_the_budget(native_lib):
                              src_x=np.array([10 ** 6]), rcv_z=req.rcv_z, rcv_x=req.rcv_x, nabc=req.nabc)
         with pytest.raises(RuntimeError):
             srv.submit(bad).result()
+
+
+def test_graph_replays_equal_eager_solves_and_take_new_models(native_lib):
+    """The second solve of a shape is captured in a CUDA graph and replayed; replays with other
+    models of the same shape give exactly the eager results."""
+    req_a, vp_true = _request(21, 48, 80, 2, 300)
+    with S.SolveServer(hbm_budget=1 << 30, slots=1, graphs=False) as srv:
+        _with_obs(srv, req_a, vp_true)
+        req_b = S.SolveRequest(**{**req_a.__dict__, "vp": (req_a.vp * 1.03).astype(np.float32), "rid": 99})
+        eager = [srv.submit(r).result() for r in (req_a, req_b, req_a)]
+    with S.SolveServer(hbm_budget=1 << 30, slots=1, graphs=True) as srv:
+        served = [srv.submit(r).result() for r in (req_a, req_b, req_a, req_b)]
+        st = srv.stats()
+    assert st["graph_replays"] >= 2
+    for e, g in zip(eager + [eager[1]], served):
+        assert e.loss == g.loss and np.array_equal(e.grad, g.grad)
+    assert not np.array_equal(served[0].grad, served[1].grad)
+
+
+def test_idle_shapes_are_evicted_for_room(native_lib):
+    """Two shapes that do not fit together: each admission evicts the other's idle range."""
+    ra, va = _request(31, 48, 80, 2, 300)
+    rb, vb = _request(32, 56, 72, 3, 280)
+    with S.SolveServer(hbm_budget=1 << 30, slots=1) as srv:
+        _with_obs(srv, ra, va)
+        _with_obs(srv, rb, vb)
+    need = max(S._Shape(r, "bf16", 64 << 20, 1e-6).nbytes for r in (ra, rb))
+    with S.SolveServer(hbm_budget=int(need * 1.5), reserve=0, slots=1, per_request_budget=64 << 20,
+                       graphs=False) as srv:
+        ref = [srv.submit(r).result() for r in (ra, rb)]
+    with S.SolveServer(hbm_budget=int(need * 1.5), reserve=0, slots=1, per_request_budget=64 << 20) as srv:
+        got = [srv.submit(r).result() for r in (ra, rb, ra, rb)]
+        assert srv.stats()["peak_arena_bytes"] <= srv.book.capacity
+    for e, g in zip(ref + ref, got):
+        assert e.loss == g.loss and np.array_equal(e.grad, g.grad)

@@ -264,6 +264,140 @@ __global__ void vel_tot_pml(Geo<T> g, const T* __restrict__ vs, T* __restrict__ 
   v[VZ * NSP + o] = vz;
 }
 
+// ---- fused forms: the split update of a cell and its totals in one pass; the rows whose
+// totals read other rows (free surface) are left to the *_fs_rows kernels that follow.
+template <typename T>
+__device__ __forceinline__ bool stress_fs_row(const Geo<T>& g, int i) {
+  return g.fsurf && i >= g.h - 3 && i <= g.h - 1;
+}
+template <typename T>
+__device__ __forceinline__ bool vel_fs_row(const Geo<T>& g, int i, int j) {
+  return g.fsurf && j >= g.jlo && j <= g.jhi && (i == g.h - 2 || i == g.h - 3);
+}
+
+template <typename T, int NN>
+__global__ void stress_pml_tot(Geo<T> g, int it, const T* __restrict__ cf, const T* __restrict__ v,
+                               T* __restrict__ ts, T* __restrict__ tt, const T* __restrict__ wav) {
+  EL_CELL_SHOT
+  const int64_t occ = g.L.off(i, j);
+  T sp[6];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) sp[k] = ts[k * NSP + o];
+  if (in_I(g, i, j)) {
+    const T* vx = v;
+    const T* vz = v + NSP;
+    const T dxbm_vx = dxb<NN>(g, vx, o), dxbm_vz = dxb<NN>(g, vz, o);
+    const T dzbm_vx = dzb<NN>(g, vx, o), dzbm_vz = dzb<NN>(g, vz, o);
+    const T dxfm_vx = dxf<NN>(g, vx, o), dzfm_vx = dzf<NN>(g, vx, o);
+    const T dxfm_vz = dxf<NN>(g, vz, o), dzfm_vz = dzf<NN>(g, vz, o);
+    const T bcx = cf[BCX * PL + occ], bcz = cf[BCZ * PL + occ];
+    const T pxd = radd(T(1), rmul(g.hdt, bcx)), pxn = rsub(T(1), rmul(g.hdt, bcx));
+    const T pzd = radd(T(1), rmul(g.hdt, bcz)), pzn = rsub(T(1), rmul(g.hdt, bcz));
+    const T pxi = rdiv(T(1), pxd), pzi = rdiv(T(1), pzd);
+    const T c11 = cf[C11 * PL + occ], c13 = cf[C13 * PL + occ], c15 = cf[C15 * PL + occ];
+    const T c33 = cf[C33 * PL + occ], c35 = cf[C35 * PL + occ], c55 = cf[C55 * PL + occ];
+    sp[TXX_X] = rmul(radd(rmul(pxn, sp[TXX_X]), rmul(g.dt_dx, radd(rmul(c11, dxbm_vx), rmul(c15, dxbm_vz)))), pxi);
+    sp[TXX_Z] = rmul(radd(rmul(pzn, sp[TXX_Z]), rmul(g.dt_dz, radd(rmul(c15, dzbm_vx), rmul(c13, dzbm_vz)))), pzi);
+    sp[TZZ_X] = rmul(radd(rmul(pxn, sp[TZZ_X]), rmul(g.dt_dx, radd(rmul(c13, dxbm_vx), rmul(c35, dxbm_vz)))), pxi);
+    sp[TZZ_Z] = rmul(radd(rmul(pzn, sp[TZZ_Z]), rmul(g.dt_dz, radd(rmul(c35, dzbm_vx), rmul(c33, dzbm_vz)))), pzi);
+    sp[TXZ_X] = rmul(radd(rmul(pxn, sp[TXZ_X]), rmul(g.dt_dx, radd(rmul(c15, dxfm_vx), rmul(c55, dxfm_vz)))), pxi);
+    sp[TXZ_Z] = rmul(radd(rmul(pzn, sp[TXZ_Z]), rmul(g.dt_dz, radd(rmul(c55, dzfm_vx), rmul(c35, dzfm_vz)))), pzi);
+  }
+  if (i == g.src_z[s] && j == g.src_x[s]) {
+    const T w = wav[(int64_t)s * g.nt + it];
+    const T axx = rmul(g.src_m[3 * s + 0], w), azz = rmul(g.src_m[3 * s + 1], w), axz = rmul(g.src_m[3 * s + 2], w);
+    sp[TXX_X] = radd(sp[TXX_X], axx);
+    sp[TXX_Z] = radd(sp[TXX_Z], axx);
+    sp[TZZ_X] = radd(sp[TZZ_X], azz);
+    sp[TZZ_Z] = radd(sp[TZZ_Z], azz);
+    sp[TXZ_X] = radd(sp[TXZ_X], axz);
+    sp[TXZ_Z] = radd(sp[TXZ_Z], axz);
+  }
+#pragma unroll
+  for (int k = 0; k < 6; ++k) ts[k * NSP + o] = sp[k];
+  if (!stress_fs_row(g, i)) {
+    tt[TXX * NSP + o] = radd(sp[TXX_X], sp[TXX_Z]);
+    tt[TZZ * NSP + o] = radd(sp[TZZ_X], sp[TZZ_Z]);
+    tt[TXZ * NSP + o] = radd(sp[TXZ_X], sp[TXZ_Z]);
+  }
+}
+
+// Stress totals of the free-surface rows h-3 .. h-1 (elastic_kernels.py:375-384).
+template <typename T>
+__global__ void stress_fs_rows_pml(Geo<T> g, const T* __restrict__ ts, T* __restrict__ tt) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= g.L.nxp) return;
+  const int i = g.h - 3 + (int)blockIdx.z, s = blockIdx.y;
+  const int64_t PL = g.L.plane, NSP = (int64_t)g.ns * PL, P = g.L.pitch;
+  const int64_t o = (int64_t)s * PL + g.L.off(i, j);
+  auto sum = [&](int f, int64_t oo) { return radd(ts[(2 * f) * NSP + oo], ts[(2 * f + 1) * NSP + oo]); };
+  T xx = sum(TXX, o), zz = sum(TZZ, o), xz = sum(TXZ, o);
+  const int h = g.h;
+  if (i == h - 1) zz = T(0);
+  if (i == h - 2) zz = -sum(TZZ, o + 2 * P);
+  if (i == h - 2) xz = -sum(TXZ, o + P);
+  if (i == h - 3) xz = -sum(TXZ, o + 3 * P);
+  tt[TXX * NSP + o] = xx;
+  tt[TZZ * NSP + o] = zz;
+  tt[TXZ * NSP + o] = xz;
+}
+
+template <typename T, int NN>
+__global__ void vel_pml_tot(Geo<T> g, const T* __restrict__ cf, const T* __restrict__ tt, T* __restrict__ vs,
+                            T* __restrict__ v) {
+  EL_CELL_SHOT
+  T sv[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) sv[k] = vs[k * NSP + o];
+  if (in_I(g, i, j)) {
+    const int64_t occ = g.L.off(i, j);
+    const T dxfm_txx = dxf<NN>(g, tt + TXX * NSP, o);
+    const T dzbm_txz = dzb<NN>(g, tt + TXZ * NSP, o);
+    const T dxbm_txz = dxb<NN>(g, tt + TXZ * NSP, o);
+    const T dzfm_tzz = dzf<NN>(g, tt + TZZ * NSP, o);
+    const T bcx = cf[BCX * PL + occ], bcz = cf[BCZ * PL + occ];
+    const T pxd = radd(T(1), rmul(g.hdt, bcx)), pxn = rsub(T(1), rmul(g.hdt, bcx));
+    const T pzd = radd(T(1), rmul(g.hdt, bcz)), pzn = rsub(T(1), rmul(g.hdt, bcz));
+    const T bx = cf[BX * PL + occ], bz = cf[BZ * PL + occ];
+    const T dbx = rmul(g.dt, bx), dbz = rmul(g.dt, bz);
+    sv[VX_X] = rdiv(radd(rmul(pxn, sv[VX_X]), rdiv(rmul(dbx, dxfm_txx), g.dx)), pxd);
+    sv[VX_Z] = rdiv(radd(rmul(pzn, sv[VX_Z]), rdiv(rmul(dbx, dzbm_txz), g.dz)), pzd);
+    sv[VZ_X] = rdiv(radd(rmul(pxn, sv[VZ_X]), rdiv(rmul(dbz, dxbm_txz), g.dx)), pxd);
+    sv[VZ_Z] = rdiv(radd(rmul(pzn, sv[VZ_Z]), rdiv(rmul(dbz, dzfm_tzz), g.dz)), pzd);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) vs[k * NSP + o] = sv[k];
+  }
+  if (!vel_fs_row(g, i, j)) {
+    v[VX * NSP + o] = radd(sv[VX_X], sv[VX_Z]);
+    v[VZ * NSP + o] = radd(sv[VZ_X], sv[VZ_Z]);
+  }
+}
+
+// Velocity totals of the free-surface rows h-3, h-2 (elastic_kernels.py:395-402), from the
+// split velocities of all rows.
+template <typename T>
+__global__ void vel_fs_rows_pml(Geo<T> g, const T* __restrict__ vs, T* __restrict__ v) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < g.jlo || j > g.jhi || j >= g.L.nxp) return;
+  const int i = g.h - 3 + (int)blockIdx.z, s = blockIdx.y;
+  const int64_t PL = g.L.plane, NSP = (int64_t)g.ns * PL, P = g.L.pitch;
+  const int64_t o = (int64_t)s * PL + g.L.off(i, j);
+  auto vxs = [&](int64_t oo) { return radd(vs[VX_X * NSP + oo], vs[VX_Z * NSP + oo]); };
+  auto vzs = [&](int64_t oo) { return radd(vs[VZ_X * NSP + oo], vs[VZ_Z * NSP + oo]); };
+  T vx = vxs(o), vz = vzs(o);
+  const int h = g.h;
+  if (i == h - 2) {
+    const T vz_up = vzs(o + P);
+    const T vzn_r = (j + 1 <= g.jhi) ? vzs(o + P + 1) : vzs(o + 1);
+    vz = vz_up;
+    vx = radd(rsub(radd(rsub(vzn_r, vz_up), vzs(o + P + 1)), vz_up), vxs(o + 2 * P));
+  } else {
+    vz = vzs(o + 2 * P);
+  }
+  v[VX * NSP + o] = vx;
+  v[VZ * NSP + o] = vz;
+}
+
 // ======================================================================= forward, absorbing layer
 template <typename T, int NN>
 __global__ void stress_abl(Geo<T> g, int it, const T* __restrict__ cf, const T* __restrict__ v, T* __restrict__ ts,
@@ -666,6 +800,97 @@ __global__ void adj_vq(Geo<T> g, const T* __restrict__ cf, const T* __restrict__
   for (int k = 0; k < 8; ++k) q8[k * NSP + o] = v[k];
 }
 
+// (B4 + B3q) fused per cell and shot: the split velocities' lambda after the step (adj_vfs_pml)
+// and, from those new values, the velocity update's adjoint sources (adj_tq, PML form).
+template <typename T>
+__global__ void adj_vfs_tq_pml(Geo<T> g, const T* __restrict__ cf, const T* __restrict__ lv, T* lvs,
+                               T* __restrict__ q4) {
+  EL_CELL_SHOT
+  T ax, az;
+  vfs_adjoint(g, lv + VX * NSP, lv + VZ * NSP, i, j, o, ax, az);
+  const bool inside = in_I(g, i, j);
+  const int64_t c0 = g.L.off(i, j);
+  T sx = T(1), sz = T(1);
+  Pml<T> p;
+  if (inside) {
+    p = pml_at(g, cf, c0, PL);
+    sx = p.xn / p.xd;
+    sz = p.zn / p.zd;
+  }
+  const T vxx = sx * lvs[VX_X * NSP + o] + ax, vxz = sz * lvs[VX_Z * NSP + o] + ax;
+  const T vzx = sx * lvs[VZ_X * NSP + o] + az, vzz = sz * lvs[VZ_Z * NSP + o] + az;
+  lvs[VX_X * NSP + o] = vxx;
+  lvs[VX_Z * NSP + o] = vxz;
+  lvs[VZ_X * NSP + o] = vzx;
+  lvs[VZ_Z * NSP + o] = vzz;
+  T a = T(0), b = T(0), c = T(0), d = T(0);
+  if (inside) {
+    const T bx = cf[BX * PL + c0], bz = cf[BZ * PL + c0];
+    a = vxx * (g.dt * bx) / (g.dx * p.xd);
+    b = vxz * (g.dt * bx) / (g.dz * p.zd);
+    c = vzx * (g.dt * bz) / (g.dx * p.xd);
+    d = vzz * (g.dt * bz) / (g.dz * p.zd);
+  }
+  q4[0 * NSP + o] = a;
+  q4[1 * NSP + o] = b;
+  q4[2 * NSP + o] = c;
+  q4[3 * NSP + o] = d;
+}
+
+// (B2 + B1q) fused per cell and shot: the split stresses' lambda (adj_tfs_pml) and, from those
+// new values, the stress update's adjoint sources for the velocity transposes (adj_vq, PML).
+template <typename T>
+__global__ void adj_tfs_vq_pml(Geo<T> g, const T* __restrict__ cf, const T* __restrict__ lt, T* lts,
+                               T* __restrict__ q8) {
+  EL_CELL_SHOT
+  T azz, axz;
+  tfs_adjoint(g, lt + TZZ * NSP, lt + TXZ * NSP, i, o, azz, axz);
+  const T axx = lt[TXX * NSP + o];
+  const bool inside = in_I(g, i, j);
+  const int64_t c0 = g.L.off(i, j);
+  T sx = T(1), sz = T(1);
+  Pml<T> p;
+  if (inside) {
+    p = pml_at(g, cf, c0, PL);
+    sx = p.xn / p.xd;
+    sz = p.zn / p.zd;
+  }
+  T ls[6];
+  ls[0] = sx * lts[TXX_X * NSP + o] + axx;
+  ls[1] = sz * lts[TXX_Z * NSP + o] + axx;
+  ls[2] = sx * lts[TZZ_X * NSP + o] + azz;
+  ls[3] = sz * lts[TZZ_Z * NSP + o] + azz;
+  ls[4] = sx * lts[TXZ_X * NSP + o] + axz;
+  ls[5] = sz * lts[TXZ_Z * NSP + o] + axz;
+#pragma unroll
+  for (int k = 0; k < 6; ++k) lts[k * NSP + o] = ls[k];
+  T v[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) v[k] = T(0);
+  if (inside) {
+    const T kx = g.dt_dx / p.xd, kz = g.dt_dz / p.zd;
+    StressQ<T> r;
+    r.a = ls[0] * kx;
+    r.b = ls[1] * kz;
+    r.c = ls[2] * kx;
+    r.d = ls[3] * kz;
+    r.e = ls[4] * kx;
+    r.f = ls[5] * kz;
+    const T c11 = cf[C11 * PL + c0], c13 = cf[C13 * PL + c0], c15 = cf[C15 * PL + c0];
+    const T c33 = cf[C33 * PL + c0], c35 = cf[C35 * PL + c0], c55 = cf[C55 * PL + c0];
+    v[0] = c11 * r.a + c13 * r.c;
+    v[1] = c15 * r.b + c35 * r.d;
+    v[2] = c15 * r.e;
+    v[3] = c55 * r.f;
+    v[4] = c15 * r.a + c35 * r.c;
+    v[5] = c13 * r.b + c33 * r.d;
+    v[6] = c55 * r.e;
+    v[7] = c35 * r.f;
+  }
+#pragma unroll
+  for (int k = 0; k < 8; ++k) q8[k * NSP + o] = v[k];
+}
+
 // (B1a) lambda of the velocity totals at the start of the step (overwrite) and the C gradients.
 // pml = 1: split-field update; pml = 0: absorbing-layer update (lts then holds txx, tzz, txz,
 // and lv is accumulated instead of overwritten because v' = v + ...).
@@ -1015,10 +1240,16 @@ void estep(const adfwi_elastic_plan* p, const el::Geo<T>& g, int it, const T* cf
   if (p->d.pml) {
     T* ts = st;
     T* vs = st + 6 * NSP;
-    ADFWI_LAUNCH(kElFwdStep, s, (el::stress_pml<T, NN><<<gc, b, 0, s>>>(g, it, cf, vin, ts, wav)));
-    ADFWI_LAUNCH(kElFwdStep, s, (el::stress_tot_pml<T><<<gc, b, 0, s>>>(g, ts, tt)));
-    ADFWI_LAUNCH(kElFwdStep, s, (el::vel_pml<T, NN><<<gc, b, 0, s>>>(g, cf, tt, vs)));
-    ADFWI_LAUNCH(kElFwdStep, s, (el::vel_tot_pml<T><<<gc, b, 0, s>>>(g, vs, vout)));
+    ADFWI_LAUNCH(kElFwdStep, s, (el::stress_pml_tot<T, NN><<<gc, b, 0, s>>>(g, it, cf, vin, ts, tt, wav)));
+    if (p->d.free_surface) {
+      const dim3 gfs((unsigned)((p->nxp + 127) / 128), p->d.ns, 3);
+      ADFWI_LAUNCH(kElFwdStep, s, (el::stress_fs_rows_pml<T><<<gfs, 128, 0, s>>>(g, ts, tt)));
+    }
+    ADFWI_LAUNCH(kElFwdStep, s, (el::vel_pml_tot<T, NN><<<gc, b, 0, s>>>(g, cf, tt, vs, vout)));
+    if (p->d.free_surface) {
+      const dim3 gfs((unsigned)((p->nxp + 127) / 128), p->d.ns, 2);
+      ADFWI_LAUNCH(kElFwdStep, s, (el::vel_fs_rows_pml<T><<<gfs, 128, 0, s>>>(g, vs, vout)));
+    }
   } else {
     // ABL: stresses live in `tt`, velocities in place in vin (== vout)
     T* v = vout;
@@ -1188,12 +1419,10 @@ int ebackward(const adfwi_elastic_plan* p, const void* wavelet, const void* grec
       if (p->d.pml) {
         ADFWI_CUDA_TRY(cudaMemsetAsync(lt, 0, 3 * NSP * sizeof(T), s));
         if (gr) ADFWI_LAUNCH(kAux, s, (el::adj_inject<T><<<ginj, 128, 0, s>>>(g, it, gr, lt, lv, 1)));
-        ADFWI_LAUNCH(kElAdjStep, s, (el::adj_vfs_pml<T><<<gcs, b, 0, s>>>(g, cf, lv, lst + 6 * NSP)));
-        ADFWI_LAUNCH(kElAdjStep, s, (el::adj_tq<T, true><<<gcs, b, 0, s>>>(g, cf, lst + 6 * NSP, qsrc)));
+        ADFWI_LAUNCH(kElAdjStep, s, (el::adj_vfs_tq_pml<T><<<gcs, b, 0, s>>>(g, cf, lv, lst + 6 * NSP, qsrc)));
         ADFWI_LAUNCH(kElAdjStep, s, (el::adj_t_pml<T, NN><<<gcg, b, 0, s>>>(g, cf, lst + 6 * NSP, qsrc, lt, th, gcp,
                                                                             eg)));
-        ADFWI_LAUNCH(kElAdjStep, s, (el::adj_tfs_pml<T><<<gcs, b, 0, s>>>(g, cf, lt, lst)));
-        ADFWI_LAUNCH(kElAdjStep, s, (el::adj_vq<T, true><<<gcs, b, 0, s>>>(g, cf, lst, qsrc)));
+        ADFWI_LAUNCH(kElAdjStep, s, (el::adj_tfs_vq_pml<T><<<gcs, b, 0, s>>>(g, cf, lt, lst, qsrc)));
         ADFWI_LAUNCH(kElAdjStep, s, (el::adj_v<T, NN, true><<<gcg, b, 0, s>>>(g, cf, lst, qsrc, lv, vh, gcp, eg)));
       } else {
         if (gr) ADFWI_LAUNCH(kAux, s, (el::adj_inject<T><<<ginj, 128, 0, s>>>(g, it, gr, lst, lv, 1)));

@@ -1103,7 +1103,10 @@ int ncoef(const adfwi_elastic_plan* p) { return p->d.pml ? 10 : 9; }
 // 600 k), at most one group per shot.
 int egroups(const adfwi_elastic_plan* p) {
   const int64_t cells = (int64_t)p->nzp * p->nxp;
-  const int64_t want = (600000 + cells - 1) / cells;
+#ifndef ADFWI_EL_THREADS
+#define ADFWI_EL_THREADS 600000
+#endif
+  const int64_t want = ((int64_t)ADFWI_EL_THREADS + cells - 1) / cells;
   const int g = (int)std::max<int64_t>(1, std::min<int64_t>(p->d.ns, want));
   const int eg = (p->d.ns + g - 1) / g;
   return (p->d.ns + eg - 1) / eg;

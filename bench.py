@@ -323,7 +323,7 @@ def elastic_arm(args, dev):
     eps and delta through the hand-written adjoint)."""
     import adfwi_gb300 as A
     from adfwi_gb300.synthetic import vti_gradient_case
-    model, survey = vti_gradient_case(seed=0, device=str(dev))
+    model, survey = vti_gradient_case(seed=0, device=str(dev), nt=args.elastic_nt)
     prop = A.ElasticPropagator(model, survey, device=str(dev))
     nt, ns = prop.nt, prop.src_n
     gen = torch.Generator().manual_seed(0)
@@ -466,6 +466,9 @@ def main():
     ap.add_argument("--serve-rate", type=float, default=50.0, help="Poisson arrival rate of the served stream (1/s)")
     ap.add_argument("--serve-slots", type=int, default=4, help="concurrent solves of the server")
     ap.add_argument("--no-elastic", action="store_true", help="skip the VTI-elastic gradient measurement")
+    ap.add_argument("--elastic-only", action="store_true", help="run only the VTI-elastic gradient measurement")
+    ap.add_argument("--elastic-nt", type=int, default=2000,
+                    help="time steps of the elastic workload (2000 measured; fewer for profiling captures)")
     ap.add_argument("--precision", action="store_true",
                     help="run only the snapshot-precision study (BF16 / FP16 / FP32 checkpoints vs FP64)")
     ap.add_argument("--precision-nt", type=int, default=6000)
@@ -478,6 +481,11 @@ def main():
     if args.impl == "reference":
         if rank == 0:
             print(json.dumps(reference_arm(args)), flush=True)
+        return
+    if args.elastic_only:
+        if rank == 0:
+            torch.cuda.set_device(local)
+            print(json.dumps(elastic_arm(args, torch.device("cuda", local))), flush=True)
         return
     line = gpu_arm(args, world, rank, local)
     if world == 1 and not args.no_elastic:

@@ -105,3 +105,25 @@ def test_elastic_coefficient_gradient_matches_finite_differences_f64(abc_type):
         minus = float(loss([l - eps * d for l, d in zip(leaves, dirs)]))
     fd = (plus - minus) / (2 * eps)
     assert abs(fd - an) <= 1e-6 * abs(an), (fd, an)
+
+
+@pytest.mark.parametrize("precision,tol", [("bf16", 3e-2), ("fp16", 3e-3)])
+@pytest.mark.parametrize("abc_type", ["PML", "gerjan"])
+def test_elastic_low_precision_snapshots_stay_close(precision, tol, abc_type):
+    """BF16 / FP16 checkpoints (per-snapshot max-abs scale) change the elastic gradients by at
+    most a few parts in 1e2 / 1e3 of the native-snapshot gradients; the records not at all."""
+    grads, recs = {}, {}
+    for prec in ("native", precision):
+        model, survey, prop = elastic_problem(A, abc_type=abc_type, seed=17, snapshot_every=20,
+                                              snapshot_precision=prec)
+        rec = prop.forward(fd_order=4)
+        gen = torch.Generator().manual_seed(7)
+        w = {k: torch.randn(rec[k].shape, generator=gen) for k in ELASTIC_KEYS}
+        sum((rec[k] * w[k].cuda()).sum() for k in ELASTIC_KEYS).backward()
+        grads[prec] = {p: getattr(model, p).grad.detach().clone() for p in PARS}
+        recs[prec] = {k: rec[k].detach().clone() for k in ELASTIC_KEYS}
+    for k in ELASTIC_KEYS:
+        assert torch.equal(recs["native"][k], recs[precision][k])
+    for p in PARS:
+        err = rel(grads[precision][p], grads["native"][p])
+        assert err <= tol, (p, err)

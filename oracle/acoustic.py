@@ -15,6 +15,7 @@ Follows ``ADFWI/propagator/acoustic_kernels.py`` of the reference:
 Test infrastructure only: never imported by the product package.
 """
 import torch
+import torch.utils.checkpoint
 
 C1 = 9.0 / 8.0
 C2 = -1.0 / 24.0
@@ -76,7 +77,7 @@ def _step(p, u, w, it, co, src, rcv, fs, free_surface, dt, nabc, nz, nx):
 
 
 def acoustic_forward(vp, rho, damp, src_x, src_z, wavelet, rcv_x, rcv_z, *, nabc, free_surface,
-                     dx, dz, dt, checkpoint_segments=1, allow_gpu=False):
+                     dx, dz, dt, checkpoint_segments=1, allow_gpu=False, checkpoint_chunks=False):
     """Records of the reference acoustic propagator (acoustic_kernels.py:179-301).
 
     ``vp``, ``rho``: (nz, nx); ``damp``: (nz+2nabc, nx+2nabc); ``src_*``: int (ns,);
@@ -90,13 +91,15 @@ def acoustic_forward(vp, rho, damp, src_x, src_z, wavelet, rcv_x, rcv_z, *, nabc
     alpha2 = dt / (den * dz)
     return acoustic_forward_coef(alpha1, alpha2, damp, src_x, src_z, wavelet, rcv_x, rcv_z, nabc=nabc,
                                  free_surface=free_surface, dt=dt, checkpoint_segments=checkpoint_segments,
-                                 allow_gpu=allow_gpu)
+                                 allow_gpu=allow_gpu, checkpoint_chunks=checkpoint_chunks)
 
 
 def acoustic_forward_coef(alpha1, alpha2, damp, src_x, src_z, wavelet, rcv_x, rcv_z, *, nabc, free_surface, dt,
-                          checkpoint_segments=1, allow_gpu=False):
+                          checkpoint_segments=1, allow_gpu=False, checkpoint_chunks=False):
     """The time loop of acoustic_kernels.py:239-301 given alpha1 = rho c^2 dt/dz and
-    alpha2 = dt/(rho dz) on the padded grid (differentiable w.r.t. both)."""
+    alpha2 = dt/(rho dz) on the padded grid (differentiable w.r.t. both). ``checkpoint_chunks``
+    runs every chunk under torch.utils.checkpoint as the reference does (same values; the
+    backward recomputes the chunk), for timing the reference's memory-bounded mode."""
     _cpu_only(alpha1, alpha2, damp, wavelet, allow_gpu=allow_gpu)
     nzp, nxp = alpha1.shape
     nz, nx = nzp - 2 * nabc, nxp - 2 * nabc
@@ -121,25 +124,39 @@ def acoustic_forward_coef(alpha1, alpha2, damp, src_x, src_z, wavelet, rcv_x, rc
     fwp = torch.zeros((nz, nx), dtype=dtype, device=dev)
     fwu = torch.zeros((nz, nx), dtype=dtype, device=dev)
     fww = torch.zeros((nz, nx), dtype=dtype, device=dev)
-    recs = ([], [], [])
-    for chunk in torch.chunk(wavelet, checkpoint_segments, dim=-1):
+    def run_chunk(p, u, w, chunk, alpha1, alpha2):
+        cc = (alpha1, kappa1, alpha2, kappa2, kappa3)
+        rec_chunk = ([], [], [])
         seg_p = torch.zeros((nz, nx), dtype=dtype, device=dev)
         seg_u = torch.zeros((nz, nx), dtype=dtype, device=dev)
         seg_w = torch.zeros((nz, nx), dtype=dtype, device=dev)
         for it in range(chunk.shape[-1]):
-            p, u, w, rec, sq = _step(p, u, w, it, co, (sz, sx, chunk), (rz, rx), fs, free_surface,
+            p, u, w, rec, sq = _step(p, u, w, it, cc, (sz, sx, chunk), (rz, rx), fs, free_surface,
                                      dt, nabc, nz, nx)
-            for lst, r in zip(recs, rec):
+            for lst, r in zip(rec_chunk, rec):
                 lst.append(r)
             seg_p = seg_p + sq[0]
             seg_u = seg_u + sq[1]
             seg_w = seg_u + sq[2]
+        return (p, u, w) + tuple(torch.stack(lst, dim=1) for lst in rec_chunk) + (seg_p, seg_u, seg_w)
+
+    recs = ([], [], [])
+    for chunk in torch.chunk(wavelet, checkpoint_segments, dim=-1):
+        if checkpoint_chunks:
+            # the reference runs each chunk under torch.utils.checkpoint (acoustic_kernels.py:268-278)
+            res = torch.utils.checkpoint.checkpoint(run_chunk, p, u, w, chunk, alpha1, alpha2, use_reentrant=True)
+        else:
+            res = run_chunk(p, u, w, chunk, alpha1, alpha2)
+        p, u, w = res[:3]
+        for lst, r in zip(recs, res[3:6]):
+            lst.append(r)
+        seg_p, seg_u, seg_w = res[6:]
         fwp = fwp + seg_p
         fwu = fwp + seg_u
         fww = fwp + seg_w
     out = {}
     for key, lst in zip(("p", "u", "w"), recs):
-        out[key] = torch.stack(lst, dim=1)
+        out[key] = torch.cat(lst, dim=1)
     out["forward_wavefield_p"] = fwp
     out["forward_wavefield_u"] = fwu
     out["forward_wavefield_w"] = fww

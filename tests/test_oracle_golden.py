@@ -63,3 +63,24 @@ def test_oracle_refuses_gpu_tensors():
     if torch.cuda.is_available():
         with pytest.raises(RuntimeError):
             _cpu_only(t.cuda())
+
+
+@pytest.mark.parametrize("path", golden_files("acoustic")[:2], ids=lambda p: p.split("/")[-1])
+def test_oracle_checkpointed_chunks_match_reference(path):
+    """Running every chunk under torch.utils.checkpoint (the reference's memory-bounded mode)
+    gives the fixture's records bit for bit and its gradient to rounding."""
+    g = np.load(path)
+    dt_ = torch.float64 if str(g["dtype"]) == "f64" else torch.float32
+    vp = torch.tensor(g["vp"], dtype=dt_, requires_grad=True)
+    rho = torch.tensor(g["rho"], dtype=dt_, requires_grad=True)
+    out = acoustic_forward(vp, rho, torch.tensor(g["damp"]), g["src_x"], g["src_z"],
+                           torch.tensor(g["wavelet"], dtype=dt_), g["rcv_x"], g["rcv_z"],
+                           nabc=int(g["nabc"]), free_surface=bool(g["free_surface"]), dx=float(g["dx"]),
+                           dz=float(g["dx"]), dt=float(g["dt"]), checkpoint_segments=int(g["segments"]),
+                           checkpoint_chunks=True)
+    for k in out:
+        assert np.array_equal(out[k].detach().numpy(), g["rec_" + k]), k
+    loss = sum((out[k] * torch.tensor(g["w_" + k], dtype=dt_)).sum() for k in "puw")
+    loss.backward()
+    tol = 1e-12 if dt_ == torch.float64 else 1e-6
+    assert rel(vp.grad, g["grad_vp"]) < tol

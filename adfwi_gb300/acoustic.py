@@ -164,6 +164,9 @@ class AcousticSolve(torch.autograd.Function):
         damp = damp.contiguous()
         wavelet = wavelet.contiguous()
         need_grad = bool(ctx.needs_input_grad[0] or ctx.needs_input_grad[1])
+        # records the loss does not use reach backward as None (no zero-filled adjoint sources
+        # to allocate and inject)
+        ctx.set_materialize_grads(False)
         rp, ru, rw, fp, fu, fw, ws = plan.run_forward(alpha1, alpha2, damp, wavelet, need_grad)
         ctx.plan = plan
         ctx.ws = ws if need_grad else None

@@ -40,8 +40,10 @@ struct ItemHeader {
 struct SmemHeader {
   uint64_t full[MAXSTAGES];
   uint64_t empty[MAXSTAGES];
+  uint64_t stored[MAXSTAGES];  // consumers -> relay lanes: the item's outputs are in global memory
   int abort_flag;
 };
+static_assert(sizeof(SmemHeader) <= 512, "the item headers start 512 bytes into shared memory");
 
 __device__ __forceinline__ bool aborted(const SmemHeader* h) { return *(volatile const int*)&h->abort_flag != 0; }
 __device__ __forceinline__ void set_abort(SmemHeader* h, int* flag) {

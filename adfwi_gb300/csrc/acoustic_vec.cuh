@@ -19,7 +19,10 @@
 //              j0+66, j0+67 are computed but never read);
 //   tile pass  (256 threads): u and w after the step on the 16 x 64 tile (1 row x 4 columns
 //              per thread), the three stores and the illumination;
-//   receivers  (tiles holding receivers only): one warp gathers p, u, w.
+//   receivers  (tiles holding receivers only): the consumers arrive on the stage's `stored`
+//              mbarrier instead of `empty`, and the 31 idle lanes of the producer warp (the
+//              relay) gather p, u, w of the item from the global stores just made and release
+//              the stage, so a receiver tile costs the consumers nothing extra.
 // The operation order of every cell value is the reference's (acoustic_kernels.py:115-160),
 // with explicitly rounded arithmetic as in fwd_step_tma, so the records are bit-identical.
 #pragma once
@@ -97,11 +100,44 @@ struct VecFwdLayout {
   static constexpr int kW = round128(WZ * BOXX * (int)sizeof(T));
   static constexpr int kStage = 2 * kE + kW;  // U, W, P boxes
   static constexpr int kStageTx = (2 * EZ + WZ) * BOXX * (int)sizeof(T);
-  static constexpr int kSP = kE;                               // new p on the halo (box columns)
-  static constexpr int kSO = round128(TZ * TX * (int)sizeof(T));  // new u / w of a receiver tile
-  static constexpr int kGroup = 2 * kSP + 2 * kSO;
+  static constexpr int kSP = kE;  // new p on the halo (box columns)
+  static constexpr int kGroup = 2 * kSP;
   static int bytes(int stages) { return kVecSmemFixed + stages * kStage + kGroup; }
 };
+
+// Relay lanes (lanes 1..31 of the producer warp). For every item of the block's units whose
+// tile `relayed(tile)` holds, wait until the consumers have stored the item (their VG arrivals
+// on the stage's `stored` mbarrier, release / acquire at CTA scope, so the item's global stores
+// are visible here), release the stage to the producer with VG arrivals on `empty`, and run
+// `work(tile, shot)`, which touches global memory only (`prep(tile)` runs once per relayed
+// unit first). The relay cannot fall two `stored` phases behind: the producer refills a stage
+// only after the relay's arrival on `empty`.
+template <typename T, typename Pred, typename Prep, typename Work>
+__device__ __forceinline__ void relay(const ac::Geo<T>& g, const StepArgs<T>& a, SmemHeader* h, int u_beg,
+                                      int u_end, int lane, Pred relayed, Prep prep, Work work) {
+  const int S = a.stages;
+  unsigned par = 0;  // parity of each stage's next `stored` phase
+  int k = 0;
+  for (int un = u_beg; un < u_end && !aborted(h); ++un) {
+    const int tile = un / a.ngroups, grp = un - tile * a.ngroups;
+    const int s_beg = grp * a.G, s_end = min(g.ns, s_beg + a.G);
+    if (!relayed(tile)) {
+      k += s_end - s_beg;
+      continue;
+    }
+    prep(tile);
+    for (int sh = s_beg; sh < s_end; ++sh, ++k) {
+      const int st = k % S;
+      if (!mbar_wait(&h->stored[st], (par >> st) & 1u)) {
+        set_abort(h, a.flag);
+        return;
+      }
+      par ^= 1u << st;
+      if (lane == 1) mbar_arrive_cnt(&h->empty[st], VG);
+      work(tile, sh);
+    }
+  }
+}
 
 template <typename T>
 __global__ void __launch_bounds__(VTHREADS, VMINB)
@@ -118,6 +154,7 @@ __global__ void __launch_bounds__(VTHREADS, VMINB)
     for (int s = 0; s < S; ++s) {
       mbar_init(&h->full[s], 1);
       mbar_init(&h->empty[s], VG);
+      mbar_init(&h->stored[s], VG);
     }
     h->abort_flag = 0;
     fence_barrier_init();
@@ -128,11 +165,64 @@ __global__ void __launch_bounds__(VTHREADS, VMINB)
   const int nunits = a.ntiles * a.ngroups;
   const int per = (nunits + gridDim.x - 1) / gridDim.x;
   const int u_beg = blockIdx.x * per, u_end = min(nunits, u_beg + per);
+  const bool recording = a.rec_p != nullptr;
 
   if (warp == VG / 32) {
     if (lane == 0) {
       const int ymap[3][3] = {{0, -1, 0}, {1, -3, LY::kE}, {2, -1, LY::kE + LY::kW}};
       produce<T, 3>(maps, g, a, h, ih, stage0, LY::kStage, LY::kStageTx, ymap, u_beg, u_end, true);
+    } else if (recording) {
+      // records of step it (acoustic_kernels.py:167-169) from the item's stored p, u, w; a lane
+      // keeps the cells and ids of its receivers rb + lane - 1 + 31 m (m < 2) for the unit
+      const Layout L = g.L;
+      T* rp = const_cast<T*>(a.rec_p);
+      T* ru = const_cast<T*>(a.rec_u);
+      T* rw = const_cast<T*>(a.rec_w);
+      int64_t coff[2] = {0, 0};
+      int rid[2] = {0, 0}, rn = 0, rb = 0, re = 0, i0 = 0, j0 = 0;
+      relay(g, a, h, u_beg, u_end, lane, [&](int tile) { return g.tile_rcv_beg[tile + 1] > g.tile_rcv_beg[tile]; },
+            [&](int tile) {
+              rb = g.tile_rcv_beg[tile];
+              re = g.tile_rcv_beg[tile + 1];
+              i0 = g.zbeg + (tile / g.tiles_x) * TZ;
+              j0 = (tile % g.tiles_x) * TX;
+              rn = 0;
+#pragma unroll
+              for (int m = 0; m < 2; ++m) {
+                const int q = rb + lane - 1 + 31 * m;
+                if (q < re) {
+                  const int cell = g.trcv_cell[q];
+                  coff[m] = L.off(i0 + (cell >> 16), j0 + (cell & 0xffff));
+                  rid[m] = g.trcv_id[q];
+                  rn = m + 1;
+                }
+              }
+            },
+            [&](int tile, int sh) {
+              const int64_t rowbase = ((int64_t)sh * g.nt + a.it) * g.nr, so = (int64_t)sh * L.plane;
+              T vp[2], vu[2], vw[2];
+#pragma unroll
+              for (int m = 0; m < 2; ++m)
+                if (m < rn) {
+                  vp[m] = a.o0[so + coff[m]];
+                  vu[m] = a.o1[so + coff[m]];
+                  vw[m] = a.o2[so + coff[m]];
+                }
+#pragma unroll
+              for (int m = 0; m < 2; ++m)
+                if (m < rn) {
+                  rp[rowbase + rid[m]] = vp[m];
+                  ru[rowbase + rid[m]] = vu[m];
+                  rw[rowbase + rid[m]] = vw[m];
+                }
+              for (int q = rb + lane - 1 + 62; q < re; q += 31) {  // more than 62 receivers in the tile
+                const int cell = g.trcv_cell[q];
+                const int64_t o = rowbase + g.trcv_id[q], c = so + L.off(i0 + (cell >> 16), j0 + (cell & 0xffff));
+                rp[o] = a.o0[c];
+                ru[o] = a.o1[c];
+                rw[o] = a.o2[c];
+              }
+            });
     }
     return;
   }
@@ -142,14 +232,9 @@ __global__ void __launch_bounds__(VTHREADS, VMINB)
   unsigned char* gs = stage0 + S * LY::kStage;
   T* SPB0 = reinterpret_cast<T*>(gs);
   T* SPB1 = reinterpret_cast<T*>(gs + LY::kSP);
-  T* SOU = reinterpret_cast<T*>(gs + 2 * LY::kSP);
-  T* SOW = reinterpret_cast<T*>(gs + 2 * LY::kSP + LY::kSO);
   const Layout L = g.L;
   const int64_t PL = L.plane;
   const T* cf = a.cf;
-  T* rec_p = const_cast<T*>(a.rec_p);
-  T* rec_u = const_cast<T*>(a.rec_u);
-  T* rec_w = const_cast<T*>(a.rec_w);
 
   // halo task: rows 2*erp, 2*erp+1 of the p halo, box columns 4*ecg .. 4*ecg+3
   const bool has_ext = gt < EXT_TASKS;
@@ -309,10 +394,6 @@ __global__ void __launch_bounds__(VTHREADS, VMINB)
         st4(a.o0 + so + ot, pv);
         st4(a.o1 + so + ot, un);
         st4(a.o2 + so + ot, wn);
-        if (re_ > rb) {
-          st4(SOU + tli * TX + 4 * tcg, un);
-          st4(SOW + tli * TX + 4 * tcg, wn);
-        }
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
           if ((twin >> c) & 1u) {
@@ -321,21 +402,8 @@ __global__ void __launch_bounds__(VTHREADS, VMINB)
           }
         }
       }
-      mbar_arrive(&h->empty[st]);
-      if (re_ > rb) {  // receiver tiles only (uniform across the group)
-        named_sync(bar, VG);
-        if (ready && rec_p != nullptr && gt < 32) {
-          const int64_t rowbase = ((int64_t)sh * g.nt + a.it) * g.nr;
-          for (int q = rb + lane; q < re_; q += 32) {
-            const int cell = g.trcv_cell[q];
-            const int ci = cell >> 16, cj = cell & 0xffff;
-            const int64_t o = rowbase + g.trcv_id[q];
-            rec_p[o] = SP[(ci + 1) * BOXX + cj + 4];
-            rec_u[o] = SOU[ci * TX + cj];
-            rec_w[o] = SOW[ci * TX + cj];
-          }
-        }
-      }
+      // a receiver tile's item goes through the relay lanes, which record it from the stores
+      mbar_arrive(recording && re_ > rb ? &h->stored[st] : &h->empty[st]);
       sel ^= 1;
     }
     if (a.acc0 != nullptr && twin) {
@@ -357,10 +425,14 @@ __global__ void __launch_bounds__(VTHREADS, VMINB)
 //      its free-surface folds, dL/d alpha1 at the tile cells, the new lambda_p of the tile
 //      and q_p = -alpha1 lambda_p on the halo;
 //   C  (256 threads, 1 tile row x 4 columns): the new lambda_u / lambda_w and dL/d alpha2;
-//   D  (tiles holding receivers or the free-surface rows): the new tile passes through shared
-//      memory (lambda_u / lambda_w in the space of q_u / q_w, dead after B), where the dL/d
-//      records of step it-1 are injected and the free-surface fold of lambda_w applied, before
-//      the stores.
+//   D  (tiles holding the free-surface rows, or receivers of u / w): the new tile passes through
+//      shared memory (lambda_u / lambda_w in the space of q_u / q_w, dead after B), where the
+//      dL/d records of step it-1 are injected and the free-surface fold of lambda_w applied,
+//      before the stores.
+// Tiles whose receivers record p only take the ordinary path: the consumers arrive on the
+// stage's `stored` mbarrier, and the relay lanes of the producer warp add the dL/d p-records
+// to the stored lambda_p (a read-modify-write of the item's own output, in the order the
+// shared-memory path adds them) and release the stage.
 #ifndef ADFWI_VEC_ADJ_MINB
 #define ADFWI_VEC_ADJ_MINB 3
 #endif
@@ -386,6 +458,20 @@ struct VecAdjLayout {
   static int bytes(int stages) { return kVecSmemFixed + stages * kStage + kScratch; }
 };
 
+// An adjoint tile whose outputs pass through shared memory (phase D).
+template <typename T>
+__device__ __forceinline__ bool adj_smem_tile(const ac::Geo<T>& g, const StepArgs<T>& a, int tile) {
+  const int i0 = g.zbeg + (tile / g.tiles_x) * TZ;
+  const bool rcv = g.tile_cell_beg[tile + 1] > g.tile_cell_beg[tile];
+  return (g.fsurf && i0 <= g.fs && g.fs - 1 <= i0 + TZ - 1) || (rcv && (a.rec_u != nullptr || a.rec_w != nullptr));
+}
+// An adjoint tile whose dL/d p-records the relay lanes inject.
+template <typename T>
+__device__ __forceinline__ bool adj_relay_tile(const ac::Geo<T>& g, const StepArgs<T>& a, int tile) {
+  return a.it >= 1 && a.rec_p != nullptr && g.tile_cell_beg[tile + 1] > g.tile_cell_beg[tile] &&
+         !adj_smem_tile(g, a, tile);
+}
+
 template <typename T>
 __global__ void __launch_bounds__(VTHREADS, VAMINB)
     adj_step_vec(const __grid_constant__ Maps maps, ac::Geo<T> g, StepArgs<T> a) {
@@ -401,6 +487,7 @@ __global__ void __launch_bounds__(VTHREADS, VAMINB)
     for (int s = 0; s < S; ++s) {
       mbar_init(&h->full[s], 1);
       mbar_init(&h->empty[s], VG);
+      mbar_init(&h->stored[s], VG);
     }
     h->abort_flag = 0;
     fence_barrier_init();
@@ -420,6 +507,62 @@ __global__ void __launch_bounds__(VTHREADS, VAMINB)
                               {3, -1, 2 * LY::kE + LY::kW},
                               {4, -1, 3 * LY::kE + LY::kW}};
       produce<T, 5>(maps, g, a, h, ih, stage0, LY::kStage, LY::kStageTx, ymap, u_beg, u_end, false);
+    } else if (a.it >= 1 && a.rec_p != nullptr) {
+      // dL/d p-records of step it-1 enter lambda_p after step it-1 (acoustic_kernels.py:167-169),
+      // added to the item's stored lambda_p. A lane keeps its receiver cells cb + lane - 1 + 31 m
+      // (m < 2) with their receiver for the unit; cells with several receivers, and a tile's
+      // cells past the 62nd, walk the tables per item.
+      const Layout L = g.L;
+      int64_t coff[2] = {0, 0};
+      int rid[2] = {0, 0}, cn = 0, cb = 0, ce = 0, i0 = 0, j0 = 0;
+      bool walk = false;
+      relay(g, a, h, u_beg, u_end, lane, [&](int tile) { return adj_relay_tile(g, a, tile); },
+            [&](int tile) {
+              cb = g.tile_cell_beg[tile];
+              ce = g.tile_cell_beg[tile + 1];
+              i0 = g.zbeg + (tile / g.tiles_x) * TZ;
+              j0 = (tile % g.tiles_x) * TX;
+              cn = 0;
+              walk = ce - cb > 62;
+#pragma unroll
+              for (int m = 0; m < 2; ++m) {
+                const int q = cb + lane - 1 + 31 * m;
+                if (q < ce) {
+                  const int cell = g.tcell_cell[q], m0 = g.tcell_rbeg[q];
+                  coff[m] = L.off(i0 + (cell >> 16), j0 + (cell & 0xffff));
+                  rid[m] = g.cell_rcv[m0];
+                  if (g.tcell_rbeg[q + 1] - m0 != 1) walk = true;
+                  cn = m + 1;
+                }
+              }
+            },
+            [&](int tile, int sh) {
+              const int64_t rowbase = ((int64_t)sh * g.nt + (a.it - 1)) * g.nr, so = (int64_t)sh * L.plane;
+              if (!walk) {
+                T v[2], o[2];
+#pragma unroll
+                for (int m = 0; m < 2; ++m)
+                  if (m < cn) {
+                    v[m] = a.rec_p[rowbase + rid[m]];
+                    o[m] = a.o0[so + coff[m]];
+                  }
+#pragma unroll
+                for (int m = 0; m < 2; ++m)
+                  if (m < cn) {
+                    T ap = T(0);
+                    ap += v[m];
+                    a.o0[so + coff[m]] = o[m] + ap;
+                  }
+              } else {
+                for (int q = cb + lane - 1; q < ce; q += 31) {
+                  const int cell = g.tcell_cell[q];
+                  T ap = T(0);
+                  for (int mm = g.tcell_rbeg[q]; mm < g.tcell_rbeg[q + 1]; ++mm) ap += a.rec_p[rowbase + g.cell_rcv[mm]];
+                  T* o = a.o0 + so + L.off(i0 + (cell >> 16), j0 + (cell & 0xffff));
+                  *o = *o + ap;
+                }
+              }
+            });
     }
     return;
   }
@@ -478,7 +621,7 @@ __global__ void __launch_bounds__(VTHREADS, VAMINB)
           }
         }
       }
-      special = (ce > cb) || (g.fsurf && i0 <= g.fs && g.fs - 1 <= i0 + TZ - 1);
+      special = adj_smem_tile(g, a, tile);
       prev_tile = tile;
     }
     const int64_t go = (int64_t)sgrp * PL;
@@ -650,7 +793,8 @@ __global__ void __launch_bounds__(VTHREADS, VAMINB)
           st4(a.o2 + o, lwo);
         }
       }
-      if (!special) mbar_arrive(&h->empty[st]);
+      // an ordinary tile that injects (p receivers only: adj_relay_tile) hands the item to the relay
+      if (!special) mbar_arrive(inject ? &h->stored[st] : &h->empty[st]);
       // ---- D: tiles with receivers or the free-surface rows
       if (special) {
         named_sync(bar, VG);

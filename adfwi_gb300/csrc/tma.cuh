@@ -59,6 +59,11 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
+// `count` arrivals at once (release semantics at CTA scope, like every arrive here).
+__device__ __forceinline__ void mbar_arrive_cnt(uint64_t* bar, unsigned count) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
 // Wait for the phase with the given parity to complete. Returns false once kWaitNs have passed.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
   const uint32_t a = smem_u32(bar);

@@ -132,6 +132,7 @@ class ElasticSolve(torch.autograd.Function):
     def forward(ctx, c11, c13, c15, c33, c35, c55, bx, bz, abc0, abc1, wavelet, plan):
         coefs = [c11, c13, c15, c33, c35, c55, bx, bz, abc0, abc1]
         need = any(ctx.needs_input_grad[:8])
+        ctx.set_materialize_grads(False)  # unused record components reach backward as None
         rec, fw, ws, ts = plan.run_forward(coefs, wavelet, need)
         ctx.plan = plan
         ctx.ws = ws if need else None

@@ -142,6 +142,39 @@ def test_gradient_matches_centred_finite_differences_f64():
     assert abs(fd - an) <= 1e-6 * abs(an), (fd, an)
 
 
+@pytest.mark.parametrize("dtype,tol", [(torch.float32, 1e-4), (torch.float64, 1e-9)])
+@pytest.mark.parametrize("free_surface", [False, True])
+def test_gradient_of_pressure_records_only(dtype, tol, free_surface):
+    """A loss on the pressure records alone (dL/d u- and w-records absent): receiver tiles take
+    the ordinary path and their dL/d p-records are added to the stored adjoint state after
+    each item. The survey puts 64 receiver cells in one 64-column tile, two receivers on some
+    cells and receivers on two depths, so every variant of that injection runs (cached cells,
+    the per-item table walk, a free-surface tile next to an ordinary one)."""
+    nz, nx, nabc, nt = 40, 120, 12, 200
+    rng = np.random.default_rng(41)
+    from _cases import layered_vp
+    npdt = np.float64 if dtype == torch.float64 else np.float32
+    vp = layered_vp(nz, nx, rng).astype(npdt)
+    rho = (np.power(vp, 0.25) * 310).astype(npdt)
+    model = A.AcousticModel(0, 0, nx, nz, 10.0, 10.0, vp=vp, rho=rho, vp_grad=True, rho_grad=True,
+                            free_surface=free_surface, nabc=nabc, device="cuda:0", dtype=dtype)
+    src = A.Source(nt=nt, dt=1e-3, f0=20.0)
+    _, wav = A.wavelet(nt, 1e-3, 20.0)
+    src.add_sources(src_x=np.array([5, 60, 110]), src_z=np.array([1, 1, 1]), src_wavelet=wav)
+    rx = np.concatenate([np.arange(nx), np.arange(0, nx, 7), np.arange(3, nx, 5)])
+    rz = np.concatenate([np.full(nx, 2), np.full(len(np.arange(0, nx, 7)), 2), np.full(len(np.arange(3, nx, 5)), 21)])
+    rcv = A.Receiver(nt=nt, dt=1e-3)
+    rcv.add_receivers(rcv_x=rx, rcv_z=rz, rcv_type="pr")
+    prop = A.AcousticPropagator(model, A.Survey(src, rcv), device="cuda:0", dtype=dtype, snapshot_every=30)
+    rec = prop.forward()
+    w = torch.randn(rec["p"].shape, generator=torch.Generator().manual_seed(3), dtype=dtype)
+    (rec["p"] * w.cuda()).sum().backward()
+    ref, vpo, rhoo = oracle_acoustic(prop, model)
+    (ref["p"] * w).sum().backward()
+    assert rel(model.vp.grad, vpo.grad) <= tol, rel(model.vp.grad, vpo.grad)
+    assert rel(model.rho.grad, rhoo.grad) <= tol, rel(model.rho.grad, rhoo.grad)
+
+
 def test_repeated_backward_and_shot_batches_agree():
     model, survey, prop = acoustic_problem(A, ns=4, seed=31, snapshot_every=40)
     rec = prop.forward()

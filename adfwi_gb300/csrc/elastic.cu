@@ -694,6 +694,14 @@ __global__ void adj_t_pml(Geo<T> g, const T* __restrict__ cf, const T* __restric
   T* gbx = gbase + 6 * PL;
   T* gbz = gbase + 7 * PL;
   T gx = T(0), gz = T(0);
+  const bool inside = in_I(g, i, j);
+  // d(v_x')/d(bx) = dt * D(T) / (d * pml_d), likewise for bz: the cell's factors dt / (d pml_d)
+  T kx = T(0), kz = T(0);
+  if (inside) {
+    const Pml<T> p = pml_at(g, cf, oc, PL);
+    kx = g.dt / (g.dx * p.xd);
+    kz = g.dt / (g.dz * p.zd);
+  }
   for (int s = s_beg; s < s_end; ++s) {
     const int64_t so = (int64_t)s * PL;
     const PlaneQ<T> q_vxx{q4 + 0 * NSP + so, g.L}, q_vxz{q4 + 1 * NSP + so, g.L};
@@ -702,17 +710,15 @@ __global__ void adj_t_pml(Geo<T> g, const T* __restrict__ cf, const T* __restric
     lt[TXX * NSP + o] += dxf_t<NN>(g, q_vxx, i, j);
     lt[TXZ * NSP + o] += dzb_t<NN>(g, q_vxz, i, j) + dxb_t<NN>(g, q_vzx, i, j);
     lt[TZZ * NSP + o] += dzf_t<NN>(g, q_vzz, i, j);
-    if (in_I(g, i, j)) {
-      // d(v_x')/d(bx) = dt * D(T) / (d * pml_d), likewise for bz
+    if (inside) {
       const T* th = tt_hist;
-      const Pml<T> p = pml_at(g, cf, oc, PL);
-      gx += lvs[VX_X * NSP + o] * g.dt * dxf<NN>(g, th + TXX * NSP, o) / (g.dx * p.xd) +
-            lvs[VX_Z * NSP + o] * g.dt * dzb<NN>(g, th + TXZ * NSP, o) / (g.dz * p.zd);
-      gz += lvs[VZ_X * NSP + o] * g.dt * dxb<NN>(g, th + TXZ * NSP, o) / (g.dx * p.xd) +
-            lvs[VZ_Z * NSP + o] * g.dt * dzf<NN>(g, th + TZZ * NSP, o) / (g.dz * p.zd);
+      gx += lvs[VX_X * NSP + o] * dxf<NN>(g, th + TXX * NSP, o) * kx +
+            lvs[VX_Z * NSP + o] * dzb<NN>(g, th + TXZ * NSP, o) * kz;
+      gz += lvs[VZ_X * NSP + o] * dxb<NN>(g, th + TXZ * NSP, o) * kx +
+            lvs[VZ_Z * NSP + o] * dzf<NN>(g, th + TZZ * NSP, o) * kz;
     }
   }
-  if (in_I(g, i, j)) {
+  if (inside) {
     gbx[oc] += gx;
     gbz[oc] += gz;
   }
@@ -748,14 +754,23 @@ struct StressQ {
 };
 
 // Coefficient-weighted adjoint sources of the stress update at cell (i, j) of one shot.
+// The cell's factors: dt/dx / pml_xd and dt/dz / pml_zd (PML form), dt/dx and dt/dz (ABL form).
 template <typename T, bool PMLM>
-__device__ __forceinline__ StressQ<T> stress_q(const Geo<T>& g, const T* __restrict__ cf,
-                                               const T* __restrict__ lts, int64_t c0, int64_t oo, int64_t PL,
-                                               int64_t NSP) {
-  StressQ<T> r;
+__device__ __forceinline__ void stress_k(const Geo<T>& g, const T* __restrict__ cf, int64_t c0, int64_t PL, T& kx,
+                                         T& kz) {
   if (PMLM) {
     const Pml<T> p = pml_at(g, cf, c0, PL);
-    const T kx = g.dt_dx / p.xd, kz = g.dt_dz / p.zd;
+    kx = g.dt_dx / p.xd;
+    kz = g.dt_dz / p.zd;
+  } else {
+    kx = g.dt / g.dx;
+    kz = g.dt / g.dz;
+  }
+}
+template <typename T, bool PMLM>
+__device__ __forceinline__ StressQ<T> stress_q(const T* __restrict__ lts, int64_t oo, int64_t NSP, T kx, T kz) {
+  StressQ<T> r;
+  if (PMLM) {
     r.a = lts[TXX_X * NSP + oo] * kx;
     r.b = lts[TXX_Z * NSP + oo] * kz;
     r.c = lts[TZZ_X * NSP + oo] * kx;
@@ -763,7 +778,6 @@ __device__ __forceinline__ StressQ<T> stress_q(const Geo<T>& g, const T* __restr
     r.e = lts[TXZ_X * NSP + oo] * kx;
     r.f = lts[TXZ_Z * NSP + oo] * kz;
   } else {
-    const T kx = g.dt / g.dx, kz = g.dt / g.dz;
     r.a = lts[TXX * NSP + oo] * kx;
     r.b = lts[TXX * NSP + oo] * kz;
     r.c = lts[TZZ * NSP + oo] * kx;
@@ -784,7 +798,9 @@ __global__ void adj_vq(Geo<T> g, const T* __restrict__ cf, const T* __restrict__
   for (int k = 0; k < 8; ++k) v[k] = T(0);
   if (in_I(g, i, j)) {
     const int64_t c0 = g.L.off(i, j);
-    const StressQ<T> r = stress_q<T, PMLM>(g, cf, lts, c0, o, PL, NSP);
+    T kx, kz;
+    stress_k<T, PMLM>(g, cf, c0, PL, kx, kz);
+    const StressQ<T> r = stress_q<T, PMLM>(lts, o, NSP, kx, kz);
     const T c11 = cf[C11 * PL + c0], c13 = cf[C13 * PL + c0], c15 = cf[C15 * PL + c0];
     const T c33 = cf[C33 * PL + c0], c35 = cf[C35 * PL + c0], c55 = cf[C55 * PL + c0];
     v[0] = c11 * r.a + c13 * r.c;
@@ -810,12 +826,13 @@ __global__ void adj_vfs_tq_pml(Geo<T> g, const T* __restrict__ cf, const T* __re
   vfs_adjoint(g, lv + VX * NSP, lv + VZ * NSP, i, j, o, ax, az);
   const bool inside = in_I(g, i, j);
   const int64_t c0 = g.L.off(i, j);
-  T sx = T(1), sz = T(1);
-  Pml<T> p;
+  T sx = T(1), sz = T(1), ix = T(0), iz = T(0);
   if (inside) {
-    p = pml_at(g, cf, c0, PL);
-    sx = p.xn / p.xd;
-    sz = p.zn / p.zd;
+    const Pml<T> p = pml_at(g, cf, c0, PL);
+    ix = T(1) / p.xd;  // one division per direction; the adjoint needs no bit-exact rounding
+    iz = T(1) / p.zd;
+    sx = p.xn * ix;
+    sz = p.zn * iz;
   }
   const T vxx = sx * lvs[VX_X * NSP + o] + ax, vxz = sz * lvs[VX_Z * NSP + o] + ax;
   const T vzx = sx * lvs[VZ_X * NSP + o] + az, vzz = sz * lvs[VZ_Z * NSP + o] + az;
@@ -826,10 +843,11 @@ __global__ void adj_vfs_tq_pml(Geo<T> g, const T* __restrict__ cf, const T* __re
   T a = T(0), b = T(0), c = T(0), d = T(0);
   if (inside) {
     const T bx = cf[BX * PL + c0], bz = cf[BZ * PL + c0];
-    a = vxx * (g.dt * bx) / (g.dx * p.xd);
-    b = vxz * (g.dt * bx) / (g.dz * p.zd);
-    c = vzx * (g.dt * bz) / (g.dx * p.xd);
-    d = vzz * (g.dt * bz) / (g.dz * p.zd);
+    const T kx = g.dt_dx * ix, kz = g.dt_dz * iz;
+    a = vxx * (bx * kx);
+    b = vxz * (bx * kz);
+    c = vzx * (bz * kx);
+    d = vzz * (bz * kz);
   }
   q4[0 * NSP + o] = a;
   q4[1 * NSP + o] = b;
@@ -848,12 +866,13 @@ __global__ void adj_tfs_vq_pml(Geo<T> g, const T* __restrict__ cf, const T* __re
   const T axx = lt[TXX * NSP + o];
   const bool inside = in_I(g, i, j);
   const int64_t c0 = g.L.off(i, j);
-  T sx = T(1), sz = T(1);
-  Pml<T> p;
+  T sx = T(1), sz = T(1), ix = T(0), iz = T(0);
   if (inside) {
-    p = pml_at(g, cf, c0, PL);
-    sx = p.xn / p.xd;
-    sz = p.zn / p.zd;
+    const Pml<T> p = pml_at(g, cf, c0, PL);
+    ix = T(1) / p.xd;
+    iz = T(1) / p.zd;
+    sx = p.xn * ix;
+    sz = p.zn * iz;
   }
   T ls[6];
   ls[0] = sx * lts[TXX_X * NSP + o] + axx;
@@ -868,7 +887,7 @@ __global__ void adj_tfs_vq_pml(Geo<T> g, const T* __restrict__ cf, const T* __re
 #pragma unroll
   for (int k = 0; k < 8; ++k) v[k] = T(0);
   if (inside) {
-    const T kx = g.dt_dx / p.xd, kz = g.dt_dz / p.zd;
+    const T kx = g.dt_dx * ix, kz = g.dt_dz * iz;
     StressQ<T> r;
     r.a = ls[0] * kx;
     r.b = ls[1] * kz;
@@ -901,6 +920,9 @@ __global__ void adj_v(Geo<T> g, const T* __restrict__ cf, const T* __restrict__ 
   EL_SHOT_GROUP
   T* gc = gbase;
   T g11 = T(0), g13 = T(0), g15 = T(0), g33 = T(0), g35 = T(0), g55 = T(0);
+  const bool inside = in_I(g, i, j);
+  T kx = T(0), kz = T(0);
+  if (inside) stress_k<T, PMLM>(g, cf, oc, PL, kx, kz);
   for (int s = s_beg; s < s_end; ++s) {
     const int64_t so = (int64_t)s * PL;
     const PlaneQ<T> sx_b{q8 + 0 * NSP + so, g.L}, sx_zb{q8 + 1 * NSP + so, g.L};
@@ -919,8 +941,8 @@ __global__ void adj_v(Geo<T> g, const T* __restrict__ cf, const T* __restrict__ 
       lv[VX * NSP + o] += avx;
       lv[VZ * NSP + o] += avz;
     }
-    if (in_I(g, i, j)) {
-      const StressQ<T> r = stress_q<T, PMLM>(g, cf, lts, oc, o, PL, NSP);
+    if (inside) {
+      const StressQ<T> r = stress_q<T, PMLM>(lts, o, NSP, kx, kz);
       const T* vx = v_hist + VX * NSP;
       const T* vz = v_hist + VZ * NSP;
       const T dxb_vx = dxb<NN>(g, vx, o), dxb_vz = dxb<NN>(g, vz, o);
@@ -935,7 +957,7 @@ __global__ void adj_v(Geo<T> g, const T* __restrict__ cf, const T* __restrict__ 
       g55 += r.e * dxf_vz + r.f * dzf_vx;
     }
   }
-  if (in_I(g, i, j)) {
+  if (inside) {
     gc[C11 * PL + oc] += g11;
     gc[C13 * PL + oc] += g13;
     gc[C15 * PL + oc] += g15;

@@ -144,6 +144,28 @@ __device__ __forceinline__ T dzb_t(const Geo<T>& g, const Q& q, int i, int j) {
   const int64_t o = (int64_t)s * PL + g.L.off(i, j);                                 \
   (void)NSP;
 
+// Per-cell kernels that take several shots of one cell per thread (blockIdx.y picks a block of
+// kCellShots consecutive shots): the cell's coefficients and PML factors are loaded and formed
+// once, and the shots' field loads are independent, so more of them are in flight.
+#ifndef ADFWI_EL_CELL_SHOTS
+#define ADFWI_EL_CELL_SHOTS 2
+#endif
+constexpr int kCellShots = ADFWI_EL_CELL_SHOTS;
+#define EL_CELL_SHOTS                                                                \
+  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;                  \
+  if (e >= (int64_t)g.L.nzp * g.L.nxp) return;                                      \
+  const int i = (int)(e / g.L.nxp), j = (int)(e - (int64_t)i * g.L.nxp);            \
+  const int s_lo = blockIdx.y * kCellShots;                                          \
+  const int64_t PL = g.L.plane, NSP = (int64_t)g.ns * PL;                            \
+  const int64_t occ = g.L.off(i, j);
+
+// x / d where d is a PML denominator 1 + dt/2 d(x): exactly x wherever d is 1 (outside the
+// absorbing frame), so the division runs only inside the frame.
+template <typename T>
+__device__ __forceinline__ T rdiv_pml(T x, T d) {
+  return d == T(1) ? x : rdiv(x, d);
+}
+
 #define EL_CELL                                                                      \
   const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;                  \
   if (e >= (int64_t)g.L.nzp * g.L.nxp) return;                                      \
@@ -278,47 +300,63 @@ __device__ __forceinline__ bool vel_fs_row(const Geo<T>& g, int i, int j) {
 template <typename T, int NN>
 __global__ void stress_pml_tot(Geo<T> g, int it, const T* __restrict__ cf, const T* __restrict__ v,
                                T* __restrict__ ts, T* __restrict__ tt, const T* __restrict__ wav) {
-  EL_CELL_SHOT
-  const int64_t occ = g.L.off(i, j);
-  T sp[6];
-#pragma unroll
-  for (int k = 0; k < 6; ++k) sp[k] = ts[k * NSP + o];
-  if (in_I(g, i, j)) {
-    const T* vx = v;
-    const T* vz = v + NSP;
-    const T dxbm_vx = dxb<NN>(g, vx, o), dxbm_vz = dxb<NN>(g, vz, o);
-    const T dzbm_vx = dzb<NN>(g, vx, o), dzbm_vz = dzb<NN>(g, vz, o);
-    const T dxfm_vx = dxf<NN>(g, vx, o), dzfm_vx = dzf<NN>(g, vx, o);
-    const T dxfm_vz = dxf<NN>(g, vz, o), dzfm_vz = dzf<NN>(g, vz, o);
+  EL_CELL_SHOTS
+  const bool inside = in_I(g, i, j);
+  T pxn = T(0), pzn = T(0), pxi = T(0), pzi = T(0);
+  T c11 = T(0), c13 = T(0), c15 = T(0), c33 = T(0), c35 = T(0), c55 = T(0);
+  if (inside) {
     const T bcx = cf[BCX * PL + occ], bcz = cf[BCZ * PL + occ];
-    const T pxd = radd(T(1), rmul(g.hdt, bcx)), pxn = rsub(T(1), rmul(g.hdt, bcx));
-    const T pzd = radd(T(1), rmul(g.hdt, bcz)), pzn = rsub(T(1), rmul(g.hdt, bcz));
-    const T pxi = rdiv(T(1), pxd), pzi = rdiv(T(1), pzd);
-    const T c11 = cf[C11 * PL + occ], c13 = cf[C13 * PL + occ], c15 = cf[C15 * PL + occ];
-    const T c33 = cf[C33 * PL + occ], c35 = cf[C35 * PL + occ], c55 = cf[C55 * PL + occ];
-    sp[TXX_X] = rmul(radd(rmul(pxn, sp[TXX_X]), rmul(g.dt_dx, radd(rmul(c11, dxbm_vx), rmul(c15, dxbm_vz)))), pxi);
-    sp[TXX_Z] = rmul(radd(rmul(pzn, sp[TXX_Z]), rmul(g.dt_dz, radd(rmul(c15, dzbm_vx), rmul(c13, dzbm_vz)))), pzi);
-    sp[TZZ_X] = rmul(radd(rmul(pxn, sp[TZZ_X]), rmul(g.dt_dx, radd(rmul(c13, dxbm_vx), rmul(c35, dxbm_vz)))), pxi);
-    sp[TZZ_Z] = rmul(radd(rmul(pzn, sp[TZZ_Z]), rmul(g.dt_dz, radd(rmul(c35, dzbm_vx), rmul(c33, dzbm_vz)))), pzi);
-    sp[TXZ_X] = rmul(radd(rmul(pxn, sp[TXZ_X]), rmul(g.dt_dx, radd(rmul(c15, dxfm_vx), rmul(c55, dxfm_vz)))), pxi);
-    sp[TXZ_Z] = rmul(radd(rmul(pzn, sp[TXZ_Z]), rmul(g.dt_dz, radd(rmul(c55, dzfm_vx), rmul(c35, dzfm_vz)))), pzi);
-  }
-  if (i == g.src_z[s] && j == g.src_x[s]) {
-    const T w = wav[(int64_t)s * g.nt + it];
-    const T axx = rmul(g.src_m[3 * s + 0], w), azz = rmul(g.src_m[3 * s + 1], w), axz = rmul(g.src_m[3 * s + 2], w);
-    sp[TXX_X] = radd(sp[TXX_X], axx);
-    sp[TXX_Z] = radd(sp[TXX_Z], axx);
-    sp[TZZ_X] = radd(sp[TZZ_X], azz);
-    sp[TZZ_Z] = radd(sp[TZZ_Z], azz);
-    sp[TXZ_X] = radd(sp[TXZ_X], axz);
-    sp[TXZ_Z] = radd(sp[TXZ_Z], axz);
+    const T pxd = radd(T(1), rmul(g.hdt, bcx)), pzd = radd(T(1), rmul(g.hdt, bcz));
+    pxn = rsub(T(1), rmul(g.hdt, bcx));
+    pzn = rsub(T(1), rmul(g.hdt, bcz));
+    pxi = rdiv_pml(T(1), pxd);
+    pzi = rdiv_pml(T(1), pzd);
+    c11 = cf[C11 * PL + occ];
+    c13 = cf[C13 * PL + occ];
+    c15 = cf[C15 * PL + occ];
+    c33 = cf[C33 * PL + occ];
+    c35 = cf[C35 * PL + occ];
+    c55 = cf[C55 * PL + occ];
   }
 #pragma unroll
-  for (int k = 0; k < 6; ++k) ts[k * NSP + o] = sp[k];
-  if (!stress_fs_row(g, i)) {
-    tt[TXX * NSP + o] = radd(sp[TXX_X], sp[TXX_Z]);
-    tt[TZZ * NSP + o] = radd(sp[TZZ_X], sp[TZZ_Z]);
-    tt[TXZ * NSP + o] = radd(sp[TXZ_X], sp[TXZ_Z]);
+  for (int q = 0; q < kCellShots; ++q) {
+    const int s = s_lo + q;
+    if (s >= g.ns) break;
+    const int64_t o = (int64_t)s * PL + occ;
+    T sp[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) sp[k] = ts[k * NSP + o];
+    if (inside) {
+      const T* vx = v;
+      const T* vz = v + NSP;
+      const T dxbm_vx = dxb<NN>(g, vx, o), dxbm_vz = dxb<NN>(g, vz, o);
+      const T dzbm_vx = dzb<NN>(g, vx, o), dzbm_vz = dzb<NN>(g, vz, o);
+      const T dxfm_vx = dxf<NN>(g, vx, o), dzfm_vx = dzf<NN>(g, vx, o);
+      const T dxfm_vz = dxf<NN>(g, vz, o), dzfm_vz = dzf<NN>(g, vz, o);
+      sp[TXX_X] = rmul(radd(rmul(pxn, sp[TXX_X]), rmul(g.dt_dx, radd(rmul(c11, dxbm_vx), rmul(c15, dxbm_vz)))), pxi);
+      sp[TXX_Z] = rmul(radd(rmul(pzn, sp[TXX_Z]), rmul(g.dt_dz, radd(rmul(c15, dzbm_vx), rmul(c13, dzbm_vz)))), pzi);
+      sp[TZZ_X] = rmul(radd(rmul(pxn, sp[TZZ_X]), rmul(g.dt_dx, radd(rmul(c13, dxbm_vx), rmul(c35, dxbm_vz)))), pxi);
+      sp[TZZ_Z] = rmul(radd(rmul(pzn, sp[TZZ_Z]), rmul(g.dt_dz, radd(rmul(c35, dzbm_vx), rmul(c33, dzbm_vz)))), pzi);
+      sp[TXZ_X] = rmul(radd(rmul(pxn, sp[TXZ_X]), rmul(g.dt_dx, radd(rmul(c15, dxfm_vx), rmul(c55, dxfm_vz)))), pxi);
+      sp[TXZ_Z] = rmul(radd(rmul(pzn, sp[TXZ_Z]), rmul(g.dt_dz, radd(rmul(c55, dzfm_vx), rmul(c35, dzfm_vz)))), pzi);
+    }
+    if (i == g.src_z[s] && j == g.src_x[s]) {
+      const T w = wav[(int64_t)s * g.nt + it];
+      const T axx = rmul(g.src_m[3 * s + 0], w), azz = rmul(g.src_m[3 * s + 1], w), axz = rmul(g.src_m[3 * s + 2], w);
+      sp[TXX_X] = radd(sp[TXX_X], axx);
+      sp[TXX_Z] = radd(sp[TXX_Z], axx);
+      sp[TZZ_X] = radd(sp[TZZ_X], azz);
+      sp[TZZ_Z] = radd(sp[TZZ_Z], azz);
+      sp[TXZ_X] = radd(sp[TXZ_X], axz);
+      sp[TXZ_Z] = radd(sp[TXZ_Z], axz);
+    }
+#pragma unroll
+    for (int k = 0; k < 6; ++k) ts[k * NSP + o] = sp[k];
+    if (!stress_fs_row(g, i)) {
+      tt[TXX * NSP + o] = radd(sp[TXX_X], sp[TXX_Z]);
+      tt[TZZ * NSP + o] = radd(sp[TZZ_X], sp[TZZ_Z]);
+      tt[TXZ * NSP + o] = radd(sp[TXZ_X], sp[TXZ_Z]);
+    }
   }
 }
 
@@ -345,31 +383,42 @@ __global__ void stress_fs_rows_pml(Geo<T> g, const T* __restrict__ ts, T* __rest
 template <typename T, int NN>
 __global__ void vel_pml_tot(Geo<T> g, const T* __restrict__ cf, const T* __restrict__ tt, T* __restrict__ vs,
                             T* __restrict__ v) {
-  EL_CELL_SHOT
-  T sv[4];
-#pragma unroll
-  for (int k = 0; k < 4; ++k) sv[k] = vs[k * NSP + o];
-  if (in_I(g, i, j)) {
-    const int64_t occ = g.L.off(i, j);
-    const T dxfm_txx = dxf<NN>(g, tt + TXX * NSP, o);
-    const T dzbm_txz = dzb<NN>(g, tt + TXZ * NSP, o);
-    const T dxbm_txz = dxb<NN>(g, tt + TXZ * NSP, o);
-    const T dzfm_tzz = dzf<NN>(g, tt + TZZ * NSP, o);
+  EL_CELL_SHOTS
+  const bool inside = in_I(g, i, j);
+  T pxd = T(1), pxn = T(0), pzd = T(1), pzn = T(0), dbx = T(0), dbz = T(0);
+  if (inside) {
     const T bcx = cf[BCX * PL + occ], bcz = cf[BCZ * PL + occ];
-    const T pxd = radd(T(1), rmul(g.hdt, bcx)), pxn = rsub(T(1), rmul(g.hdt, bcx));
-    const T pzd = radd(T(1), rmul(g.hdt, bcz)), pzn = rsub(T(1), rmul(g.hdt, bcz));
-    const T bx = cf[BX * PL + occ], bz = cf[BZ * PL + occ];
-    const T dbx = rmul(g.dt, bx), dbz = rmul(g.dt, bz);
-    sv[VX_X] = rdiv(radd(rmul(pxn, sv[VX_X]), rdiv(rmul(dbx, dxfm_txx), g.dx)), pxd);
-    sv[VX_Z] = rdiv(radd(rmul(pzn, sv[VX_Z]), rdiv(rmul(dbx, dzbm_txz), g.dz)), pzd);
-    sv[VZ_X] = rdiv(radd(rmul(pxn, sv[VZ_X]), rdiv(rmul(dbz, dxbm_txz), g.dx)), pxd);
-    sv[VZ_Z] = rdiv(radd(rmul(pzn, sv[VZ_Z]), rdiv(rmul(dbz, dzfm_tzz), g.dz)), pzd);
-#pragma unroll
-    for (int k = 0; k < 4; ++k) vs[k * NSP + o] = sv[k];
+    pxd = radd(T(1), rmul(g.hdt, bcx));
+    pxn = rsub(T(1), rmul(g.hdt, bcx));
+    pzd = radd(T(1), rmul(g.hdt, bcz));
+    pzn = rsub(T(1), rmul(g.hdt, bcz));
+    dbx = rmul(g.dt, cf[BX * PL + occ]);
+    dbz = rmul(g.dt, cf[BZ * PL + occ]);
   }
-  if (!vel_fs_row(g, i, j)) {
-    v[VX * NSP + o] = radd(sv[VX_X], sv[VX_Z]);
-    v[VZ * NSP + o] = radd(sv[VZ_X], sv[VZ_Z]);
+#pragma unroll
+  for (int q = 0; q < kCellShots; ++q) {
+    const int s = s_lo + q;
+    if (s >= g.ns) break;
+    const int64_t o = (int64_t)s * PL + occ;
+    T sv[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) sv[k] = vs[k * NSP + o];
+    if (inside) {
+      const T dxfm_txx = dxf<NN>(g, tt + TXX * NSP, o);
+      const T dzbm_txz = dzb<NN>(g, tt + TXZ * NSP, o);
+      const T dxbm_txz = dxb<NN>(g, tt + TXZ * NSP, o);
+      const T dzfm_tzz = dzf<NN>(g, tt + TZZ * NSP, o);
+      sv[VX_X] = rdiv_pml(radd(rmul(pxn, sv[VX_X]), rdiv(rmul(dbx, dxfm_txx), g.dx)), pxd);
+      sv[VX_Z] = rdiv_pml(radd(rmul(pzn, sv[VX_Z]), rdiv(rmul(dbx, dzbm_txz), g.dz)), pzd);
+      sv[VZ_X] = rdiv_pml(radd(rmul(pxn, sv[VZ_X]), rdiv(rmul(dbz, dxbm_txz), g.dx)), pxd);
+      sv[VZ_Z] = rdiv_pml(radd(rmul(pzn, sv[VZ_Z]), rdiv(rmul(dbz, dzfm_tzz), g.dz)), pzd);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) vs[k * NSP + o] = sv[k];
+    }
+    if (!vel_fs_row(g, i, j)) {
+      v[VX * NSP + o] = radd(sv[VX_X], sv[VX_Z]);
+      v[VZ * NSP + o] = radd(sv[VZ_X], sv[VZ_Z]);
+    }
   }
 }
 
@@ -821,38 +870,39 @@ __global__ void adj_vq(Geo<T> g, const T* __restrict__ cf, const T* __restrict__
 template <typename T>
 __global__ void adj_vfs_tq_pml(Geo<T> g, const T* __restrict__ cf, const T* __restrict__ lv, T* lvs,
                                T* __restrict__ q4) {
-  EL_CELL_SHOT
-  T ax, az;
-  vfs_adjoint(g, lv + VX * NSP, lv + VZ * NSP, i, j, o, ax, az);
+  EL_CELL_SHOTS
   const bool inside = in_I(g, i, j);
-  const int64_t c0 = g.L.off(i, j);
-  T sx = T(1), sz = T(1), ix = T(0), iz = T(0);
+  T sx = T(1), sz = T(1), kbx_x = T(0), kbx_z = T(0), kbz_x = T(0), kbz_z = T(0);
   if (inside) {
-    const Pml<T> p = pml_at(g, cf, c0, PL);
-    ix = T(1) / p.xd;  // one division per direction; the adjoint needs no bit-exact rounding
-    iz = T(1) / p.zd;
+    const Pml<T> p = pml_at(g, cf, occ, PL);
+    const T ix = T(1) / p.xd, iz = T(1) / p.zd;  // the adjoint needs no bit-exact rounding
     sx = p.xn * ix;
     sz = p.zn * iz;
-  }
-  const T vxx = sx * lvs[VX_X * NSP + o] + ax, vxz = sz * lvs[VX_Z * NSP + o] + ax;
-  const T vzx = sx * lvs[VZ_X * NSP + o] + az, vzz = sz * lvs[VZ_Z * NSP + o] + az;
-  lvs[VX_X * NSP + o] = vxx;
-  lvs[VX_Z * NSP + o] = vxz;
-  lvs[VZ_X * NSP + o] = vzx;
-  lvs[VZ_Z * NSP + o] = vzz;
-  T a = T(0), b = T(0), c = T(0), d = T(0);
-  if (inside) {
-    const T bx = cf[BX * PL + c0], bz = cf[BZ * PL + c0];
+    const T bx = cf[BX * PL + occ], bz = cf[BZ * PL + occ];
     const T kx = g.dt_dx * ix, kz = g.dt_dz * iz;
-    a = vxx * (bx * kx);
-    b = vxz * (bx * kz);
-    c = vzx * (bz * kx);
-    d = vzz * (bz * kz);
+    kbx_x = bx * kx;
+    kbx_z = bx * kz;
+    kbz_x = bz * kx;
+    kbz_z = bz * kz;
   }
-  q4[0 * NSP + o] = a;
-  q4[1 * NSP + o] = b;
-  q4[2 * NSP + o] = c;
-  q4[3 * NSP + o] = d;
+#pragma unroll
+  for (int q = 0; q < kCellShots; ++q) {
+    const int s = s_lo + q;
+    if (s >= g.ns) break;
+    const int64_t o = (int64_t)s * PL + occ;
+    T ax, az;
+    vfs_adjoint(g, lv + VX * NSP, lv + VZ * NSP, i, j, o, ax, az);
+    const T vxx = sx * lvs[VX_X * NSP + o] + ax, vxz = sz * lvs[VX_Z * NSP + o] + ax;
+    const T vzx = sx * lvs[VZ_X * NSP + o] + az, vzz = sz * lvs[VZ_Z * NSP + o] + az;
+    lvs[VX_X * NSP + o] = vxx;
+    lvs[VX_Z * NSP + o] = vxz;
+    lvs[VZ_X * NSP + o] = vzx;
+    lvs[VZ_Z * NSP + o] = vzz;
+    q4[0 * NSP + o] = inside ? vxx * kbx_x : T(0);  // zero outside I
+    q4[1 * NSP + o] = inside ? vxz * kbx_z : T(0);
+    q4[2 * NSP + o] = inside ? vzx * kbz_x : T(0);
+    q4[3 * NSP + o] = inside ? vzz * kbz_z : T(0);
+  }
 }
 
 // (B2 + B1q) fused per cell and shot: the split stresses' lambda (adj_tfs_pml) and, from those
@@ -860,54 +910,58 @@ __global__ void adj_vfs_tq_pml(Geo<T> g, const T* __restrict__ cf, const T* __re
 template <typename T>
 __global__ void adj_tfs_vq_pml(Geo<T> g, const T* __restrict__ cf, const T* __restrict__ lt, T* lts,
                                T* __restrict__ q8) {
-  EL_CELL_SHOT
-  T azz, axz;
-  tfs_adjoint(g, lt + TZZ * NSP, lt + TXZ * NSP, i, o, azz, axz);
-  const T axx = lt[TXX * NSP + o];
+  EL_CELL_SHOTS
   const bool inside = in_I(g, i, j);
-  const int64_t c0 = g.L.off(i, j);
-  T sx = T(1), sz = T(1), ix = T(0), iz = T(0);
+  T sx = T(1), sz = T(1), kx = T(0), kz = T(0);
+  T c11 = T(0), c13 = T(0), c15 = T(0), c33 = T(0), c35 = T(0), c55 = T(0);
   if (inside) {
-    const Pml<T> p = pml_at(g, cf, c0, PL);
-    ix = T(1) / p.xd;
-    iz = T(1) / p.zd;
+    const Pml<T> p = pml_at(g, cf, occ, PL);
+    const T ix = T(1) / p.xd, iz = T(1) / p.zd;
     sx = p.xn * ix;
     sz = p.zn * iz;
-  }
-  T ls[6];
-  ls[0] = sx * lts[TXX_X * NSP + o] + axx;
-  ls[1] = sz * lts[TXX_Z * NSP + o] + axx;
-  ls[2] = sx * lts[TZZ_X * NSP + o] + azz;
-  ls[3] = sz * lts[TZZ_Z * NSP + o] + azz;
-  ls[4] = sx * lts[TXZ_X * NSP + o] + axz;
-  ls[5] = sz * lts[TXZ_Z * NSP + o] + axz;
-#pragma unroll
-  for (int k = 0; k < 6; ++k) lts[k * NSP + o] = ls[k];
-  T v[8];
-#pragma unroll
-  for (int k = 0; k < 8; ++k) v[k] = T(0);
-  if (inside) {
-    const T kx = g.dt_dx * ix, kz = g.dt_dz * iz;
-    StressQ<T> r;
-    r.a = ls[0] * kx;
-    r.b = ls[1] * kz;
-    r.c = ls[2] * kx;
-    r.d = ls[3] * kz;
-    r.e = ls[4] * kx;
-    r.f = ls[5] * kz;
-    const T c11 = cf[C11 * PL + c0], c13 = cf[C13 * PL + c0], c15 = cf[C15 * PL + c0];
-    const T c33 = cf[C33 * PL + c0], c35 = cf[C35 * PL + c0], c55 = cf[C55 * PL + c0];
-    v[0] = c11 * r.a + c13 * r.c;
-    v[1] = c15 * r.b + c35 * r.d;
-    v[2] = c15 * r.e;
-    v[3] = c55 * r.f;
-    v[4] = c15 * r.a + c35 * r.c;
-    v[5] = c13 * r.b + c33 * r.d;
-    v[6] = c55 * r.e;
-    v[7] = c35 * r.f;
+    kx = g.dt_dx * ix;
+    kz = g.dt_dz * iz;
+    c11 = cf[C11 * PL + occ];
+    c13 = cf[C13 * PL + occ];
+    c15 = cf[C15 * PL + occ];
+    c33 = cf[C33 * PL + occ];
+    c35 = cf[C35 * PL + occ];
+    c55 = cf[C55 * PL + occ];
   }
 #pragma unroll
-  for (int k = 0; k < 8; ++k) q8[k * NSP + o] = v[k];
+  for (int q = 0; q < kCellShots; ++q) {
+    const int s = s_lo + q;
+    if (s >= g.ns) break;
+    const int64_t o = (int64_t)s * PL + occ;
+    T azz, axz;
+    tfs_adjoint(g, lt + TZZ * NSP, lt + TXZ * NSP, i, o, azz, axz);
+    const T axx = lt[TXX * NSP + o];
+    T ls[6];
+    ls[0] = sx * lts[TXX_X * NSP + o] + axx;
+    ls[1] = sz * lts[TXX_Z * NSP + o] + axx;
+    ls[2] = sx * lts[TZZ_X * NSP + o] + azz;
+    ls[3] = sz * lts[TZZ_Z * NSP + o] + azz;
+    ls[4] = sx * lts[TXZ_X * NSP + o] + axz;
+    ls[5] = sz * lts[TXZ_Z * NSP + o] + axz;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) lts[k * NSP + o] = ls[k];
+    T v8[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) v8[k] = T(0);  // zero outside I
+    if (inside) {
+      const T ra = ls[0] * kx, rb = ls[1] * kz, rc = ls[2] * kx, rd = ls[3] * kz, re = ls[4] * kx, rf = ls[5] * kz;
+      v8[0] = c11 * ra + c13 * rc;
+      v8[1] = c15 * rb + c35 * rd;
+      v8[2] = c15 * re;
+      v8[3] = c55 * rf;
+      v8[4] = c15 * ra + c35 * rc;
+      v8[5] = c13 * rb + c33 * rd;
+      v8[6] = c55 * re;
+      v8[7] = c35 * rf;
+    }
+#pragma unroll
+    for (int k = 0; k < 8; ++k) q8[k * NSP + o] = v8[k];
+  }
 }
 
 // (B1a) lambda of the velocity totals at the start of the step (overwrite) and the C gradients.
@@ -1265,12 +1319,13 @@ void estep(const adfwi_elastic_plan* p, const el::Geo<T>& g, int it, const T* cf
   if (p->d.pml) {
     T* ts = st;
     T* vs = st + 6 * NSP;
-    ADFWI_LAUNCH(kElFwdStep, s, (el::stress_pml_tot<T, NN><<<gc, b, 0, s>>>(g, it, cf, vin, ts, tt, wav)));
+    const dim3 gcs = cells_grid(p, (p->d.ns + el::kCellShots - 1) / el::kCellShots);
+    ADFWI_LAUNCH(kElFwdStep, s, (el::stress_pml_tot<T, NN><<<gcs, b, 0, s>>>(g, it, cf, vin, ts, tt, wav)));
     if (p->d.free_surface) {
       const dim3 gfs((unsigned)((p->nxp + 127) / 128), p->d.ns, 3);
       ADFWI_LAUNCH(kElFwdStep, s, (el::stress_fs_rows_pml<T><<<gfs, 128, 0, s>>>(g, ts, tt)));
     }
-    ADFWI_LAUNCH(kElFwdStep, s, (el::vel_pml_tot<T, NN><<<gc, b, 0, s>>>(g, cf, tt, vs, vout)));
+    ADFWI_LAUNCH(kElFwdStep, s, (el::vel_pml_tot<T, NN><<<gcs, b, 0, s>>>(g, cf, tt, vs, vout)));
     if (p->d.free_surface) {
       const dim3 gfs((unsigned)((p->nxp + 127) / 128), p->d.ns, 2);
       ADFWI_LAUNCH(kElFwdStep, s, (el::vel_fs_rows_pml<T><<<gfs, 128, 0, s>>>(g, vs, vout)));
@@ -1416,6 +1471,7 @@ int ebackward(const adfwi_elastic_plan* p, const void* wavelet, const void* grec
     if (rc0) return rc0;
   }
   const dim3 gcs = cells_grid(p, ns), gcg = cells_grid(p, egroups(p)), b(256);
+  const dim3 gcm = cells_grid(p, (ns + el::kCellShots - 1) / el::kCellShots);
   const dim3 gcol((unsigned)((p->nxp + 127) / 128), ns);
   const dim3 ginj((unsigned)std::max(1, (p->ncells + 127) / 128), ns);
   const int nseg = full ? 1 : (nt + K - 1) / K;
@@ -1444,10 +1500,10 @@ int ebackward(const adfwi_elastic_plan* p, const void* wavelet, const void* grec
       if (p->d.pml) {
         ADFWI_CUDA_TRY(cudaMemsetAsync(lt, 0, 3 * NSP * sizeof(T), s));
         if (gr) ADFWI_LAUNCH(kAux, s, (el::adj_inject<T><<<ginj, 128, 0, s>>>(g, it, gr, lt, lv, 1)));
-        ADFWI_LAUNCH(kElAdjStep, s, (el::adj_vfs_tq_pml<T><<<gcs, b, 0, s>>>(g, cf, lv, lst + 6 * NSP, qsrc)));
+        ADFWI_LAUNCH(kElAdjStep, s, (el::adj_vfs_tq_pml<T><<<gcm, b, 0, s>>>(g, cf, lv, lst + 6 * NSP, qsrc)));
         ADFWI_LAUNCH(kElAdjStep, s, (el::adj_t_pml<T, NN><<<gcg, b, 0, s>>>(g, cf, lst + 6 * NSP, qsrc, lt, th, gcp,
                                                                             eg)));
-        ADFWI_LAUNCH(kElAdjStep, s, (el::adj_tfs_vq_pml<T><<<gcs, b, 0, s>>>(g, cf, lt, lst, qsrc)));
+        ADFWI_LAUNCH(kElAdjStep, s, (el::adj_tfs_vq_pml<T><<<gcm, b, 0, s>>>(g, cf, lt, lst, qsrc)));
         ADFWI_LAUNCH(kElAdjStep, s, (el::adj_v<T, NN, true><<<gcg, b, 0, s>>>(g, cf, lst, qsrc, lv, vh, gcp, eg)));
       } else {
         if (gr) ADFWI_LAUNCH(kAux, s, (el::adj_inject<T><<<ginj, 128, 0, s>>>(g, it, gr, lst, lv, 1)));

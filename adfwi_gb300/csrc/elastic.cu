@@ -135,10 +135,19 @@ __device__ __forceinline__ T dzb_t(const Geo<T>& g, const Q& q, int i, int j) {
   return r;
 }
 
+// The cell of this thread in the per-cell kernels: a block of 256 threads covers a tile of
+// 32 x 8 cells (full 128-byte rows of a plane; most rows that the vertical stencils read belong
+// to the same block, so they come from L1), tiles row-major over the padded grid.
+constexpr int kTileX = 32, kTileZ = 8, kTileThreads = kTileX * kTileZ;
+#define EL_TILE_IJ                                                                   \
+  const int tiles_x_ = (g.L.nxp + kTileX - 1) / kTileX;                              \
+  const int ti_ = (int)blockIdx.x / tiles_x_, tj_ = (int)blockIdx.x - ti_ * tiles_x_; \
+  const int i = ti_ * kTileZ + (int)threadIdx.x / kTileX;                            \
+  const int j = tj_ * kTileX + (int)threadIdx.x % kTileX;                            \
+  if (i >= g.L.nzp || j >= g.L.nxp) return;
+
 #define EL_CELL_SHOT                                                                 \
-  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;                  \
-  if (e >= (int64_t)g.L.nzp * g.L.nxp) return;                                      \
-  const int i = (int)(e / g.L.nxp), j = (int)(e - (int64_t)i * g.L.nxp);            \
+  EL_TILE_IJ                                                                         \
   const int s = blockIdx.y;                                                          \
   const int64_t PL = g.L.plane, NSP = (int64_t)g.ns * PL;                            \
   const int64_t o = (int64_t)s * PL + g.L.off(i, j);                                 \
@@ -152,9 +161,7 @@ __device__ __forceinline__ T dzb_t(const Geo<T>& g, const Q& q, int i, int j) {
 #endif
 constexpr int kCellShots = ADFWI_EL_CELL_SHOTS;
 #define EL_CELL_SHOTS                                                                \
-  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;                  \
-  if (e >= (int64_t)g.L.nzp * g.L.nxp) return;                                      \
-  const int i = (int)(e / g.L.nxp), j = (int)(e - (int64_t)i * g.L.nxp);            \
+  EL_TILE_IJ                                                                         \
   const int s_lo = blockIdx.y * kCellShots;                                          \
   const int64_t PL = g.L.plane, NSP = (int64_t)g.ns * PL;                            \
   const int64_t occ = g.L.off(i, j);
@@ -167,9 +174,7 @@ __device__ __forceinline__ T rdiv_pml(T x, T d) {
 }
 
 #define EL_CELL                                                                      \
-  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;                  \
-  if (e >= (int64_t)g.L.nzp * g.L.nxp) return;                                      \
-  const int i = (int)(e / g.L.nxp), j = (int)(e - (int64_t)i * g.L.nxp);            \
+  EL_TILE_IJ                                                                         \
   const int64_t PL = g.L.plane, NSP = (int64_t)g.ns * PL;                            \
   const int64_t oc = g.L.off(i, j);
 
@@ -737,7 +742,8 @@ __global__ void adj_tq(Geo<T> g, const T* __restrict__ cf, const T* __restrict__
 // (B3a) lt += transposes of the velocity update's stress differences; bx, bz gradients.
 template <typename T, int NN>
 __global__ void adj_t_pml(Geo<T> g, const T* __restrict__ cf, const T* __restrict__ lvs,
-                          const T* __restrict__ q4, T* lt, const T* __restrict__ tt_hist, T* gpart, int eg) {
+                          const T* __restrict__ q4, T* __restrict__ lt, const T* __restrict__ tt_hist,
+                          T* __restrict__ gpart, int eg) {
   EL_CELL
   EL_SHOT_GROUP
   T* gbx = gbase + 6 * PL;
@@ -969,7 +975,7 @@ __global__ void adj_tfs_vq_pml(Geo<T> g, const T* __restrict__ cf, const T* __re
 // and lv is accumulated instead of overwritten because v' = v + ...).
 template <typename T, int NN, bool PMLM>
 __global__ void adj_v(Geo<T> g, const T* __restrict__ cf, const T* __restrict__ lts, const T* __restrict__ q8,
-                      T* lv, const T* __restrict__ v_hist, T* gpart, int eg) {
+                      T* __restrict__ lv, const T* __restrict__ v_hist, T* __restrict__ gpart, int eg) {
   EL_CELL
   EL_SHOT_GROUP
   T* gc = gbase;
@@ -1283,8 +1289,10 @@ el::Geo<T> egeo(const adfwi_elastic_plan* p, const unsigned char* ws, const ECar
   return g;
 }
 
+// Blocks of the per-cell kernels (el::kTileThreads threads each): one per 32 x 8 tile.
 inline dim3 cells_grid(const adfwi_elastic_plan* p, int ns) {
-  return dim3((unsigned)(((int64_t)p->nzp * p->nxp + 255) / 256), ns);
+  const int64_t tiles = (int64_t)((p->nzp + el::kTileZ - 1) / el::kTileZ) * ((p->nxp + el::kTileX - 1) / el::kTileX);
+  return dim3((unsigned)tiles, ns);
 }
 
 template <typename T>
@@ -1314,7 +1322,7 @@ int esetup(const adfwi_elastic_plan* p, unsigned char* ws, const ECarve& c, cons
 template <typename T, int NN>
 void estep(const adfwi_elastic_plan* p, const el::Geo<T>& g, int it, const T* cf, const T* wav, T* st, T* tt,
            const T* vin, T* vout, cudaStream_t s) {
-  const dim3 gc = cells_grid(p, p->d.ns), b(256);
+  const dim3 gc = cells_grid(p, p->d.ns), b(el::kTileThreads);
   const int64_t NSP = (int64_t)p->d.ns * p->L.plane;
   if (p->d.pml) {
     T* ts = st;
@@ -1470,7 +1478,7 @@ int ebackward(const adfwi_elastic_plan* p, const void* wavelet, const void* grec
     if (!rc0 && p->d.pml) rc0 = zero_frames<T>(ht, (int64_t)K * 3 * ns, p->L, s);
     if (rc0) return rc0;
   }
-  const dim3 gcs = cells_grid(p, ns), gcg = cells_grid(p, egroups(p)), b(256);
+  const dim3 gcs = cells_grid(p, ns), gcg = cells_grid(p, egroups(p)), b(el::kTileThreads);
   const dim3 gcm = cells_grid(p, (ns + el::kCellShots - 1) / el::kCellShots);
   const dim3 gcol((unsigned)((p->nxp + 127) / 128), ns);
   const dim3 ginj((unsigned)std::max(1, (p->ncells + 127) / 128), ns);

@@ -91,20 +91,27 @@ __device__ __forceinline__ T dxb(const Geo<T>& g, const T* a, int64_t o) {
   return r;
 }
 template <int NN, typename T>
-__device__ __forceinline__ T dzf(const Geo<T>& g, const T* a, int64_t o) {
-  const int64_t P = g.L.pitch;
+__device__ __forceinline__ T dzf(const Geo<T>& g, const T* a, int64_t o, int64_t P) {
   T r = rmul(g.f0, rsub(a[o + P], a[o]));
   r = radd(r, rmul(g.f1, rsub(a[o + 2 * P], a[o - P])));
   if (NN == 3) r = radd(r, rmul(g.f2, rsub(a[o + 3 * P], a[o - 2 * P])));
   return r;
 }
 template <int NN, typename T>
-__device__ __forceinline__ T dzb(const Geo<T>& g, const T* a, int64_t o) {
-  const int64_t P = g.L.pitch;
+__device__ __forceinline__ T dzb(const Geo<T>& g, const T* a, int64_t o, int64_t P) {
   T r = rmul(g.f0, rsub(a[o], a[o - P]));
   r = radd(r, rmul(g.f1, rsub(a[o + P], a[o - 2 * P])));
   if (NN == 3) r = radd(r, rmul(g.f2, rsub(a[o + 2 * P], a[o - 3 * P])));
   return r;
+}
+// planes in global memory (row pitch of the layout)
+template <int NN, typename T>
+__device__ __forceinline__ T dzf(const Geo<T>& g, const T* a, int64_t o) {
+  return dzf<NN>(g, a, o, (int64_t)g.L.pitch);
+}
+template <int NN, typename T>
+__device__ __forceinline__ T dzb(const Geo<T>& g, const T* a, int64_t o) {
+  return dzb<NN>(g, a, o, (int64_t)g.L.pitch);
 }
 
 // ---- transposes in gather form: contribution to cell (i, j) of q placed at the cells that
@@ -184,6 +191,45 @@ __device__ __forceinline__ T rdiv_pml(T x, T d) {
 #define EL_SHOT_GROUP                                                                \
   const int s_beg = blockIdx.y * eg, s_end = min(g.ns, s_beg + eg);                  \
   T* gbase = gpart + (int64_t)blockIdx.y * 8 * PL;
+
+// Staging of the shot-group gradient kernels. Per shot, a block copies the 32 x 8 tile of every
+// plane it reads into shared memory with 16-byte asynchronous copies, with the halo its
+// stencils need (4 columns each side for x differences, 3 rows each side for z differences,
+// none for pointwise reads), then evaluates its cells there: each staged element is fetched
+// once per block instead of once per reading thread.
+constexpr int kSW = kTileX + 8;     // staged row: columns j0-4 .. j0+kTileX+3
+constexpr int kSZ = kTileZ + 6;     // staged rows: i0-3 .. i0+kTileZ+2
+constexpr int kSPlane = kSW * kSZ;  // elements of one staged plane
+constexpr int kSC = 3 * kSW + 4;    // staged index of the tile's cell (i0, j0)
+
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((unsigned)__cvta_generic_to_shared(dst)), "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// Queue the copies of rows i0-zh .. i0+kTileZ+zh-1 and columns j0-xh .. j0+kTileX+xh-1 (xh 0 or
+// 4, zh 0 or 3) of `plane` into the staged plane `dst`. Every copy starts on a 16-byte boundary
+// (j0 is a multiple of 32, rows are 128-byte multiples, the ghost frame is 4 columns wide), and
+// every row and column read lies in the plane's allocation: the layout keeps 4 ghost rows and
+// columns before the grid and a 16-row / 64-column margin after it.
+template <typename T>
+__device__ __forceinline__ void stage(T* dst, const T* plane, const Layout& L, int i0, int j0, int zh, int xh) {
+  constexpr int E = 16 / (int)sizeof(T);
+  const int cols = (kTileX + 2 * xh) / E, rows = kTileZ + 2 * zh;
+  for (int t = threadIdx.x; t < rows * cols; t += kTileThreads) {
+    const int r = t / cols, c = t - r * cols;
+    cp_async16(dst + (r - zh + 3) * kSW + (c * E - xh + 4), plane + L.off(i0 - zh + r, j0 - xh + c * E));
+  }
+}
+
+// A staged plane read at grid cells (ii, jj) of the block's tile.
+template <typename T>
+struct StagedQ {
+  const T* s;
+  int i0, j0;
+  __device__ __forceinline__ T operator()(int ii, int jj) const { return s[(ii - i0 + 3) * kSW + (jj - j0 + 4)]; }
+};
 
 // ======================================================================= forward, PML
 // Split stresses in I (elastic_kernels.py:351-356), then the moment-tensor source on both
@@ -740,38 +786,64 @@ __global__ void adj_tq(Geo<T> g, const T* __restrict__ cf, const T* __restrict__
 }
 
 // (B3a) lt += transposes of the velocity update's stress differences; bx, bz gradients.
+// Staged planes per shot: 0 q_vxx (x), 1 q_vxz (z), 2 q_vzx (x), 3 q_vzz (z), 4 txx (x),
+// 5 txz (x, z), 6 tzz (z) of the forward history, 7-10 lambda of the split velocities, 11-13 lt.
+constexpr int kAdjTPlanes = 14;
 template <typename T, int NN>
-__global__ void adj_t_pml(Geo<T> g, const T* __restrict__ cf, const T* __restrict__ lvs,
-                          const T* __restrict__ q4, T* __restrict__ lt, const T* __restrict__ tt_hist,
-                          T* __restrict__ gpart, int eg) {
-  EL_CELL
+__global__ void __launch_bounds__(kTileThreads)
+    adj_t_pml(Geo<T> g, const T* __restrict__ cf, const T* __restrict__ lvs, const T* __restrict__ q4,
+              T* __restrict__ lt, const T* __restrict__ tt_hist, T* __restrict__ gpart, int eg) {
+  extern __shared__ __align__(16) unsigned char el_smem[];
+  T* sm = reinterpret_cast<T*>(el_smem);
+  const int tiles_x = (g.L.nxp + kTileX - 1) / kTileX;
+  const int i0 = ((int)blockIdx.x / tiles_x) * kTileZ, j0 = ((int)blockIdx.x % tiles_x) * kTileX;
+  const int ty = (int)threadIdx.x / kTileX, tx = (int)threadIdx.x % kTileX;
+  const int i = i0 + ty, j = j0 + tx;
+  const bool valid = i < g.L.nzp && j < g.L.nxp, inside = valid && in_I(g, i, j);
+  const int64_t PL = g.L.plane, NSP = (int64_t)g.ns * PL, oc = g.L.off(i, j);
+  const int sc = kSC + ty * kSW + tx;  // this cell in a staged plane
   EL_SHOT_GROUP
   T* gbx = gbase + 6 * PL;
   T* gbz = gbase + 7 * PL;
-  T gx = T(0), gz = T(0);
-  const bool inside = in_I(g, i, j);
   // d(v_x')/d(bx) = dt * D(T) / (d * pml_d), likewise for bz: the cell's factors dt / (d pml_d)
-  T kx = T(0), kz = T(0);
+  T kx = T(0), kz = T(0), gx = T(0), gz = T(0);
   if (inside) {
     const Pml<T> p = pml_at(g, cf, oc, PL);
     kx = g.dt / (g.dx * p.xd);
     kz = g.dt / (g.dz * p.zd);
   }
+  const StagedQ<T> q_vxx{sm, i0, j0}, q_vxz{sm + kSPlane, i0, j0};
+  const StagedQ<T> q_vzx{sm + 2 * kSPlane, i0, j0}, q_vzz{sm + 3 * kSPlane, i0, j0};
   for (int s = s_beg; s < s_end; ++s) {
     const int64_t so = (int64_t)s * PL;
-    const PlaneQ<T> q_vxx{q4 + 0 * NSP + so, g.L}, q_vxz{q4 + 1 * NSP + so, g.L};
-    const PlaneQ<T> q_vzx{q4 + 2 * NSP + so, g.L}, q_vzz{q4 + 3 * NSP + so, g.L};
-    const int64_t o = so + oc;
-    lt[TXX * NSP + o] += dxf_t<NN>(g, q_vxx, i, j);
-    lt[TXZ * NSP + o] += dzb_t<NN>(g, q_vxz, i, j) + dxb_t<NN>(g, q_vzx, i, j);
-    lt[TZZ * NSP + o] += dzf_t<NN>(g, q_vzz, i, j);
-    if (inside) {
-      const T* th = tt_hist;
-      gx += lvs[VX_X * NSP + o] * dxf<NN>(g, th + TXX * NSP, o) * kx +
-            lvs[VX_Z * NSP + o] * dzb<NN>(g, th + TXZ * NSP, o) * kz;
-      gz += lvs[VZ_X * NSP + o] * dxb<NN>(g, th + TXZ * NSP, o) * kx +
-            lvs[VZ_Z * NSP + o] * dzf<NN>(g, th + TZZ * NSP, o) * kz;
+    stage(sm, q4 + so, g.L, i0, j0, 0, 4);
+    stage(sm + kSPlane, q4 + NSP + so, g.L, i0, j0, 3, 0);
+    stage(sm + 2 * kSPlane, q4 + 2 * NSP + so, g.L, i0, j0, 0, 4);
+    stage(sm + 3 * kSPlane, q4 + 3 * NSP + so, g.L, i0, j0, 3, 0);
+    stage(sm + 4 * kSPlane, tt_hist + TXX * NSP + so, g.L, i0, j0, 0, 4);
+    stage(sm + 5 * kSPlane, tt_hist + TXZ * NSP + so, g.L, i0, j0, 3, 4);
+    stage(sm + 6 * kSPlane, tt_hist + TZZ * NSP + so, g.L, i0, j0, 3, 0);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) stage(sm + (7 + k) * kSPlane, lvs + k * NSP + so, g.L, i0, j0, 0, 0);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) stage(sm + (11 + k) * kSPlane, lt + k * NSP + so, g.L, i0, j0, 0, 0);
+    cp_async_wait_all();
+    __syncthreads();
+    if (valid) {
+      const int64_t o = so + oc;
+      const T* l0 = sm + 11 * kSPlane + sc;
+      lt[TXX * NSP + o] = l0[TXX * kSPlane] + dxf_t<NN>(g, q_vxx, i, j);
+      lt[TXZ * NSP + o] = l0[TXZ * kSPlane] + (dzb_t<NN>(g, q_vxz, i, j) + dxb_t<NN>(g, q_vzx, i, j));
+      lt[TZZ * NSP + o] = l0[TZZ * kSPlane] + dzf_t<NN>(g, q_vzz, i, j);
+      if (inside) {
+        const T* lv = sm + 7 * kSPlane + sc;
+        gx += lv[VX_X * kSPlane] * dxf<NN>(g, sm + 4 * kSPlane, sc) * kx +
+              lv[VX_Z * kSPlane] * dzb<NN>(g, sm + 5 * kSPlane, sc, kSW) * kz;
+        gz += lv[VZ_X * kSPlane] * dxb<NN>(g, sm + 5 * kSPlane, sc) * kx +
+              lv[VZ_Z * kSPlane] * dzf<NN>(g, sm + 6 * kSPlane, sc, kSW) * kz;
+      }
     }
+    __syncthreads();  // the next shot's copies overwrite the staged planes
   }
   if (inside) {
     gbx[oc] += gx;
@@ -973,49 +1045,74 @@ __global__ void adj_tfs_vq_pml(Geo<T> g, const T* __restrict__ cf, const T* __re
 // (B1a) lambda of the velocity totals at the start of the step (overwrite) and the C gradients.
 // pml = 1: split-field update; pml = 0: absorbing-layer update (lts then holds txx, tzz, txz,
 // and lv is accumulated instead of overwritten because v' = v + ...).
+// Staged planes per shot: 0-7 the stress update's adjoint sources (sx_b x, sx_zb z, sx_f x,
+// sx_zf z, sz_b x, sz_zb z, sz_f x, sz_zf z), 8-9 vx, vz of the forward history (x, z),
+// 10.. lambda of the (split) stresses (6 with the PML, 3 without).
+template <bool PMLM>
+constexpr int adj_v_planes() {
+  return PMLM ? 16 : 13;
+}
 template <typename T, int NN, bool PMLM>
-__global__ void adj_v(Geo<T> g, const T* __restrict__ cf, const T* __restrict__ lts, const T* __restrict__ q8,
-                      T* __restrict__ lv, const T* __restrict__ v_hist, T* __restrict__ gpart, int eg) {
-  EL_CELL
+__global__ void __launch_bounds__(kTileThreads)
+    adj_v(Geo<T> g, const T* __restrict__ cf, const T* __restrict__ lts, const T* __restrict__ q8,
+          T* __restrict__ lv, const T* __restrict__ v_hist, T* __restrict__ gpart, int eg) {
+  extern __shared__ __align__(16) unsigned char el_smem[];
+  T* sm = reinterpret_cast<T*>(el_smem);
+  const int tiles_x = (g.L.nxp + kTileX - 1) / kTileX;
+  const int i0 = ((int)blockIdx.x / tiles_x) * kTileZ, j0 = ((int)blockIdx.x % tiles_x) * kTileX;
+  const int ty = (int)threadIdx.x / kTileX, tx = (int)threadIdx.x % kTileX;
+  const int i = i0 + ty, j = j0 + tx;
+  const bool valid = i < g.L.nzp && j < g.L.nxp, inside = valid && in_I(g, i, j);
+  const int64_t PL = g.L.plane, NSP = (int64_t)g.ns * PL, oc = g.L.off(i, j);
+  const int sc = kSC + ty * kSW + tx;
   EL_SHOT_GROUP
   T* gc = gbase;
   T g11 = T(0), g13 = T(0), g15 = T(0), g33 = T(0), g35 = T(0), g55 = T(0);
-  const bool inside = in_I(g, i, j);
   T kx = T(0), kz = T(0);
   if (inside) stress_k<T, PMLM>(g, cf, oc, PL, kx, kz);
+  constexpr int nst = PMLM ? 6 : 3;
   for (int s = s_beg; s < s_end; ++s) {
     const int64_t so = (int64_t)s * PL;
-    const PlaneQ<T> sx_b{q8 + 0 * NSP + so, g.L}, sx_zb{q8 + 1 * NSP + so, g.L};
-    const PlaneQ<T> sx_f{q8 + 2 * NSP + so, g.L}, sx_zf{q8 + 3 * NSP + so, g.L};
-    const PlaneQ<T> sz_b{q8 + 4 * NSP + so, g.L}, sz_zb{q8 + 5 * NSP + so, g.L};
-    const PlaneQ<T> sz_f{q8 + 6 * NSP + so, g.L}, sz_zf{q8 + 7 * NSP + so, g.L};
-    const T avx = dxb_t<NN>(g, sx_b, i, j) + dzb_t<NN>(g, sx_zb, i, j) + dxf_t<NN>(g, sx_f, i, j) +
-                  dzf_t<NN>(g, sx_zf, i, j);
-    const T avz = dxb_t<NN>(g, sz_b, i, j) + dzb_t<NN>(g, sz_zb, i, j) + dxf_t<NN>(g, sz_f, i, j) +
-                  dzf_t<NN>(g, sz_zf, i, j);
-    const int64_t o = so + oc;
-    if (PMLM) {
-      lv[VX * NSP + o] = avx;
-      lv[VZ * NSP + o] = avz;
-    } else {
-      lv[VX * NSP + o] += avx;
-      lv[VZ * NSP + o] += avz;
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+      stage(sm + k * kSPlane, q8 + k * NSP + so, g.L, i0, j0, (k & 1) ? 3 : 0, (k & 1) ? 0 : 4);
+    stage(sm + 8 * kSPlane, v_hist + VX * NSP + so, g.L, i0, j0, 3, 4);
+    stage(sm + 9 * kSPlane, v_hist + VZ * NSP + so, g.L, i0, j0, 3, 4);
+#pragma unroll
+    for (int k = 0; k < nst; ++k) stage(sm + (10 + k) * kSPlane, lts + k * NSP + so, g.L, i0, j0, 0, 0);
+    cp_async_wait_all();
+    __syncthreads();
+    if (valid) {
+      const StagedQ<T> q0{sm, i0, j0}, q1{sm + kSPlane, i0, j0}, q2{sm + 2 * kSPlane, i0, j0},
+          q3{sm + 3 * kSPlane, i0, j0}, q4{sm + 4 * kSPlane, i0, j0}, q5{sm + 5 * kSPlane, i0, j0},
+          q6{sm + 6 * kSPlane, i0, j0}, q7{sm + 7 * kSPlane, i0, j0};
+      const T avx = dxb_t<NN>(g, q0, i, j) + dzb_t<NN>(g, q1, i, j) + dxf_t<NN>(g, q2, i, j) + dzf_t<NN>(g, q3, i, j);
+      const T avz = dxb_t<NN>(g, q4, i, j) + dzb_t<NN>(g, q5, i, j) + dxf_t<NN>(g, q6, i, j) + dzf_t<NN>(g, q7, i, j);
+      const int64_t o = so + oc;
+      if (PMLM) {
+        lv[VX * NSP + o] = avx;
+        lv[VZ * NSP + o] = avz;
+      } else {
+        lv[VX * NSP + o] += avx;
+        lv[VZ * NSP + o] += avz;
+      }
+      if (inside) {
+        const StressQ<T> r = stress_q<T, PMLM>(sm + 10 * kSPlane + sc, 0, kSPlane, kx, kz);
+        const T* vx = sm + 8 * kSPlane;
+        const T* vz = sm + 9 * kSPlane;
+        const T dxb_vx = dxb<NN>(g, vx, sc), dxb_vz = dxb<NN>(g, vz, sc);
+        const T dzb_vx = dzb<NN>(g, vx, sc, kSW), dzb_vz = dzb<NN>(g, vz, sc, kSW);
+        const T dxf_vx = dxf<NN>(g, vx, sc), dxf_vz = dxf<NN>(g, vz, sc);
+        const T dzf_vx = dzf<NN>(g, vx, sc, kSW), dzf_vz = dzf<NN>(g, vz, sc, kSW);
+        g11 += r.a * dxb_vx;
+        g13 += r.b * dzb_vz + r.c * dxb_vx;
+        g15 += r.a * dxb_vz + r.b * dzb_vx + r.e * dxf_vx;
+        g33 += r.d * dzb_vz;
+        g35 += r.c * dxb_vz + r.d * dzb_vx + r.f * dzf_vz;
+        g55 += r.e * dxf_vz + r.f * dzf_vx;
+      }
     }
-    if (inside) {
-      const StressQ<T> r = stress_q<T, PMLM>(lts, o, NSP, kx, kz);
-      const T* vx = v_hist + VX * NSP;
-      const T* vz = v_hist + VZ * NSP;
-      const T dxb_vx = dxb<NN>(g, vx, o), dxb_vz = dxb<NN>(g, vz, o);
-      const T dzb_vx = dzb<NN>(g, vx, o), dzb_vz = dzb<NN>(g, vz, o);
-      const T dxf_vx = dxf<NN>(g, vx, o), dxf_vz = dxf<NN>(g, vz, o);
-      const T dzf_vx = dzf<NN>(g, vx, o), dzf_vz = dzf<NN>(g, vz, o);
-      g11 += r.a * dxb_vx;
-      g13 += r.b * dzb_vz + r.c * dxb_vx;
-      g15 += r.a * dxb_vz + r.b * dzb_vx + r.e * dxf_vx;
-      g33 += r.d * dzb_vz;
-      g35 += r.c * dxb_vz + r.d * dzb_vx + r.f * dzf_vz;
-      g55 += r.e * dxf_vz + r.f * dzf_vx;
-    }
+    __syncthreads();  // the next shot's copies overwrite the staged planes
   }
   if (inside) {
     gc[C11 * PL + oc] += g11;
@@ -1480,6 +1577,13 @@ int ebackward(const adfwi_elastic_plan* p, const void* wavelet, const void* grec
   }
   const dim3 gcs = cells_grid(p, ns), gcg = cells_grid(p, egroups(p)), b(el::kTileThreads);
   const dim3 gcm = cells_grid(p, (ns + el::kCellShots - 1) / el::kCellShots);
+  // shared memory of the staged gradient kernels (above the 48 KB default in double precision)
+  const int smem_t = el::kAdjTPlanes * el::kSPlane * (int)sizeof(T);
+  const int smem_vp = el::adj_v_planes<true>() * el::kSPlane * (int)sizeof(T);
+  const int smem_va = el::adj_v_planes<false>() * el::kSPlane * (int)sizeof(T);
+  ADFWI_CUDA_TRY(cudaFuncSetAttribute(el::adj_t_pml<T, NN>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_t));
+  ADFWI_CUDA_TRY(cudaFuncSetAttribute(el::adj_v<T, NN, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_vp));
+  ADFWI_CUDA_TRY(cudaFuncSetAttribute(el::adj_v<T, NN, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_va));
   const dim3 gcol((unsigned)((p->nxp + 127) / 128), ns);
   const dim3 ginj((unsigned)std::max(1, (p->ncells + 127) / 128), ns);
   const int nseg = full ? 1 : (nt + K - 1) / K;
@@ -1509,10 +1613,10 @@ int ebackward(const adfwi_elastic_plan* p, const void* wavelet, const void* grec
         ADFWI_CUDA_TRY(cudaMemsetAsync(lt, 0, 3 * NSP * sizeof(T), s));
         if (gr) ADFWI_LAUNCH(kAux, s, (el::adj_inject<T><<<ginj, 128, 0, s>>>(g, it, gr, lt, lv, 1)));
         ADFWI_LAUNCH(kElAdjStep, s, (el::adj_vfs_tq_pml<T><<<gcm, b, 0, s>>>(g, cf, lv, lst + 6 * NSP, qsrc)));
-        ADFWI_LAUNCH(kElAdjStep, s, (el::adj_t_pml<T, NN><<<gcg, b, 0, s>>>(g, cf, lst + 6 * NSP, qsrc, lt, th, gcp,
-                                                                            eg)));
+        ADFWI_LAUNCH(kElAdjStep, s, (el::adj_t_pml<T, NN><<<gcg, b, smem_t, s>>>(g, cf, lst + 6 * NSP, qsrc, lt, th,
+                                                                                 gcp, eg)));
         ADFWI_LAUNCH(kElAdjStep, s, (el::adj_tfs_vq_pml<T><<<gcm, b, 0, s>>>(g, cf, lt, lst, qsrc)));
-        ADFWI_LAUNCH(kElAdjStep, s, (el::adj_v<T, NN, true><<<gcg, b, 0, s>>>(g, cf, lst, qsrc, lv, vh, gcp, eg)));
+        ADFWI_LAUNCH(kElAdjStep, s, (el::adj_v<T, NN, true><<<gcg, b, smem_vp, s>>>(g, cf, lst, qsrc, lv, vh, gcp, eg)));
       } else {
         if (gr) ADFWI_LAUNCH(kAux, s, (el::adj_inject<T><<<ginj, 128, 0, s>>>(g, it, gr, lst, lv, 1)));
         ADFWI_LAUNCH(kElAdjStep, s, (el::adj_vfs_abl<T><<<gcs, b, 0, s>>>(g, cf, lv, lv2, nullptr)));
@@ -1521,7 +1625,7 @@ int ebackward(const adfwi_elastic_plan* p, const void* wavelet, const void* grec
         ADFWI_LAUNCH(kElAdjStep, s, (el::adj_t_abl<T, NN><<<gcg, b, 0, s>>>(g, cf, lv, qsrc, lst, th, gcp, eg)));
         if (p->d.free_surface) ADFWI_LAUNCH(kElAdjStep, s, (el::adj_tfs_abl<T><<<gcol, 128, 0, s>>>(g, lst)));
         ADFWI_LAUNCH(kElAdjStep, s, (el::adj_vq<T, false><<<gcs, b, 0, s>>>(g, cf, lst, qsrc)));
-        ADFWI_LAUNCH(kElAdjStep, s, (el::adj_v<T, NN, false><<<gcg, b, 0, s>>>(g, cf, lst, qsrc, lv, vh, gcp, eg)));
+        ADFWI_LAUNCH(kElAdjStep, s, (el::adj_v<T, NN, false><<<gcg, b, smem_va, s>>>(g, cf, lst, qsrc, lv, vh, gcp, eg)));
       }
     }
     ADFWI_CUDA_TRY(cudaGetLastError());

@@ -79,6 +79,35 @@ struct PinnedBytes {
   bool assign(const void* src, size_t n);
 };
 
+// Programmatic dependent launch. A step kernel is launched with programmatic stream
+// serialisation, so its blocks may become resident while the previous step kernel's last
+// blocks still run: every block signals at once that the next launch may start
+// (launch_dependents), and waits for the previous grid's completion and memory (wait)
+// before its first read of the fields and its first write of anything. In a kernel launched
+// without the attribute both are no-ops.
+__device__ __forceinline__ void griddep_launch_dependents() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+__device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+// Host: launch `kernel` with programmatic stream serialisation (the kernel must call
+// griddep_wait() before it touches data of the previous launch on the stream).
+template <typename... KArgs, typename... Args>
+cudaError_t launch_pdl_kernel(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                              Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, static_cast<Args&&>(args)...);
+}
+
 }  // namespace adfwi
 
 #define ADFWI_CUDA_TRY(expr)                                                      \

@@ -351,6 +351,8 @@ __device__ __forceinline__ bool vel_fs_row(const Geo<T>& g, int i, int j) {
 template <typename T, int NN>
 __global__ void stress_pml_tot(Geo<T> g, int it, const T* __restrict__ cf, const T* __restrict__ v,
                                T* __restrict__ ts, T* __restrict__ tt, const T* __restrict__ wav) {
+  griddep_wait();  // launched with programmatic serialisation in the PML time loops
+  griddep_launch_dependents();
   EL_CELL_SHOTS
   const bool inside = in_I(g, i, j);
   T pxn = T(0), pzn = T(0), pxi = T(0), pzi = T(0);
@@ -414,6 +416,8 @@ __global__ void stress_pml_tot(Geo<T> g, int it, const T* __restrict__ cf, const
 // Stress totals of the free-surface rows h-3 .. h-1 (elastic_kernels.py:375-384).
 template <typename T>
 __global__ void stress_fs_rows_pml(Geo<T> g, const T* __restrict__ ts, T* __restrict__ tt) {
+  griddep_wait();  // launched with programmatic serialisation in the PML time loops
+  griddep_launch_dependents();
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= g.L.nxp) return;
   const int i = g.h - 3 + (int)blockIdx.z, s = blockIdx.y;
@@ -434,6 +438,8 @@ __global__ void stress_fs_rows_pml(Geo<T> g, const T* __restrict__ ts, T* __rest
 template <typename T, int NN>
 __global__ void vel_pml_tot(Geo<T> g, const T* __restrict__ cf, const T* __restrict__ tt, T* __restrict__ vs,
                             T* __restrict__ v) {
+  griddep_wait();  // launched with programmatic serialisation in the PML time loops
+  griddep_launch_dependents();
   EL_CELL_SHOTS
   const bool inside = in_I(g, i, j);
   T pxd = T(1), pxn = T(0), pzd = T(1), pzn = T(0), dbx = T(0), dbz = T(0);
@@ -477,6 +483,8 @@ __global__ void vel_pml_tot(Geo<T> g, const T* __restrict__ cf, const T* __restr
 // split velocities of all rows.
 template <typename T>
 __global__ void vel_fs_rows_pml(Geo<T> g, const T* __restrict__ vs, T* __restrict__ v) {
+  griddep_wait();  // launched with programmatic serialisation in the PML time loops
+  griddep_launch_dependents();
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j < g.jlo || j > g.jhi || j >= g.L.nxp) return;
   const int i = g.h - 3 + (int)blockIdx.z, s = blockIdx.y;
@@ -593,6 +601,8 @@ __global__ void damp_v(Geo<T> g, const T* __restrict__ cf, T* __restrict__ v) {
 // Receivers: txx, tzz, txz, vx, vz totals at each receiver (elastic_kernels.py:407-411).
 template <typename T>
 __global__ void record(Geo<T> g, int it, const T* __restrict__ tt, const T* __restrict__ v, T* rec) {
+  griddep_wait();  // launched with programmatic serialisation in the PML time loops
+  griddep_launch_dependents();
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= g.nr) return;
   const int s = blockIdx.y;
@@ -630,7 +640,9 @@ __global__ void energy(Geo<T> g, const T* __restrict__ tt, const T* __restrict__
 // Receiver residuals of step `it` into the adjoint stress totals lt (overwritten: zero + injection)
 // and added to the adjoint velocity totals lv. One thread per (unique receiver cell, shot).
 template <typename T>
-__global__ void adj_inject(Geo<T> g, int it, const T* __restrict__ grec, T* lt, T* lv, int write_lt) {
+__global__ void adj_inject(Geo<T> g, int it, const T* __restrict__ grec, T* lt, T* lv, int parts) {
+  griddep_wait();  // launched with programmatic serialisation in the PML time loops
+  griddep_launch_dependents();
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= g.ncells) return;
   const int s = blockIdx.y;
@@ -644,13 +656,15 @@ __global__ void adj_inject(Geo<T> g, int it, const T* __restrict__ grec, T* lt, 
     const int64_t qq = base + g.ucell_rcv[m];
     for (int c = 0; c < 5; ++c) a[c] += grec[c * RS + qq];
   }
-  if (write_lt) {
+  if (parts & 2) {  // stresses
     lt[TXX * NSP + o] += a[0];
     lt[TZZ * NSP + o] += a[1];
     lt[TXZ * NSP + o] += a[2];
   }
-  lv[VX * NSP + o] += a[3];
-  lv[VZ * NSP + o] += a[4];
+  if (parts & 1) {  // velocities
+    lv[VX * NSP + o] += a[3];
+    lv[VZ * NSP + o] += a[4];
+  }
 }
 
 // Adjoint of the free-surface velocity rows: lambda of the velocity totals BEFORE the rows
@@ -785,14 +799,17 @@ __global__ void adj_tq(Geo<T> g, const T* __restrict__ cf, const T* __restrict__
   q4[3 * NSP + o] = d;
 }
 
-// (B3a) lt += transposes of the velocity update's stress differences; bx, bz gradients.
+// (B3a) lt = transposes of the velocity update's stress differences (the dL/d stress records
+// of the step are added after it, by adj_inject); bx, bz gradients.
 // Staged planes per shot: 0 q_vxx (x), 1 q_vxz (z), 2 q_vzx (x), 3 q_vzz (z), 4 txx (x),
-// 5 txz (x, z), 6 tzz (z) of the forward history, 7-10 lambda of the split velocities, 11-13 lt.
-constexpr int kAdjTPlanes = 14;
+// 5 txz (x, z), 6 tzz (z) of the forward history, 7-10 lambda of the split velocities.
+constexpr int kAdjTPlanes = 11;
 template <typename T, int NN>
 __global__ void __launch_bounds__(kTileThreads)
     adj_t_pml(Geo<T> g, const T* __restrict__ cf, const T* __restrict__ lvs, const T* __restrict__ q4,
               T* __restrict__ lt, const T* __restrict__ tt_hist, T* __restrict__ gpart, int eg) {
+  griddep_wait();  // launched with programmatic serialisation in the PML time loops
+  griddep_launch_dependents();
   extern __shared__ __align__(16) unsigned char el_smem[];
   T* sm = reinterpret_cast<T*>(el_smem);
   const int tiles_x = (g.L.nxp + kTileX - 1) / kTileX;
@@ -825,16 +842,13 @@ __global__ void __launch_bounds__(kTileThreads)
     stage(sm + 6 * kSPlane, tt_hist + TZZ * NSP + so, g.L, i0, j0, 3, 0);
 #pragma unroll
     for (int k = 0; k < 4; ++k) stage(sm + (7 + k) * kSPlane, lvs + k * NSP + so, g.L, i0, j0, 0, 0);
-#pragma unroll
-    for (int k = 0; k < 3; ++k) stage(sm + (11 + k) * kSPlane, lt + k * NSP + so, g.L, i0, j0, 0, 0);
     cp_async_wait_all();
     __syncthreads();
     if (valid) {
       const int64_t o = so + oc;
-      const T* l0 = sm + 11 * kSPlane + sc;
-      lt[TXX * NSP + o] = l0[TXX * kSPlane] + dxf_t<NN>(g, q_vxx, i, j);
-      lt[TXZ * NSP + o] = l0[TXZ * kSPlane] + (dzb_t<NN>(g, q_vxz, i, j) + dxb_t<NN>(g, q_vzx, i, j));
-      lt[TZZ * NSP + o] = l0[TZZ * kSPlane] + dzf_t<NN>(g, q_vzz, i, j);
+      lt[TXX * NSP + o] = dxf_t<NN>(g, q_vxx, i, j);
+      lt[TXZ * NSP + o] = dzb_t<NN>(g, q_vxz, i, j) + dxb_t<NN>(g, q_vzx, i, j);
+      lt[TZZ * NSP + o] = dzf_t<NN>(g, q_vzz, i, j);
       if (inside) {
         const T* lv = sm + 7 * kSPlane + sc;
         gx += lv[VX_X * kSPlane] * dxf<NN>(g, sm + 4 * kSPlane, sc) * kx +
@@ -948,6 +962,8 @@ __global__ void adj_vq(Geo<T> g, const T* __restrict__ cf, const T* __restrict__
 template <typename T>
 __global__ void adj_vfs_tq_pml(Geo<T> g, const T* __restrict__ cf, const T* __restrict__ lv, T* lvs,
                                T* __restrict__ q4) {
+  griddep_wait();  // launched with programmatic serialisation in the PML time loops
+  griddep_launch_dependents();
   EL_CELL_SHOTS
   const bool inside = in_I(g, i, j);
   T sx = T(1), sz = T(1), kbx_x = T(0), kbx_z = T(0), kbz_x = T(0), kbz_z = T(0);
@@ -988,6 +1004,8 @@ __global__ void adj_vfs_tq_pml(Geo<T> g, const T* __restrict__ cf, const T* __re
 template <typename T>
 __global__ void adj_tfs_vq_pml(Geo<T> g, const T* __restrict__ cf, const T* __restrict__ lt, T* lts,
                                T* __restrict__ q8) {
+  griddep_wait();  // launched with programmatic serialisation in the PML time loops
+  griddep_launch_dependents();
   EL_CELL_SHOTS
   const bool inside = in_I(g, i, j);
   T sx = T(1), sz = T(1), kx = T(0), kz = T(0);
@@ -1056,6 +1074,8 @@ template <typename T, int NN, bool PMLM>
 __global__ void __launch_bounds__(kTileThreads)
     adj_v(Geo<T> g, const T* __restrict__ cf, const T* __restrict__ lts, const T* __restrict__ q8,
           T* __restrict__ lv, const T* __restrict__ v_hist, T* __restrict__ gpart, int eg) {
+  griddep_wait();  // launched with programmatic serialisation in the PML time loops
+  griddep_launch_dependents();
   extern __shared__ __align__(16) unsigned char el_smem[];
   T* sm = reinterpret_cast<T*>(el_smem);
   const int tiles_x = (g.L.nxp + kTileX - 1) / kTileX;
@@ -1425,15 +1445,16 @@ void estep(const adfwi_elastic_plan* p, const el::Geo<T>& g, int it, const T* cf
     T* ts = st;
     T* vs = st + 6 * NSP;
     const dim3 gcs = cells_grid(p, (p->d.ns + el::kCellShots - 1) / el::kCellShots);
-    ADFWI_LAUNCH(kElFwdStep, s, (el::stress_pml_tot<T, NN><<<gcs, b, 0, s>>>(g, it, cf, vin, ts, tt, wav)));
+    // programmatically serialised launches: each kernel waits for the previous one's data
+    ADFWI_LAUNCH(kElFwdStep, s, (void)launch_pdl_kernel(el::stress_pml_tot<T, NN>, gcs, b, 0, s, g, it, cf, vin, ts, tt, wav));
     if (p->d.free_surface) {
       const dim3 gfs((unsigned)((p->nxp + 127) / 128), p->d.ns, 3);
-      ADFWI_LAUNCH(kElFwdStep, s, (el::stress_fs_rows_pml<T><<<gfs, 128, 0, s>>>(g, ts, tt)));
+      ADFWI_LAUNCH(kElFwdStep, s, (void)launch_pdl_kernel(el::stress_fs_rows_pml<T>, gfs, dim3(128), 0, s, g, ts, tt));
     }
-    ADFWI_LAUNCH(kElFwdStep, s, (el::vel_pml_tot<T, NN><<<gcs, b, 0, s>>>(g, cf, tt, vs, vout)));
+    ADFWI_LAUNCH(kElFwdStep, s, (void)launch_pdl_kernel(el::vel_pml_tot<T, NN>, gcs, b, 0, s, g, cf, tt, vs, vout));
     if (p->d.free_surface) {
       const dim3 gfs((unsigned)((p->nxp + 127) / 128), p->d.ns, 2);
-      ADFWI_LAUNCH(kElFwdStep, s, (el::vel_fs_rows_pml<T><<<gfs, 128, 0, s>>>(g, vs, vout)));
+      ADFWI_LAUNCH(kElFwdStep, s, (void)launch_pdl_kernel(el::vel_fs_rows_pml<T>, gfs, dim3(128), 0, s, g, vs, vout));
     }
   } else {
     // ABL: stresses live in `tt`, velocities in place in vin (== vout)
@@ -1518,7 +1539,8 @@ int eforward(const adfwi_elastic_plan* p, const void* const* coef, const int32_t
     }
     if (rec && p->d.nr > 0) {
       dim3 gr((unsigned)((p->d.nr + 127) / 128), p->d.ns);
-      ADFWI_LAUNCH(kAux, s, (el::record<T><<<gr, 128, 0, s>>>(g, it, tt, vout, static_cast<T*>(rec))));
+      ADFWI_LAUNCH(kAux, s, (void)launch_pdl_kernel(el::record<T>, gr, dim3(128), 0, s, g, it, (const T*)tt, (const T*)vout,
+                                                    static_cast<T*>(rec)));
     }
     if (fw && chunk < p->chunk_end.size() && it == p->chunk_end[chunk]) {
       const int64_t n = (int64_t)p->d.nz * p->d.nx;
@@ -1610,15 +1632,18 @@ int ebackward(const adfwi_elastic_plan* p, const void* wavelet, const void* grec
       const T* vh = hv + (int64_t)k * 2 * NSP;  // velocity totals at the start of step it
       const T* th = ht + (int64_t)k * 3 * NSP;  // stress totals of step it
       if (p->d.pml) {
-        ADFWI_CUDA_TRY(cudaMemsetAsync(lt, 0, 3 * NSP * sizeof(T), s));
-        if (gr) ADFWI_LAUNCH(kAux, s, (el::adj_inject<T><<<ginj, 128, 0, s>>>(g, it, gr, lt, lv, 1)));
-        ADFWI_LAUNCH(kElAdjStep, s, (el::adj_vfs_tq_pml<T><<<gcm, b, 0, s>>>(g, cf, lv, lst + 6 * NSP, qsrc)));
-        ADFWI_LAUNCH(kElAdjStep, s, (el::adj_t_pml<T, NN><<<gcg, b, smem_t, s>>>(g, cf, lst + 6 * NSP, qsrc, lt, th,
-                                                                                 gcp, eg)));
-        ADFWI_LAUNCH(kElAdjStep, s, (el::adj_tfs_vq_pml<T><<<gcm, b, 0, s>>>(g, cf, lt, lst, qsrc)));
-        ADFWI_LAUNCH(kElAdjStep, s, (el::adj_v<T, NN, true><<<gcg, b, smem_vp, s>>>(g, cf, lst, qsrc, lv, vh, gcp, eg)));
+        // one stream of programmatically serialised launches per reverse step; lt is
+        // overwritten by adj_t_pml before the stress-record gradients are added to it
+        if (gr) ADFWI_LAUNCH(kAux, s, (void)launch_pdl_kernel(el::adj_inject<T>, ginj, dim3(128), 0, s, g, it, gr, lt, lv, 1));
+        ADFWI_LAUNCH(kElAdjStep, s, (void)launch_pdl_kernel(el::adj_vfs_tq_pml<T>, gcm, b, 0, s, g, cf, lv, lst + 6 * NSP, qsrc));
+        ADFWI_LAUNCH(kElAdjStep, s, (void)launch_pdl_kernel(el::adj_t_pml<T, NN>, gcg, b, (size_t)smem_t, s, g, cf,
+                                                            lst + 6 * NSP, qsrc, lt, th, gcp, eg));
+        if (gr) ADFWI_LAUNCH(kAux, s, (void)launch_pdl_kernel(el::adj_inject<T>, ginj, dim3(128), 0, s, g, it, gr, lt, lv, 2));
+        ADFWI_LAUNCH(kElAdjStep, s, (void)launch_pdl_kernel(el::adj_tfs_vq_pml<T>, gcm, b, 0, s, g, cf, lt, lst, qsrc));
+        ADFWI_LAUNCH(kElAdjStep, s, (void)launch_pdl_kernel(el::adj_v<T, NN, true>, gcg, b, (size_t)smem_vp, s, g, cf, lst,
+                                                            qsrc, lv, vh, gcp, eg));
       } else {
-        if (gr) ADFWI_LAUNCH(kAux, s, (el::adj_inject<T><<<ginj, 128, 0, s>>>(g, it, gr, lst, lv, 1)));
+        if (gr) ADFWI_LAUNCH(kAux, s, (el::adj_inject<T><<<ginj, 128, 0, s>>>(g, it, gr, lst, lv, 3)));
         ADFWI_LAUNCH(kElAdjStep, s, (el::adj_vfs_abl<T><<<gcs, b, 0, s>>>(g, cf, lv, lv2, nullptr)));
         std::swap(lv, lv2);
         ADFWI_LAUNCH(kElAdjStep, s, (el::adj_tq<T, false><<<gcs, b, 0, s>>>(g, cf, lv, qsrc)));

@@ -101,16 +101,6 @@ __device__ __forceinline__ void prefetch_tensormap(const CUtensorMap* map) {
   asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(map)) : "memory");
 }
 
-// Programmatic dependent launch. A step kernel is launched with programmatic stream
-// serialisation, so its blocks may become resident while the previous step kernel's last
-// blocks still run: every block signals at once that the next launch may start
-// (launch_dependents), and waits for the previous grid's completion and memory (wait)
-// before its first read of the fields and its first write of anything.
-__device__ __forceinline__ void griddep_launch_dependents() {
-  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-}
-__device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
-
 // Named barrier among `count` threads (count a multiple of 32), id 1..15.
 __device__ __forceinline__ void named_sync(int id, int count) {
   asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");

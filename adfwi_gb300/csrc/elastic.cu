@@ -743,25 +743,6 @@ __device__ __forceinline__ Pml<T> pml_at(const Geo<T>& g, const T* cf, int64_t o
   return p;
 }
 
-// (B4) lambda of the split velocities after the step: S (deferred PML factor of the next
-// step's update) * lambda + lambda of the totals after the free-surface adjoint.
-template <typename T>
-__global__ void adj_vfs_pml(Geo<T> g, const T* __restrict__ cf, const T* __restrict__ lv, T* lvs) {
-  EL_CELL_SHOT
-  T ax, az;
-  vfs_adjoint(g, lv + VX * NSP, lv + VZ * NSP, i, j, o, ax, az);
-  T sx = T(1), sz = T(1);
-  if (in_I(g, i, j)) {
-    Pml<T> p = pml_at(g, cf, g.L.off(i, j), PL);
-    sx = p.xn / p.xd;
-    sz = p.zn / p.zd;
-  }
-  lvs[VX_X * NSP + o] = sx * lvs[VX_X * NSP + o] + ax;
-  lvs[VX_Z * NSP + o] = sz * lvs[VX_Z * NSP + o] + ax;
-  lvs[VZ_X * NSP + o] = sx * lvs[VZ_X * NSP + o] + az;
-  lvs[VZ_Z * NSP + o] = sz * lvs[VZ_Z * NSP + o] + az;
-}
-
 // One plane of a (field, shot) block read at grid cells; the block's ghost frame is zero.
 template <typename T>
 struct PlaneQ {
@@ -866,25 +847,33 @@ __global__ void __launch_bounds__(kTileThreads)
 }
 
 // (B2) lambda of the split stresses: S * lambda + lambda of the totals after the stress
-// free-surface adjoint.
+// free-surface adjoint (the stress update's adjoint sources are formed by adj_v_pml).
 template <typename T>
-__global__ void adj_tfs_pml(Geo<T> g, const T* __restrict__ cf, const T* __restrict__ lt, T* lts) {
-  EL_CELL_SHOT
-  T azz, axz;
-  tfs_adjoint(g, lt + TZZ * NSP, lt + TXZ * NSP, i, o, azz, axz);
-  const T axx = lt[TXX * NSP + o];
+__global__ void adj_tfs_pml(Geo<T> g, const T* __restrict__ cf, const T* __restrict__ lt, T* __restrict__ lts) {
+  griddep_wait();  // launched with programmatic serialisation in the PML time loops
+  griddep_launch_dependents();
+  EL_CELL_SHOTS
   T sx = T(1), sz = T(1);
   if (in_I(g, i, j)) {
-    Pml<T> p = pml_at(g, cf, g.L.off(i, j), PL);
-    sx = p.xn / p.xd;
-    sz = p.zn / p.zd;
+    const Pml<T> p = pml_at(g, cf, occ, PL);
+    sx = p.xn * (T(1) / p.xd);  // the adjoint needs no bit-exact rounding
+    sz = p.zn * (T(1) / p.zd);
   }
-  lts[TXX_X * NSP + o] = sx * lts[TXX_X * NSP + o] + axx;
-  lts[TXX_Z * NSP + o] = sz * lts[TXX_Z * NSP + o] + axx;
-  lts[TZZ_X * NSP + o] = sx * lts[TZZ_X * NSP + o] + azz;
-  lts[TZZ_Z * NSP + o] = sz * lts[TZZ_Z * NSP + o] + azz;
-  lts[TXZ_X * NSP + o] = sx * lts[TXZ_X * NSP + o] + axz;
-  lts[TXZ_Z * NSP + o] = sz * lts[TXZ_Z * NSP + o] + axz;
+#pragma unroll
+  for (int q = 0; q < kCellShots; ++q) {
+    const int s = s_lo + q;
+    if (s >= g.ns) break;
+    const int64_t o = (int64_t)s * PL + occ;
+    T azz, axz;
+    tfs_adjoint(g, lt + TZZ * NSP, lt + TXZ * NSP, i, o, azz, axz);
+    const T axx = lt[TXX * NSP + o];
+    lts[TXX_X * NSP + o] = sx * lts[TXX_X * NSP + o] + axx;
+    lts[TXX_Z * NSP + o] = sz * lts[TXX_Z * NSP + o] + axx;
+    lts[TZZ_X * NSP + o] = sx * lts[TZZ_X * NSP + o] + azz;
+    lts[TZZ_Z * NSP + o] = sz * lts[TZZ_Z * NSP + o] + azz;
+    lts[TXZ_X * NSP + o] = sx * lts[TXZ_X * NSP + o] + axz;
+    lts[TXZ_Z * NSP + o] = sz * lts[TXZ_Z * NSP + o] + axz;
+  }
 }
 
 // Coefficient-weighted adjoint sources of the stress update at cell (ii, jj):
@@ -999,67 +988,6 @@ __global__ void adj_vfs_tq_pml(Geo<T> g, const T* __restrict__ cf, const T* __re
   }
 }
 
-// (B2 + B1q) fused per cell and shot: the split stresses' lambda (adj_tfs_pml) and, from those
-// new values, the stress update's adjoint sources for the velocity transposes (adj_vq, PML).
-template <typename T>
-__global__ void adj_tfs_vq_pml(Geo<T> g, const T* __restrict__ cf, const T* __restrict__ lt, T* lts,
-                               T* __restrict__ q8) {
-  griddep_wait();  // launched with programmatic serialisation in the PML time loops
-  griddep_launch_dependents();
-  EL_CELL_SHOTS
-  const bool inside = in_I(g, i, j);
-  T sx = T(1), sz = T(1), kx = T(0), kz = T(0);
-  T c11 = T(0), c13 = T(0), c15 = T(0), c33 = T(0), c35 = T(0), c55 = T(0);
-  if (inside) {
-    const Pml<T> p = pml_at(g, cf, occ, PL);
-    const T ix = T(1) / p.xd, iz = T(1) / p.zd;
-    sx = p.xn * ix;
-    sz = p.zn * iz;
-    kx = g.dt_dx * ix;
-    kz = g.dt_dz * iz;
-    c11 = cf[C11 * PL + occ];
-    c13 = cf[C13 * PL + occ];
-    c15 = cf[C15 * PL + occ];
-    c33 = cf[C33 * PL + occ];
-    c35 = cf[C35 * PL + occ];
-    c55 = cf[C55 * PL + occ];
-  }
-#pragma unroll
-  for (int q = 0; q < kCellShots; ++q) {
-    const int s = s_lo + q;
-    if (s >= g.ns) break;
-    const int64_t o = (int64_t)s * PL + occ;
-    T azz, axz;
-    tfs_adjoint(g, lt + TZZ * NSP, lt + TXZ * NSP, i, o, azz, axz);
-    const T axx = lt[TXX * NSP + o];
-    T ls[6];
-    ls[0] = sx * lts[TXX_X * NSP + o] + axx;
-    ls[1] = sz * lts[TXX_Z * NSP + o] + axx;
-    ls[2] = sx * lts[TZZ_X * NSP + o] + azz;
-    ls[3] = sz * lts[TZZ_Z * NSP + o] + azz;
-    ls[4] = sx * lts[TXZ_X * NSP + o] + axz;
-    ls[5] = sz * lts[TXZ_Z * NSP + o] + axz;
-#pragma unroll
-    for (int k = 0; k < 6; ++k) lts[k * NSP + o] = ls[k];
-    T v8[8];
-#pragma unroll
-    for (int k = 0; k < 8; ++k) v8[k] = T(0);  // zero outside I
-    if (inside) {
-      const T ra = ls[0] * kx, rb = ls[1] * kz, rc = ls[2] * kx, rd = ls[3] * kz, re = ls[4] * kx, rf = ls[5] * kz;
-      v8[0] = c11 * ra + c13 * rc;
-      v8[1] = c15 * rb + c35 * rd;
-      v8[2] = c15 * re;
-      v8[3] = c55 * rf;
-      v8[4] = c15 * ra + c35 * rc;
-      v8[5] = c13 * rb + c33 * rd;
-      v8[6] = c55 * re;
-      v8[7] = c35 * rf;
-    }
-#pragma unroll
-    for (int k = 0; k < 8; ++k) q8[k * NSP + o] = v8[k];
-  }
-}
-
 // (B1a) lambda of the velocity totals at the start of the step (overwrite) and the C gradients.
 // pml = 1: split-field update; pml = 0: absorbing-layer update (lts then holds txx, tzz, txz,
 // and lv is accumulated instead of overwritten because v' = v + ...).
@@ -1120,6 +1048,120 @@ __global__ void __launch_bounds__(kTileThreads)
         const StressQ<T> r = stress_q<T, PMLM>(sm + 10 * kSPlane + sc, 0, kSPlane, kx, kz);
         const T* vx = sm + 8 * kSPlane;
         const T* vz = sm + 9 * kSPlane;
+        const T dxb_vx = dxb<NN>(g, vx, sc), dxb_vz = dxb<NN>(g, vz, sc);
+        const T dzb_vx = dzb<NN>(g, vx, sc, kSW), dzb_vz = dzb<NN>(g, vz, sc, kSW);
+        const T dxf_vx = dxf<NN>(g, vx, sc), dxf_vz = dxf<NN>(g, vz, sc);
+        const T dzf_vx = dzf<NN>(g, vx, sc, kSW), dzf_vz = dzf<NN>(g, vz, sc, kSW);
+        g11 += r.a * dxb_vx;
+        g13 += r.b * dzb_vz + r.c * dxb_vx;
+        g15 += r.a * dxb_vz + r.b * dzb_vx + r.e * dxf_vx;
+        g33 += r.d * dzb_vz;
+        g35 += r.c * dxb_vz + r.d * dzb_vx + r.f * dzf_vz;
+        g55 += r.e * dxf_vz + r.f * dzf_vx;
+      }
+    }
+    __syncthreads();  // the next shot's copies overwrite the staged planes
+  }
+  if (inside) {
+    gc[C11 * PL + oc] += g11;
+    gc[C13 * PL + oc] += g13;
+    gc[C15 * PL + oc] += g15;
+    gc[C33 * PL + oc] += g33;
+    gc[C35 * PL + oc] += g35;
+    gc[C55 * PL + oc] += g55;
+  }
+}
+
+// (B1a, PML) lambda of the velocity totals at the start of the step (overwrite) and the C
+// gradients, with the stress update's adjoint sources formed in shared memory. Per block the
+// tile's cell coefficients C11 .. C55 and PML factors dt/dx / pml_xd, dt/dz / pml_zd (zero outside
+// I) are staged once with the full halo; per shot the lambda of the six split stresses and vx, vz
+// of the forward history are staged, the eight sources q (sx_b, sx_zb, sx_f, sx_zf, sz_b, sz_zb,
+// sz_f, sz_zf: coefficient-weighted lambda, zero outside I) formed at every staged cell, and the
+// transposes and gradients evaluated from them. Planes: 0-5 C, 6-7 factors, 8-13 lambda,
+// 14-15 vx, vz, 16-23 q.
+constexpr int kAdjVPmlPlanes = 24;
+template <typename T, int NN>
+__global__ void __launch_bounds__(kTileThreads)
+    adj_v_pml(Geo<T> g, const T* __restrict__ cf, const T* __restrict__ lts, T* __restrict__ lv,
+              const T* __restrict__ v_hist, T* __restrict__ gpart, int eg) {
+  griddep_wait();  // launched with programmatic serialisation in the PML time loops
+  griddep_launch_dependents();
+  extern __shared__ __align__(16) unsigned char el_smem[];
+  T* sC = reinterpret_cast<T*>(el_smem);
+  T* sK = sC + 6 * kSPlane;
+  T* sL = sC + 8 * kSPlane;
+  T* sV = sC + 14 * kSPlane;
+  T* sQ = sC + 16 * kSPlane;
+  const int tiles_x = (g.L.nxp + kTileX - 1) / kTileX;
+  const int i0 = ((int)blockIdx.x / tiles_x) * kTileZ, j0 = ((int)blockIdx.x % tiles_x) * kTileX;
+  const int ty = (int)threadIdx.x / kTileX, tx = (int)threadIdx.x % kTileX;
+  const int i = i0 + ty, j = j0 + tx;
+  const bool valid = i < g.L.nzp && j < g.L.nxp, inside = valid && in_I(g, i, j);
+  const int64_t PL = g.L.plane, NSP = (int64_t)g.ns * PL, oc = g.L.off(i, j);
+  const int sc = kSC + ty * kSW + tx;
+  EL_SHOT_GROUP
+  T* gc = gbase;
+#pragma unroll
+  for (int k = 0; k < 6; ++k) stage(sC + k * kSPlane, cf + (C11 + k) * PL, g.L, i0, j0, 3, 4);
+  stage(sK, cf + BCX * PL, g.L, i0, j0, 3, 4);
+  stage(sK + kSPlane, cf + BCZ * PL, g.L, i0, j0, 3, 4);
+  cp_async_wait_all();
+  __syncthreads();
+  for (int t = threadIdx.x; t < kSPlane; t += kTileThreads) {  // bcx, bcz -> the factors, in place
+    const int ii = i0 + t / kSW - 3, jj = j0 + t % kSW - 4;
+    T kx = T(0), kz = T(0);
+    if (in_I(g, ii, jj)) {
+      kx = g.dt_dx / (T(1) + g.hdt * sK[t]);
+      kz = g.dt_dz / (T(1) + g.hdt * sK[kSPlane + t]);
+    }
+    sK[t] = kx;
+    sK[kSPlane + t] = kz;
+  }
+  // (the barrier after the first shot's copies orders these writes before their reads)
+  T g11 = T(0), g13 = T(0), g15 = T(0), g33 = T(0), g35 = T(0), g55 = T(0);
+  for (int s = s_beg; s < s_end; ++s) {
+    const int64_t so = (int64_t)s * PL;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) stage(sL + k * kSPlane, lts + k * NSP + so, g.L, i0, j0, 3, 4);
+    stage(sV, v_hist + VX * NSP + so, g.L, i0, j0, 3, 4);
+    stage(sV + kSPlane, v_hist + VZ * NSP + so, g.L, i0, j0, 3, 4);
+    cp_async_wait_all();
+    __syncthreads();
+    for (int t = threadIdx.x; t < kSPlane; t += kTileThreads) {
+      const T kx = sK[t], kz = sK[kSPlane + t];
+      T q[8] = {T(0), T(0), T(0), T(0), T(0), T(0), T(0), T(0)};
+      if (kx != T(0)) {  // inside I (the factors are positive there)
+        const T ra = sL[t] * kx, rb = sL[kSPlane + t] * kz, rc = sL[2 * kSPlane + t] * kx;
+        const T rd = sL[3 * kSPlane + t] * kz, re = sL[4 * kSPlane + t] * kx, rf = sL[5 * kSPlane + t] * kz;
+        const T c11 = sC[t], c13 = sC[kSPlane + t], c15 = sC[2 * kSPlane + t];
+        const T c33 = sC[3 * kSPlane + t], c35 = sC[4 * kSPlane + t], c55 = sC[5 * kSPlane + t];
+        q[0] = c11 * ra + c13 * rc;
+        q[1] = c15 * rb + c35 * rd;
+        q[2] = c15 * re;
+        q[3] = c55 * rf;
+        q[4] = c15 * ra + c35 * rc;
+        q[5] = c13 * rb + c33 * rd;
+        q[6] = c55 * re;
+        q[7] = c35 * rf;
+      }
+#pragma unroll
+      for (int k = 0; k < 8; ++k) sQ[k * kSPlane + t] = q[k];
+    }
+    __syncthreads();
+    if (valid) {
+      const StagedQ<T> q0{sQ, i0, j0}, q1{sQ + kSPlane, i0, j0}, q2{sQ + 2 * kSPlane, i0, j0},
+          q3{sQ + 3 * kSPlane, i0, j0}, q4{sQ + 4 * kSPlane, i0, j0}, q5{sQ + 5 * kSPlane, i0, j0},
+          q6{sQ + 6 * kSPlane, i0, j0}, q7{sQ + 7 * kSPlane, i0, j0};
+      const T avx = dxb_t<NN>(g, q0, i, j) + dzb_t<NN>(g, q1, i, j) + dxf_t<NN>(g, q2, i, j) + dzf_t<NN>(g, q3, i, j);
+      const T avz = dxb_t<NN>(g, q4, i, j) + dzb_t<NN>(g, q5, i, j) + dxf_t<NN>(g, q6, i, j) + dzf_t<NN>(g, q7, i, j);
+      const int64_t o = so + oc;
+      lv[VX * NSP + o] = avx;
+      lv[VZ * NSP + o] = avz;
+      if (inside) {
+        const StressQ<T> r = stress_q<T, true>(sL + sc, 0, kSPlane, sK[sc], sK[kSPlane + sc]);
+        const T* vx = sV;
+        const T* vz = sV + kSPlane;
         const T dxb_vx = dxb<NN>(g, vx, sc), dxb_vz = dxb<NN>(g, vz, sc);
         const T dzb_vx = dzb<NN>(g, vx, sc, kSW), dzb_vz = dzb<NN>(g, vz, sc, kSW);
         const T dxf_vx = dxf<NN>(g, vx, sc), dxf_vz = dxf<NN>(g, vz, sc);
@@ -1601,10 +1643,10 @@ int ebackward(const adfwi_elastic_plan* p, const void* wavelet, const void* grec
   const dim3 gcm = cells_grid(p, (ns + el::kCellShots - 1) / el::kCellShots);
   // shared memory of the staged gradient kernels (above the 48 KB default in double precision)
   const int smem_t = el::kAdjTPlanes * el::kSPlane * (int)sizeof(T);
-  const int smem_vp = el::adj_v_planes<true>() * el::kSPlane * (int)sizeof(T);
+  const int smem_vp = el::kAdjVPmlPlanes * el::kSPlane * (int)sizeof(T);
   const int smem_va = el::adj_v_planes<false>() * el::kSPlane * (int)sizeof(T);
   ADFWI_CUDA_TRY(cudaFuncSetAttribute(el::adj_t_pml<T, NN>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_t));
-  ADFWI_CUDA_TRY(cudaFuncSetAttribute(el::adj_v<T, NN, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_vp));
+  ADFWI_CUDA_TRY(cudaFuncSetAttribute(el::adj_v_pml<T, NN>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_vp));
   ADFWI_CUDA_TRY(cudaFuncSetAttribute(el::adj_v<T, NN, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_va));
   const dim3 gcol((unsigned)((p->nxp + 127) / 128), ns);
   const dim3 ginj((unsigned)std::max(1, (p->ncells + 127) / 128), ns);
@@ -1639,9 +1681,9 @@ int ebackward(const adfwi_elastic_plan* p, const void* wavelet, const void* grec
         ADFWI_LAUNCH(kElAdjStep, s, (void)launch_pdl_kernel(el::adj_t_pml<T, NN>, gcg, b, (size_t)smem_t, s, g, cf,
                                                             lst + 6 * NSP, qsrc, lt, th, gcp, eg));
         if (gr) ADFWI_LAUNCH(kAux, s, (void)launch_pdl_kernel(el::adj_inject<T>, ginj, dim3(128), 0, s, g, it, gr, lt, lv, 2));
-        ADFWI_LAUNCH(kElAdjStep, s, (void)launch_pdl_kernel(el::adj_tfs_vq_pml<T>, gcm, b, 0, s, g, cf, lt, lst, qsrc));
-        ADFWI_LAUNCH(kElAdjStep, s, (void)launch_pdl_kernel(el::adj_v<T, NN, true>, gcg, b, (size_t)smem_vp, s, g, cf, lst,
-                                                            qsrc, lv, vh, gcp, eg));
+        ADFWI_LAUNCH(kElAdjStep, s, (void)launch_pdl_kernel(el::adj_tfs_pml<T>, gcm, b, 0, s, g, cf, (const T*)lt, lst));
+        ADFWI_LAUNCH(kElAdjStep, s, (void)launch_pdl_kernel(el::adj_v_pml<T, NN>, gcg, b, (size_t)smem_vp, s, g, cf,
+                                                            (const T*)lst, lv, vh, gcp, eg));
       } else {
         if (gr) ADFWI_LAUNCH(kAux, s, (el::adj_inject<T><<<ginj, 128, 0, s>>>(g, it, gr, lst, lv, 3)));
         ADFWI_LAUNCH(kElAdjStep, s, (el::adj_vfs_abl<T><<<gcs, b, 0, s>>>(g, cf, lv, lv2, nullptr)));

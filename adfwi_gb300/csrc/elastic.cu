@@ -1341,11 +1341,11 @@ struct ECarve {
 int ncoef(const adfwi_elastic_plan* p) { return p->d.pml ? 10 : 9; }
 
 // Shot groups of the gradient kernels: enough (cell, group) threads to fill the GPU (about
-// 600 k), at most one group per shot.
+// 300 k), at most one group per shot.
 int egroups(const adfwi_elastic_plan* p) {
   const int64_t cells = (int64_t)p->nzp * p->nxp;
 #ifndef ADFWI_EL_THREADS
-#define ADFWI_EL_THREADS 600000
+#define ADFWI_EL_THREADS 300000
 #endif
   const int64_t want = ((int64_t)ADFWI_EL_THREADS + cells - 1) / cells;
   const int g = (int)std::max<int64_t>(1, std::min<int64_t>(p->d.ns, want));

@@ -130,9 +130,8 @@ def test_elastic_low_precision_snapshots_stay_close(precision, tol, abc_type):
 
 
 def test_elastic_shot_groups_agree_with_single_shots():
-    """On the 242 x 480 padded VTI grid 13 shots run as groups of 3 (the gradient kernels loop
-    over the shots of a group, restaging each shot's planes in shared memory; the last group
-    is partial). Gradients are sums over shots, so the 13-shot gradient equals the sum of the
+    """On the 242 x 480 padded VTI grid 13 shots run as groups of 5, 5 and 3 (the gradient
+    kernels loop over the shots of a group, restaging each shot's planes in shared memory). Gradients are sums over shots, so the 13-shot gradient equals the sum of the
     13 single-shot gradients (each a group of one) to rounding."""
     from adfwi_gb300.synthetic import vti_gradient_case
     model, survey = vti_gradient_case(seed=2, nt=150, n_shots=13, device="cuda:0")

@@ -544,9 +544,10 @@ class SolveServer(object):
                 self._running += 1
                 self.peak_running = max(self.peak_running, self._running)
             res = err = None
-            replayed = shape.graph is not None
+            replayed = False
             try:
                 loss, grad, rec = shape.run(req, self.arena, stream, cstream, self.device, self.graphs)
+                replayed = shape.graph is not None  # this solve ran as a graph replay (its shape's second use on)
                 res = SolveResult(req.rid, loss, grad, rec, t_arr, t_admit, time.perf_counter(), shape.cells,
                                   shape.n, shape.plan.snapshot_every)
             except Exception as e:  # the others keep running; the future carries the error

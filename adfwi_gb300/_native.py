@@ -59,6 +59,7 @@ def _bind(lib):
         "adfwi_acoustic_backward": (c_int32, [P, P, P, P, P, P, P, P, P, P, P, c_int64, P]),
         "adfwi_acoustic_status": (c_int32, [P, P, c_int64, c_int32, ctypes.POINTER(c_int32), P]),
         "adfwi_last_error": (c_int32, [ctypes.c_char_p, ctypes.c_size_t]),
+        "adfwi_wait_selftest": (c_int32, [c_int64, P, P]),
         "adfwi_profile_start": (c_int32, [c_int32]),
         "adfwi_profile_stop": (c_int32, [ctypes.POINTER(KernelStat), c_int32, ctypes.POINTER(c_int32)]),
         "adfwi_launch_count": (c_int64, []),
@@ -142,3 +143,10 @@ def profile_stop():
     n = c_int32()
     check(lib().adfwi_profile_stop(out, 16, ctypes.byref(n)), "adfwi_profile_stop")
     return {out[i].name.decode(): (out[i].launches, out[i].timed_launches, out[i].total_ms) for i in range(n.value)}
+
+
+def wait_selftest(limit_ns, flag, stream=None):
+    """Run the bounded-wait self-test: `flag` (a zeroed int32 CUDA tensor of one element) becomes
+    1 once a wait that nothing completes has run out after `limit_ns`."""
+    st = ctypes.c_void_p(stream) if stream is not None else stream_handle(flag.device)
+    check(lib().adfwi_wait_selftest(int(limit_ns), ptr(flag), st), "adfwi_wait_selftest")

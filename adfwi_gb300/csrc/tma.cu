@@ -1,6 +1,8 @@
-// Host side of the TMA helpers: tensor-map encoding through the driver entry point.
+// Host side of the TMA helpers (tensor-map encoding through the driver entry point) and the
+// self-test of the bounded mbarrier waits.
 #include <mutex>
 
+#include "../../include/adfwi_gb300.h"
 #include "tma.cuh"
 
 namespace adfwi {
@@ -43,3 +45,31 @@ int make_plane_map(CUtensorMap* map, const void* base, int elem_bytes, const Lay
 }
 
 }  // namespace adfwi
+
+// ---------------------------------------------------------------------------------------
+// Self-test of the bounded waits: one block waits on phase 0 of a fresh mbarrier that nothing
+// arrives at, through the same wait loop as the pipelined kernels, so the wait runs out after
+// `limit_ns` and the kernel raises the error flag and returns (no trap, no unbounded spin).
+namespace adfwi {
+namespace {
+__global__ void wait_selftest(unsigned long long limit_ns, int* flag) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    fence_barrier_init();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && !mbar_wait_for(&bar, 0, limit_ns)) raise_flag(flag, kErrWaitTimeout);
+}
+}  // namespace
+}  // namespace adfwi
+
+extern "C" int adfwi_wait_selftest(int64_t limit_ns, int32_t* flag, void* stream) {
+  using namespace adfwi;
+  ADFWI_CHECK_ARG(flag != nullptr, "null flag");
+  ADFWI_CHECK_ARG(limit_ns > 0 && limit_ns <= 2000000000ll, "limit_ns must be in (0, 2 s]");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  ADFWI_LAUNCH(kAux, st, (wait_selftest<<<1, 32, 0, st>>>((unsigned long long)limit_ns, reinterpret_cast<int*>(flag))));
+  ADFWI_CUDA_TRY(cudaGetLastError());
+  return kOk;
+}

@@ -64,8 +64,9 @@ __device__ __forceinline__ void mbar_arrive_cnt(uint64_t* bar, unsigned count) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
 }
 
-// Wait for the phase with the given parity to complete. Returns false once kWaitNs have passed.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
+// Wait for the phase with the given parity to complete. Returns false once `limit_ns` of the
+// global timer have passed.
+__device__ __forceinline__ bool mbar_wait_for(uint64_t* bar, unsigned parity, unsigned long long limit_ns) {
   const uint32_t a = smem_u32(bar);
   unsigned long long t0 = 0;
   for (unsigned n = 0;; ++n) {
@@ -82,11 +83,12 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
       const unsigned long long t = global_ns();
       if (t0 == 0)
         t0 = t;
-      else if (t - t0 > kWaitNs)
+      else if (t - t0 > limit_ns)
         return false;
     }
   }
 }
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) { return mbar_wait_for(bar, parity, kWaitNs); }
 
 // One 3-D tile load into shared memory, completing on `bar` (complete_tx in bytes).
 __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int x, int y, int z, uint64_t* bar) {

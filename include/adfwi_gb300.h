@@ -159,6 +159,13 @@ int adfwi_acoustic_status(const adfwi_acoustic_plan* plan, const void* workspace
                           int64_t workspace_bytes, int32_t with_gradient, int32_t* status,
                           void* stream);
 
+/* Self-test of the bounded waits behind adfwi_acoustic_status (no reference counterpart: the
+ * reference's PyTorch loop has no device-side waits). One block waits, through the pipelined
+ * kernels' wait loop, on an mbarrier phase that nothing completes; after limit_ns (at most 2 s)
+ * it gives up, writes 1 (wait timed out) to the DEVICE int *flag and exits, leaving the context
+ * usable. Stream-ordered; the caller zeroes *flag first. */
+int adfwi_wait_selftest(int64_t limit_ns, int32_t* flag, void* stream);
+
 /* ------------------------------------------------------------------------- */
 /* Normalised L2 trace misfit and its adjoint source.                          */
 /* ------------------------------------------------------------------------- */

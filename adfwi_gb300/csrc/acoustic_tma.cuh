@@ -11,7 +11,10 @@
 // `full` mbarrier with the byte count (the per-item source cell and amplitude travel in a
 // small header written before the arming arrive). The consumer warps wait on `full`,
 // compute, and arrive on the stage's `empty` mbarrier once they no longer read it, so the
-// loads of the next items overlap the arithmetic of the current one.
+// loads of the next items overlap the arithmetic of the current one. Items of tiles holding
+// receivers go through the producer warp's other 31 lanes (the relay): the consumers arrive
+// on the stage's `stored` mbarrier instead, and the relay releases the stage (`empty`) and does
+// the receiver work on the item's global outputs, off the consumers' path.
 //
 // Every wait is bounded (kWaitNs of elapsed time); a wait that runs out raises the device
 // error flag and a block-wide abort flag, after which the block skips its remaining work

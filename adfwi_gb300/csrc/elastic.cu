@@ -232,113 +232,8 @@ struct StagedQ {
 };
 
 // ======================================================================= forward, PML
-// Split stresses in I (elastic_kernels.py:351-356), then the moment-tensor source on both
-// split parts (359-372). ts: 6 fields; v: vx, vz totals at the start of the step.
-template <typename T, int NN>
-__global__ void stress_pml(Geo<T> g, int it, const T* __restrict__ cf, const T* __restrict__ v, T* __restrict__ ts,
-                           const T* __restrict__ wav) {
-  EL_CELL_SHOT
-  const int64_t occ = g.L.off(i, j);
-  if (in_I(g, i, j)) {
-    const T* vx = v;
-    const T* vz = v + NSP;
-    const T dxbm_vx = dxb<NN>(g, vx, o), dxbm_vz = dxb<NN>(g, vz, o);
-    const T dzbm_vx = dzb<NN>(g, vx, o), dzbm_vz = dzb<NN>(g, vz, o);
-    const T dxfm_vx = dxf<NN>(g, vx, o), dzfm_vx = dzf<NN>(g, vx, o);
-    const T dxfm_vz = dxf<NN>(g, vz, o), dzfm_vz = dzf<NN>(g, vz, o);
-    const T bcx = cf[BCX * PL + occ], bcz = cf[BCZ * PL + occ];
-    const T pxd = radd(T(1), rmul(g.hdt, bcx)), pxn = rsub(T(1), rmul(g.hdt, bcx));
-    const T pzd = radd(T(1), rmul(g.hdt, bcz)), pzn = rsub(T(1), rmul(g.hdt, bcz));
-    const T pxi = rdiv(T(1), pxd), pzi = rdiv(T(1), pzd);
-    const T c11 = cf[C11 * PL + occ], c13 = cf[C13 * PL + occ], c15 = cf[C15 * PL + occ];
-    const T c33 = cf[C33 * PL + occ], c35 = cf[C35 * PL + occ], c55 = cf[C55 * PL + occ];
-    T* f;
-    f = ts + TXX_X * NSP + o; *f = rmul(radd(rmul(pxn, *f), rmul(g.dt_dx, radd(rmul(c11, dxbm_vx), rmul(c15, dxbm_vz)))), pxi);
-    f = ts + TXX_Z * NSP + o; *f = rmul(radd(rmul(pzn, *f), rmul(g.dt_dz, radd(rmul(c15, dzbm_vx), rmul(c13, dzbm_vz)))), pzi);
-    f = ts + TZZ_X * NSP + o; *f = rmul(radd(rmul(pxn, *f), rmul(g.dt_dx, radd(rmul(c13, dxbm_vx), rmul(c35, dxbm_vz)))), pxi);
-    f = ts + TZZ_Z * NSP + o; *f = rmul(radd(rmul(pzn, *f), rmul(g.dt_dz, radd(rmul(c35, dzbm_vx), rmul(c33, dzbm_vz)))), pzi);
-    f = ts + TXZ_X * NSP + o; *f = rmul(radd(rmul(pxn, *f), rmul(g.dt_dx, radd(rmul(c15, dxfm_vx), rmul(c55, dxfm_vz)))), pxi);
-    f = ts + TXZ_Z * NSP + o; *f = rmul(radd(rmul(pzn, *f), rmul(g.dt_dz, radd(rmul(c55, dzfm_vx), rmul(c35, dzfm_vz)))), pzi);
-  }
-  if (i == g.src_z[s] && j == g.src_x[s]) {
-    const T w = wav[(int64_t)s * g.nt + it];
-    const T axx = rmul(g.src_m[3 * s + 0], w), azz = rmul(g.src_m[3 * s + 1], w), axz = rmul(g.src_m[3 * s + 2], w);
-    ts[TXX_X * NSP + o] = radd(ts[TXX_X * NSP + o], axx);
-    ts[TXX_Z * NSP + o] = radd(ts[TXX_Z * NSP + o], axx);
-    ts[TZZ_X * NSP + o] = radd(ts[TZZ_X * NSP + o], azz);
-    ts[TZZ_Z * NSP + o] = radd(ts[TZZ_Z * NSP + o], azz);
-    ts[TXZ_X * NSP + o] = radd(ts[TXZ_X * NSP + o], axz);
-    ts[TXZ_Z * NSP + o] = radd(ts[TXZ_Z * NSP + o], axz);
-  }
-}
-
-// Stress totals and free-surface stress rows (elastic_kernels.py:375-384) -> T (3 fields).
-template <typename T>
-__global__ void stress_tot_pml(Geo<T> g, const T* __restrict__ ts, T* __restrict__ tt) {
-  EL_CELL_SHOT
-  const int64_t P = g.L.pitch;
-  auto sum = [&](int f, int64_t oo) { return radd(ts[(2 * f) * NSP + oo], ts[(2 * f + 1) * NSP + oo]); };
-  T xx = sum(TXX, o), zz = sum(TZZ, o), xz = sum(TXZ, o);
-  if (g.fsurf) {
-    const int h = g.h;
-    if (i == h - 1) zz = T(0);
-    if (i == h - 2) zz = -sum(TZZ, o + 2 * P);
-    if (i == h - 2) xz = -sum(TXZ, o + P);
-    if (i == h - 3) xz = -sum(TXZ, o + 3 * P);
-  }
-  tt[TXX * NSP + o] = xx;
-  tt[TZZ * NSP + o] = zz;
-  tt[TXZ * NSP + o] = xz;
-}
-
-// Split velocities in I (elastic_kernels.py:387-394) from the stress totals tt.
-template <typename T, int NN>
-__global__ void vel_pml(Geo<T> g, const T* __restrict__ cf, const T* __restrict__ tt, T* __restrict__ vs) {
-  EL_CELL_SHOT
-  if (!in_I(g, i, j)) return;
-  const int64_t occ = g.L.off(i, j);
-  const T dxfm_txx = dxf<NN>(g, tt + TXX * NSP, o);
-  const T dzbm_txz = dzb<NN>(g, tt + TXZ * NSP, o);
-  const T dxbm_txz = dxb<NN>(g, tt + TXZ * NSP, o);
-  const T dzfm_tzz = dzf<NN>(g, tt + TZZ * NSP, o);
-  const T bcx = cf[BCX * PL + occ], bcz = cf[BCZ * PL + occ];
-  const T pxd = radd(T(1), rmul(g.hdt, bcx)), pxn = rsub(T(1), rmul(g.hdt, bcx));
-  const T pzd = radd(T(1), rmul(g.hdt, bcz)), pzn = rsub(T(1), rmul(g.hdt, bcz));
-  const T bx = cf[BX * PL + occ], bz = cf[BZ * PL + occ];
-  const T dbx = rmul(g.dt, bx), dbz = rmul(g.dt, bz);
-  T* f;
-  f = vs + VX_X * NSP + o; *f = rdiv(radd(rmul(pxn, *f), rdiv(rmul(dbx, dxfm_txx), g.dx)), pxd);
-  f = vs + VX_Z * NSP + o; *f = rdiv(radd(rmul(pzn, *f), rdiv(rmul(dbx, dzbm_txz), g.dz)), pzd);
-  f = vs + VZ_X * NSP + o; *f = rdiv(radd(rmul(pxn, *f), rdiv(rmul(dbz, dxbm_txz), g.dx)), pxd);
-  f = vs + VZ_Z * NSP + o; *f = rdiv(radd(rmul(pzn, *f), rdiv(rmul(dbz, dzfm_tzz), g.dz)), pzd);
-}
-
-// Velocity totals and free-surface velocity rows (elastic_kernels.py:395-402) -> v (2 fields).
-template <typename T>
-__global__ void vel_tot_pml(Geo<T> g, const T* __restrict__ vs, T* __restrict__ v) {
-  EL_CELL_SHOT
-  const int64_t P = g.L.pitch;
-  auto vxs = [&](int64_t oo) { return radd(vs[VX_X * NSP + oo], vs[VX_Z * NSP + oo]); };
-  auto vzs = [&](int64_t oo) { return radd(vs[VZ_X * NSP + oo], vs[VZ_Z * NSP + oo]); };
-  T vx = vxs(o), vz = vzs(o);
-  if (g.fsurf && j >= g.jlo && j <= g.jhi) {
-    const int h = g.h;
-    if (i == h - 2) {
-      // vz[h-2] = vz[h-1]; vx[h-2] = vz[h-2,j+1] - vz[h-2,j] + vz[h-1,j+1] - vz[h-1,j] + vx[h,j]
-      const T vz_up = vzs(o + P);                                           // vz[h-1, j]
-      const T vzn_r = (j + 1 <= g.jhi) ? vzs(o + P + 1) : vzs(o + 1);       // vz[h-2, j+1] after the first line
-      vz = vz_up;
-      vx = radd(rsub(radd(rsub(vzn_r, vz_up), vzs(o + P + 1)), vz_up), vxs(o + 2 * P));
-    } else if (i == h - 3) {
-      vz = vzs(o + 2 * P);  // vz[h-3] = vz[h-2] = vz[h-1]
-    }
-  }
-  v[VX * NSP + o] = vx;
-  v[VZ * NSP + o] = vz;
-}
-
-// ---- fused forms: the split update of a cell and its totals in one pass; the rows whose
-// totals read other rows (free surface) are left to the *_fs_rows kernels that follow.
+// Split-field update of a cell and its totals in one pass (elastic_kernels.py:351-402); the rows
+// whose totals read other rows (free surface) are left to the *_fs_rows kernels that follow.
 template <typename T>
 __device__ __forceinline__ bool stress_fs_row(const Geo<T>& g, int i) {
   return g.fsurf && i >= g.h - 3 && i <= g.h - 1;

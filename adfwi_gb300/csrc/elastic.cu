@@ -231,6 +231,38 @@ struct StagedQ {
   __device__ __forceinline__ T operator()(int ii, int jj) const { return s[(ii - i0 + 3) * kSW + (jj - j0 + 4)]; }
 };
 
+// Compact staged planes: an x plane holds only the tile rows with the x halo (kTileZ x kSW), a z
+// plane only the tile columns with the z halo (kSZ x kTileX).
+constexpr int kXPlane = kTileZ * kSW, kZPlane = kSZ * kTileX;
+template <typename T>
+__device__ __forceinline__ void stage_x(T* dst, const T* plane, const Layout& L, int i0, int j0) {
+  constexpr int E = 16 / (int)sizeof(T), cols = kSW / E;
+  for (int t = threadIdx.x; t < kTileZ * cols; t += kTileThreads) {
+    const int r = t / cols, c = t - r * cols;
+    cp_async16(dst + r * kSW + c * E, plane + L.off(i0 + r, j0 - 4 + c * E));
+  }
+}
+template <typename T>
+__device__ __forceinline__ void stage_z(T* dst, const T* plane, const Layout& L, int i0, int j0) {
+  constexpr int E = 16 / (int)sizeof(T), cols = kTileX / E;
+  for (int t = threadIdx.x; t < kSZ * cols; t += kTileThreads) {
+    const int r = t / cols, c = t - r * cols;
+    cp_async16(dst + r * kTileX + c * E, plane + L.off(i0 - 3 + r, j0 + c * E));
+  }
+}
+template <typename T>
+struct StagedX {
+  const T* s;
+  int i0, j0;
+  __device__ __forceinline__ T operator()(int ii, int jj) const { return s[(ii - i0) * kSW + (jj - j0 + 4)]; }
+};
+template <typename T>
+struct StagedZ {
+  const T* s;
+  int i0, j0;
+  __device__ __forceinline__ T operator()(int ii, int jj) const { return s[(ii - i0 + 3) * kTileX + (jj - j0)]; }
+};
+
 // ======================================================================= forward, PML
 // Split-field update of a cell and its totals in one pass (elastic_kernels.py:351-402); the rows
 // whose totals read other rows (free surface) are left to the *_fs_rows kernels that follow.
@@ -972,10 +1004,11 @@ __global__ void __launch_bounds__(kTileThreads)
 // tile's cell coefficients C11 .. C55 and PML factors dt/dx / pml_xd, dt/dz / pml_zd (zero outside
 // I) are staged once with the full halo; per shot the lambda of the six split stresses and vx, vz
 // of the forward history are staged, the eight sources q (sx_b, sx_zb, sx_f, sx_zf, sz_b, sz_zb,
-// sz_f, sz_zf: coefficient-weighted lambda, zero outside I) formed at every staged cell, and the
-// transposes and gradients evaluated from them. Planes: 0-5 C, 6-7 factors, 8-13 lambda,
-// 14-15 vx, vz, 16-23 q.
-constexpr int kAdjVPmlPlanes = 24;
+// sz_f, sz_zf: coefficient-weighted lambda, zero outside I) formed where their differences read
+// them, and the transposes and gradients evaluated from them. C, the factors, vx and vz are full
+// staged planes; the x parts of lambda and the sources of x differences are compact x planes,
+// the z ones compact z planes (43.9 KB in single precision: 5 blocks per SM).
+constexpr int kAdjVPmlElems = 10 * kSPlane + 7 * kXPlane + 7 * kZPlane;  // C, factors, vx, vz; lambda, q
 template <typename T, int NN>
 __global__ void __launch_bounds__(kTileThreads)
     adj_v_pml(Geo<T> g, const T* __restrict__ cf, const T* __restrict__ lts, T* __restrict__ lv,
@@ -983,18 +1016,20 @@ __global__ void __launch_bounds__(kTileThreads)
   griddep_wait();  // launched with programmatic serialisation in the PML time loops
   griddep_launch_dependents();
   extern __shared__ __align__(16) unsigned char el_smem[];
-  T* sC = reinterpret_cast<T*>(el_smem);
-  T* sK = sC + 6 * kSPlane;
-  T* sL = sC + 8 * kSPlane;
-  T* sV = sC + 14 * kSPlane;
-  T* sQ = sC + 16 * kSPlane;
+  T* sC = reinterpret_cast<T*>(el_smem);  // 6 full planes
+  T* sK = sC + 6 * kSPlane;                // kx, kz (full)
+  T* sV = sC + 8 * kSPlane;                // vx, vz (full)
+  T* sLx = sC + 10 * kSPlane;              // lambda txx_x, tzz_x, txz_x (x planes)
+  T* sLz = sLx + 3 * kXPlane;              // lambda txx_z, tzz_z, txz_z (z planes)
+  T* sQx = sLz + 3 * kZPlane;              // q0, q2, q4, q6 (x planes)
+  T* sQz = sQx + 4 * kXPlane;              // q1, q3, q5, q7 (z planes)
   const int tiles_x = (g.L.nxp + kTileX - 1) / kTileX;
   const int i0 = ((int)blockIdx.x / tiles_x) * kTileZ, j0 = ((int)blockIdx.x % tiles_x) * kTileX;
   const int ty = (int)threadIdx.x / kTileX, tx = (int)threadIdx.x % kTileX;
   const int i = i0 + ty, j = j0 + tx;
   const bool valid = i < g.L.nzp && j < g.L.nxp, inside = valid && in_I(g, i, j);
   const int64_t PL = g.L.plane, NSP = (int64_t)g.ns * PL, oc = g.L.off(i, j);
-  const int sc = kSC + ty * kSW + tx;
+  const int sc = kSC + ty * kSW + tx, cx = ty * kSW + tx + 4, cz = (ty + 3) * kTileX + tx;
   EL_SHOT_GROUP
   T* gc = gbase;
 #pragma unroll
@@ -1017,44 +1052,71 @@ __global__ void __launch_bounds__(kTileThreads)
   T g11 = T(0), g13 = T(0), g15 = T(0), g33 = T(0), g35 = T(0), g55 = T(0);
   for (int s = s_beg; s < s_end; ++s) {
     const int64_t so = (int64_t)s * PL;
+    // the x parts of the split stresses feed the sources of x differences, the z parts those of
+    // z differences
 #pragma unroll
-    for (int k = 0; k < 6; ++k) stage(sL + k * kSPlane, lts + k * NSP + so, g.L, i0, j0, 3, 4);
+    for (int k = 0; k < 3; ++k) {
+      stage_x(sLx + k * kXPlane, lts + (2 * k) * NSP + so, g.L, i0, j0);
+      stage_z(sLz + k * kZPlane, lts + (2 * k + 1) * NSP + so, g.L, i0, j0);
+    }
     stage(sV, v_hist + VX * NSP + so, g.L, i0, j0, 3, 4);
     stage(sV + kSPlane, v_hist + VZ * NSP + so, g.L, i0, j0, 3, 4);
     cp_async_wait_all();
     __syncthreads();
-    for (int t = threadIdx.x; t < kSPlane; t += kTileThreads) {
-      const T kx = sK[t], kz = sK[kSPlane + t];
-      T q[8] = {T(0), T(0), T(0), T(0), T(0), T(0), T(0), T(0)};
-      if (kx != T(0)) {  // inside I (the factors are positive there)
-        const T ra = sL[t] * kx, rb = sL[kSPlane + t] * kz, rc = sL[2 * kSPlane + t] * kx;
-        const T rd = sL[3 * kSPlane + t] * kz, re = sL[4 * kSPlane + t] * kx, rf = sL[5 * kSPlane + t] * kz;
-        const T c11 = sC[t], c13 = sC[kSPlane + t], c15 = sC[2 * kSPlane + t];
-        const T c33 = sC[3 * kSPlane + t], c35 = sC[4 * kSPlane + t], c55 = sC[5 * kSPlane + t];
-        q[0] = c11 * ra + c13 * rc;
-        q[1] = c15 * rb + c35 * rd;
-        q[2] = c15 * re;
-        q[3] = c55 * rf;
-        q[4] = c15 * ra + c35 * rc;
-        q[5] = c13 * rb + c33 * rd;
-        q[6] = c55 * re;
-        q[7] = c35 * rf;
+    for (int t = threadIdx.x; t < kXPlane; t += kTileThreads) {  // q0, q2, q4, q6
+      const int u = 3 * kSW + t;                                  // the same cell in a full plane
+      const T kx = sK[u];
+      T a = T(0), b = T(0), c = T(0), d = T(0);
+      if (kx != T(0)) {  // inside I (the factor is positive there)
+        const T ra = sLx[t] * kx, rc = sLx[kXPlane + t] * kx, re = sLx[2 * kXPlane + t] * kx;
+        const T c15 = sC[2 * kSPlane + u];
+        a = sC[u] * ra + sC[kSPlane + u] * rc;
+        b = c15 * re;
+        c = c15 * ra + sC[4 * kSPlane + u] * rc;
+        d = sC[5 * kSPlane + u] * re;
       }
-#pragma unroll
-      for (int k = 0; k < 8; ++k) sQ[k * kSPlane + t] = q[k];
+      sQx[t] = a;
+      sQx[kXPlane + t] = b;
+      sQx[2 * kXPlane + t] = c;
+      sQx[3 * kXPlane + t] = d;
+    }
+    for (int t = threadIdx.x; t < kZPlane; t += kTileThreads) {  // q1, q3, q5, q7
+      const int u = (t / kTileX) * kSW + 4 + t % kTileX;
+      const T kz = sK[kSPlane + u];
+      T a = T(0), b = T(0), c = T(0), d = T(0);
+      if (kz != T(0)) {
+        const T rb = sLz[t] * kz, rd = sLz[kZPlane + t] * kz, rf = sLz[2 * kZPlane + t] * kz;
+        const T c35 = sC[4 * kSPlane + u];
+        a = sC[2 * kSPlane + u] * rb + c35 * rd;
+        b = sC[5 * kSPlane + u] * rf;
+        c = sC[kSPlane + u] * rb + sC[3 * kSPlane + u] * rd;
+        d = c35 * rf;
+      }
+      sQz[t] = a;
+      sQz[kZPlane + t] = b;
+      sQz[2 * kZPlane + t] = c;
+      sQz[3 * kZPlane + t] = d;
     }
     __syncthreads();
     if (valid) {
-      const StagedQ<T> q0{sQ, i0, j0}, q1{sQ + kSPlane, i0, j0}, q2{sQ + 2 * kSPlane, i0, j0},
-          q3{sQ + 3 * kSPlane, i0, j0}, q4{sQ + 4 * kSPlane, i0, j0}, q5{sQ + 5 * kSPlane, i0, j0},
-          q6{sQ + 6 * kSPlane, i0, j0}, q7{sQ + 7 * kSPlane, i0, j0};
+      const StagedX<T> q0{sQx, i0, j0}, q2{sQx + kXPlane, i0, j0}, q4{sQx + 2 * kXPlane, i0, j0},
+          q6{sQx + 3 * kXPlane, i0, j0};
+      const StagedZ<T> q1{sQz, i0, j0}, q3{sQz + kZPlane, i0, j0}, q5{sQz + 2 * kZPlane, i0, j0},
+          q7{sQz + 3 * kZPlane, i0, j0};
       const T avx = dxb_t<NN>(g, q0, i, j) + dzb_t<NN>(g, q1, i, j) + dxf_t<NN>(g, q2, i, j) + dzf_t<NN>(g, q3, i, j);
       const T avz = dxb_t<NN>(g, q4, i, j) + dzb_t<NN>(g, q5, i, j) + dxf_t<NN>(g, q6, i, j) + dzf_t<NN>(g, q7, i, j);
       const int64_t o = so + oc;
       lv[VX * NSP + o] = avx;
       lv[VZ * NSP + o] = avz;
       if (inside) {
-        const StressQ<T> r = stress_q<T, true>(sL + sc, 0, kSPlane, sK[sc], sK[kSPlane + sc]);
+        const T kx = sK[sc], kz = sK[kSPlane + sc];
+        StressQ<T> r;  // the stress update's sources at the cell (stress_q's PML form)
+        r.a = sLx[cx] * kx;
+        r.b = sLz[cz] * kz;
+        r.c = sLx[kXPlane + cx] * kx;
+        r.d = sLz[kZPlane + cz] * kz;
+        r.e = sLx[2 * kXPlane + cx] * kx;
+        r.f = sLz[2 * kZPlane + cz] * kz;
         const T* vx = sV;
         const T* vz = sV + kSPlane;
         const T dxb_vx = dxb<NN>(g, vx, sc), dxb_vz = dxb<NN>(g, vz, sc);
@@ -1538,7 +1600,7 @@ int ebackward(const adfwi_elastic_plan* p, const void* wavelet, const void* grec
   const dim3 gcm = cells_grid(p, (ns + el::kCellShots - 1) / el::kCellShots);
   // shared memory of the staged gradient kernels (above the 48 KB default in double precision)
   const int smem_t = el::kAdjTPlanes * el::kSPlane * (int)sizeof(T);
-  const int smem_vp = el::kAdjVPmlPlanes * el::kSPlane * (int)sizeof(T);
+  const int smem_vp = el::kAdjVPmlElems * (int)sizeof(T);
   const int smem_va = el::adj_v_planes<false>() * el::kSPlane * (int)sizeof(T);
   ADFWI_CUDA_TRY(cudaFuncSetAttribute(el::adj_t_pml<T, NN>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_t));
   ADFWI_CUDA_TRY(cudaFuncSetAttribute(el::adj_v_pml<T, NN>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_vp));

@@ -191,3 +191,26 @@ def test_bad_geometry_is_rejected_on_the_host():
     survey.source.loc_x[0] = 10 ** 6
     with pytest.raises(Exception):
         A.AcousticPropagator(model, survey, device="cuda:0").forward()
+
+
+def test_full_size_gradient_is_additive_over_shots():
+    """The 200 x 600 gradient workload at full size (30 shots, 300 x 700 padded, nt = 3000,
+    600 receivers, pressure records): gradients are sums over shots, so the 30-shot gradient
+    equals the sum of three 10-shot gradients (different unit groupings and partial sums) to
+    rounding."""
+    from adfwi_gb300.synthetic import acoustic_gradient_case
+    model, survey, _, _ = acoustic_gradient_case(seed=0, device="cuda:0", nt=3000)
+    prop = A.AcousticPropagator(model, survey, device="cuda:0")
+    w = torch.randn((30, 3000, prop.rcv_n), generator=torch.Generator().manual_seed(8)).cuda()
+
+    def grad(idx):
+        model.vp.grad = None
+        rec = prop.forward(shot_index=idx)
+        sel = list(range(30)) if idx is None else idx
+        (rec["p"] * w[sel]).sum().backward()
+        return model.vp.grad.detach().clone()
+
+    g_all = grad(None)
+    g_sum = sum(grad(list(range(b, b + 10))) for b in (0, 10, 20))
+    assert torch.isfinite(g_all).all()
+    assert rel(g_all, g_sum) <= 1e-5, rel(g_all, g_sum)

@@ -154,6 +154,12 @@ class AcousticPlan(object):
         return ga1, ga2
 
 
+def _raise_on_status(code):
+    if code != 0:
+        raise RuntimeError("adfwi_gb300: a pipeline wait timed out on the GPU during this solve (status %d); "
+                           "its results are invalid" % code)
+
+
 class AcousticSolve(torch.autograd.Function):
     """records, forward wavefields = solve(alpha1, alpha2); backward = hand-written adjoint."""
 
@@ -168,6 +174,10 @@ class AcousticSolve(torch.autograd.Function):
         # to allocate and inject)
         ctx.set_materialize_grads(False)
         rp, ru, rw, fp, fu, fw, ws = plan.run_forward(alpha1, alpha2, damp, wavelet, need_grad)
+        if not need_grad:
+            # no backward will read the device status of this solve: check it now (a gradient
+            # solve is checked after its adjoint, which covers both passes)
+            _raise_on_status(plan.status(ws, False))
         ctx.plan = plan
         ctx.ws = ws if need_grad else None
         ctx.save_for_backward(alpha1, alpha2, damp, wavelet)
@@ -181,9 +191,6 @@ class AcousticSolve(torch.autograd.Function):
             raise RuntimeError("AcousticSolve.backward: the forward kept no snapshots (inputs did not require "
                                "grad) or they were already used by an earlier backward; run forward again")
         ga1, ga2 = ctx.plan.run_backward(alpha1, alpha2, damp, wavelet, (grp, gru, grw), ctx.ws)
-        code = ctx.plan.status(ctx.ws, True)
-        if code != 0:
-            raise RuntimeError("adfwi_gb300: a pipeline wait timed out on the GPU during this solve (status %d); "
-                               "its results are invalid" % code)
+        _raise_on_status(ctx.plan.status(ctx.ws, True))
         ctx.ws = None  # release the snapshot workspace as soon as the adjoint has consumed it
         return ga1, ga2, None, None, None

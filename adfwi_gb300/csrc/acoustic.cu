@@ -438,15 +438,25 @@ int launch_adj(const adfwi_acoustic_plan* p, const ac::Geo<T>& g, int it, const 
   return kOk;
 }
 
+// The opt-in above 48 KB of dynamic shared memory is a property of the kernel in one device's
+// context, so it is set once per device ordinal (and per element type), under a mutex: the
+// serving workers call solves from several threads, and a process may drive more than one GPU.
+std::mutex g_smem_mu;
+std::vector<unsigned char> g_smem_done;  // bit 0: float kernels, bit 1: double kernels, per device
+
 template <typename T>
 int set_smem_limits() {
-  static bool done = false;
-  if (!done) {
+  int dev = 0;
+  ADFWI_CUDA_TRY(cudaGetDevice(&dev));
+  const unsigned char bit = sizeof(T) == 8 ? 2 : 1;
+  std::lock_guard<std::mutex> lk(g_smem_mu);
+  if ((int)g_smem_done.size() <= dev) g_smem_done.resize(dev + 1, 0);
+  if (!(g_smem_done[dev] & bit)) {
     ADFWI_CUDA_TRY(cudaFuncSetAttribute(ac2::fwd_step_vec<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         ac2::VecFwdLayout<T>::bytes(vec_stages<T>())));
     ADFWI_CUDA_TRY(cudaFuncSetAttribute(ac2::adj_step_vec<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         ac2::VecAdjLayout<T>::bytes(vec_adj_stages<T>())));
-    done = true;
+    g_smem_done[dev] |= bit;
   }
   return kOk;
 }
@@ -774,6 +784,22 @@ int adfwi_acoustic_forward_noalloc(const adfwi_acoustic_plan* p, const void* alp
                                 kStaticScratchBytes, st);
   return forward_impl<float>(p, alpha1, alpha2, damp, wavelet, rec_p, rec_u, rec_w, fw_p, fw_u, fw_w, false, w,
                              kStaticScratchBytes, st);
+}
+
+int adfwi_acoustic_noalloc_status(const adfwi_acoustic_plan* p, int32_t* status, void* stream) {
+  ADFWI_CHECK_ARG(p && status, "null argument");
+  const Carve c = carve(p, false, 1);
+  ADFWI_CHECK_ARG(c.total <= kStaticScratchBytes, "this plan's forward does not fit the static scratch array");
+  void* ws = nullptr;
+  int rc = static_scratch_address(&ws);
+  if (rc) return rc;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  int32_t v = 0;
+  ADFWI_CUDA_TRY(cudaMemcpyAsync(&v, static_cast<const unsigned char*>(ws) + c.flag, sizeof(v),
+                                 cudaMemcpyDeviceToHost, st));
+  ADFWI_CUDA_TRY(cudaStreamSynchronize(st));
+  *status = v;
+  return kOk;
 }
 
 int adfwi_acoustic_plan_create(const adfwi_acoustic_desc* desc, const int32_t* src_z, const int32_t* src_x,

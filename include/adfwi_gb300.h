@@ -219,6 +219,14 @@ int adfwi_acoustic_forward_noalloc(const adfwi_acoustic_plan* plan, const void* 
                                    void* rec_p, void* rec_u, void* rec_w, void* fw_p, void* fw_u,
                                    void* fw_w, void* stream);
 
+/* Device status of the last adfwi_acoustic_forward_noalloc call made with `plan` on the
+ * current device: 0 = clean, 1 = a bounded pipeline wait inside a kernel ran out (the records
+ * and wavefields of that call are invalid). The allocation-free forward keeps its error flag in
+ * the library's static scratch array, whose address callers never see, so this is the way to
+ * read it (the counterpart of adfwi_acoustic_status for workspace solves). Waits for the
+ * stream; a later allocation-free call on the device overwrites the flag. */
+int adfwi_acoustic_noalloc_status(const adfwi_acoustic_plan* plan, int32_t* status, void* stream);
+
 /* ------------------------------------------------------------------------- */
 /* Errors and build information.                                             */
 /* ------------------------------------------------------------------------- */

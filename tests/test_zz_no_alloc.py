@@ -36,6 +36,15 @@ def _inputs(seed, **kw):
     return plan, a1, a2, prop.damp, prop.wavelet.contiguous()
 
 
+def _noalloc_status(plan, dev):
+    fn = N.lib().adfwi_acoustic_noalloc_status
+    fn.restype = ctypes.c_int32
+    fn.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32), ctypes.c_void_p]
+    v = ctypes.c_int32(-1)
+    N.check(fn(plan.handle, ctypes.byref(v), N.stream_handle(dev)), "adfwi_acoustic_noalloc_status")
+    return v.value
+
+
 def _call_noalloc(plan, a1, a2, damp, wav):
     dev = a1.device
     rec = [torch.empty((plan.ns, plan.nt, plan.nr), dtype=plan.dtype, device=dev) for _ in range(3)]
@@ -53,6 +62,8 @@ def test_noalloc_forward_matches_workspace_forward_twice(dtype):
         plan, a1, a2, damp, wav = _inputs(seed, dtype=dtype, **kw)
         assert plan.workspace_bytes(False) <= 64 << 20
         got = _call_noalloc(plan, a1, a2, damp, wav)
+        # the call's bounded pipeline waits all completed (its error flag lives in the static array)
+        assert _noalloc_status(plan, a1.device) == 0
         want = plan.run_forward(a1, a2, damp, wav, False)[:6]
         torch.cuda.synchronize()
         for g, w in zip(got, want):

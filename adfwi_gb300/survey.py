@@ -190,3 +190,19 @@ class SeismicData(object):
         self.t = d["t"]
         self.nt = d["nt"]
         self.dt = d["dt"]
+
+    @staticmethod
+    def _peak_normalised(a):
+        return a / np.max(np.abs(a), axis=1, keepdims=True)
+
+    def parse_elastic_data(self, normalize=False):
+        """(pressure = -(txx + tzz), txz, vx, vz) of elastic records, each optionally divided by
+        its traces' max |value| along time (data.py:100-113)."""
+        d = self.data
+        out = [-(d["txx"] + d["tzz"]), d["txz"], d["vx"], d["vz"]]
+        return tuple(self._peak_normalised(a) for a in out) if normalize else tuple(out)
+
+    def parse_acoustic_data(self, normalize=False):
+        """(p, u, w) of acoustic records, optionally trace-normalised (data.py:115-123)."""
+        out = [self.data["p"], self.data["u"], self.data["w"]]
+        return tuple(self._peak_normalised(a) for a in out) if normalize else tuple(out)

@@ -173,6 +173,7 @@ def l2_misfit(syn, obs, dt):
 def gpu_arm(args, world, rank, local):
     import adfwi_gb300 as A
     from adfwi_gb300 import _native as N
+    from adfwi_gb300.misfit import l2_misfit as cuda_l2_misfit
     from adfwi_gb300.synthetic import acoustic_gradient_case
 
     dev = torch.device("cuda", local)
@@ -194,7 +195,9 @@ def gpu_arm(args, world, rank, local):
         model.vp.data.copy_(vp0)
         model.vp.grad = None
         rec = prop.forward()
-        loss = l2_misfit(rec["p"], obs_dev, dt)
+        # normalised L2 (the CUDA misfit: trace peaks, FP64 sums and the adjoint source in one
+        # pass set; obs is normalised once at setup, as acoustic_fwi.py does)
+        loss = cuda_l2_misfit(rec["p"], obs_dev, dt, silent_rel=0.0, normalise_obs=False)
         loss.backward()
         return loss
 
@@ -284,6 +287,222 @@ def gpu_arm(args, world, rank, local):
     return line
 
 
+def _device_time(fn, dev, warmup, reps):
+    """Mean device time (CUDA events on the current stream) of fn() over reps calls after warmup."""
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        fn()
+    e1.record()
+    torch.cuda.synchronize(dev)
+    return e0.elapsed_time(e1) / reps
+
+
+def _kernel_roofline(N, stats, cls, cells_launch):
+    """Roofline of one kernel class from the library's per-launch event timing."""
+    peak, kind = peaks()
+    if cls not in stats or stats[cls][1] == 0:
+        return None
+    _, tl, tot = stats[cls]
+    avg_s = tot / tl * 1e-3
+    algo = ALGO_BYTES[cls] * cells_launch
+    tr = ncu_traffic().get(cls)
+    return {"bound": "hbm", "kernel": cls, "achieved": round(algo / avg_s / 1e9, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(algo / avg_s / 1e9 / peak, 4), "peak_source": kind,
+            "traffic": None if tr is None else tr[0] * cells_launch / tr[1],
+            "algorithmic_bytes_per_launch": algo, "avg_launch_ms": round(avg_s * 1e3, 5)}
+
+
+def fp64_error(args, dev, memory_fraction):
+    """Error of the headline FP32 gradient (and records, loss) against an FP64 run of the same
+    scheme on the same inputs (untimed): the 200 x 600 workload in both precisions."""
+    import adfwi_gb300 as A
+    from adfwi_gb300.misfit import l2_misfit as cuda_l2_misfit
+    from adfwi_gb300.synthetic import acoustic_gradient_case
+    res = {}
+    for dtype in (torch.float64, torch.float32):
+        model, survey, vp_true, vp_init = acoustic_gradient_case(seed=0, device=str(dev), nt=args.nt, dtype=dtype)
+        free, _ = torch.cuda.mem_get_info(dev)
+        prop = A.AcousticPropagator(model, survey, device=str(dev), dtype=dtype,
+                                    memory_budget=int(memory_fraction * free))
+        with torch.no_grad():
+            model.vp.data.copy_(torch.as_tensor(vp_true, device=dev))
+            obs = prop.forward()["p"]
+            obs = (obs / torch.max(torch.abs(obs), dim=1, keepdim=True).values).contiguous()
+        model.vp.data.copy_(torch.as_tensor(vp_init, device=dev))
+        rec = prop.forward()
+        loss = cuda_l2_misfit(rec["p"], obs, prop.dt, silent_rel=0.0, normalise_obs=False)
+        loss.backward()
+        res[dtype] = (rec["p"].detach().double(), model.vp.grad.detach().double(), float(loss),
+                      prop.plan()[1].snapshot_every)
+        del model, prop, rec, obs
+        torch.cuda.empty_cache()
+    r64, g64, l64, k64 = res[torch.float64]
+    r32, g32, l32, _ = res[torch.float32]
+    rel = lambda a, b: float((a - b).norm() / b.norm())  # noqa: E731
+    return {"grad_vp_rel_l2": rel(g32, g64), "records_p_rel_l2": rel(r32, r64), "loss_rel": abs(l32 - l64) / abs(l64),
+            "fp64_snapshot_every": k64,
+            "how": "same inputs, FP64 stencils and FP64 history/snapshots on the GPU; relative L2 over the whole array"}
+
+
+def forward_legs(args, dev):
+    """Forward-only solves (records, no gradient): the 100 x 100 configuration in full (PML 50,
+    200 x 200 padded, 10 shots, 100 receivers, nt = 1000, dt = 1 ms, 10 Hz) and the 200 x 600
+    workload's forward (30 shots, 300 x 700 padded, 600 receivers, nt = 3000)."""
+    import adfwi_gb300 as A
+    from adfwi_gb300 import _native as N
+    from adfwi_gb300.synthetic import acoustic_gradient_case, linear_gradient_with_anomaly, surface_acquisition
+    out = {}
+    vp1 = linear_gradient_with_anomaly(100, 100).astype(np.float32)
+    m1 = A.AcousticModel(0, 0, 100, 100, 10.0, 10.0, vp=vp1, rho=np.power(vp1, 0.25) * 310, nabc=50, device=str(dev))
+    p1 = A.AcousticPropagator(m1, surface_acquisition(100, 1000, 1e-3, 10.0, 10), device=str(dev))
+    m2, s2, _, _ = acoustic_gradient_case(seed=0, device=str(dev), nt=args.nt)
+    p2 = A.AcousticPropagator(m2, s2, device=str(dev))
+    for name, model, prop, reps in (("c1_100x100", m1, p1, 10), ("c2_200x600", m2, p2, 3)):
+        nzp, nxp = prop.nz + 2 * prop.nabc, prop.nx + 2 * prop.nabc
+        cells = prop.src_n * nzp * nxp * prop.nt
+
+        def solve():
+            with torch.no_grad():
+                return prop.forward()
+
+        ms = _device_time(solve, dev, 2, reps)
+        # e2e: vp from pinned host memory in, the three record arrays back to pinned host memory
+        vp_host = model.vp.detach().cpu().pin_memory()
+        recs_host = [torch.empty((prop.src_n, prop.nt, prop.rcv_n)).pin_memory() for _ in range(3)]
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            model.vp.data.copy_(vp_host, non_blocking=True)
+            r = solve()
+            for h, k in zip(recs_host, "puw"):
+                h.copy_(r[k], non_blocking=True)
+            torch.cuda.synchronize(dev)
+        e2e = cells * reps / (time.perf_counter() - t0) / 1e9
+        N.profile_start(True)
+        solve()
+        torch.cuda.synchronize(dev)
+        roof = _kernel_roofline(N, N.profile_stop(), "acoustic_fwd_step", prop.src_n * nzp * nxp)
+        l2 = 4 * 3 * 2 * prop.src_n * nzp * nxp > 129e6
+        out[name] = {"value": round(cells / (ms * 1e-3) / 1e9, 3), "unit": UNIT, "ms_per_solve": round(ms, 3),
+                     "reps": reps, "shots": prop.src_n, "nt": prop.nt, "grid_padded": [nzp, nxp],
+                     "receivers": prop.rcv_n,
+                     "e2e": {"value": round(e2e, 3), "unit": UNIT,
+                             "h2d_bytes_per_step": vp_host.numel() * 4,
+                             "d2h_bytes_per_step": sum(h.numel() * 4 for h in recs_host)},
+                     "roofline": roof if l2 else None,
+                     "roofline_note": None if l2 else "fields fit in L2 (129 MB): no HBM roofline reported"}
+    return out
+
+
+def checkpointed_leg(args, dev):
+    """Checkpointed gradient on the 500 x 1500 precision configuration (dx = 12.5 m, PML 50 ->
+    600 x 1600 padded, nt = 6000, dt = 1 ms, 10 Hz Ricker, snapshots every 50 steps, 1500
+    receivers): FP32 stencils with the snapshots in FP32, BF16 and FP16 (one max-abs scale per
+    snapshot, shot and field), timed; errors of records and dL/dvp (L = sum of records x fixed
+    random traces) against an FP64 run of the same scheme with FP64 snapshots (untimed)."""
+    import adfwi_gb300 as A
+    from adfwi_gb300.synthetic import linear_gradient_with_anomaly, surface_acquisition
+    nz, nx, dx, nt, dt, f0 = 500, 1500, 12.5, args.ckpt_nt, 1e-3, 10.0
+    vp = linear_gradient_with_anomaly(nz, nx)
+    sv = surface_acquisition(nx, nt, dt, f0, 64)
+    idx = np.arange(0, 64, 64 // args.ckpt_shots)[:args.ckpt_shots]
+    gen = torch.Generator(device=dev).manual_seed(0)
+    wts = torch.randn((len(idx), nt, nx), generator=gen, device=dev, dtype=torch.float64)
+    runs = [("fp64", torch.float64, "native"), ("fp32", torch.float32, "native"),
+            ("fp32_bf16", torch.float32, "bf16"), ("fp32_fp16", torch.float32, "fp16")]
+    got = {}
+    for name, dtype, prec in runs:
+        npdt = np.float64 if dtype == torch.float64 else np.float32
+        model = A.AcousticModel(0, 0, nx, nz, dx, dx, vp=vp.astype(npdt), rho=(np.power(vp, 0.25) * 310).astype(npdt),
+                                vp_grad=True, nabc=50, device=str(dev), dtype=dtype)
+        prop = A.AcousticPropagator(model, sv, device=str(dev), dtype=dtype, snapshot_precision=prec,
+                                    snapshot_every=50)
+        w = wts.to(dtype)
+
+        def grad():
+            model.vp.grad = None
+            rec = prop.forward(shot_index=idx)
+            (rec["p"] * w).sum().backward()
+            return rec
+
+        ms = None
+        if name != "fp64":
+            grad()  # warm-up (plan, first launches)
+            torch.cuda.synchronize(dev)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+        rec = grad()
+        if name != "fp64":
+            e1.record()
+        torch.cuda.synchronize(dev)
+        if name != "fp64":
+            ms = e0.elapsed_time(e1)
+        got[name] = (rec["p"].detach().double(), model.vp.grad.detach().double(), ms)
+        del model, prop, rec
+        torch.cuda.empty_cache()
+    peak, kind = peaks()
+    cells = len(idx) * (nz + 100) * (nx + 100) * nt
+    r64, g64, _ = got["fp64"]
+    rel = lambda a, b: float((a - b).norm() / b.norm())  # noqa: E731
+    res = {}
+    for name, (r, g, ms) in got.items():
+        if name == "fp64":
+            continue
+        v = cells / (ms * 1e-3) / 1e9
+        res[name] = {"value": round(v, 3), "unit": UNIT, "ms_per_gradient": round(ms, 1),
+                     "records_rel_l2_vs_fp64": rel(r, r64), "grad_vp_rel_l2_vs_fp64": rel(g, g64),
+                     "roofline": {"bound": "hbm", "bytes_per_cell_update": GRAD_BYTES,
+                                  "achieved": round(v * GRAD_BYTES, 1), "peak": peak, "unit": "GB/s",
+                                  "frac": round(v * GRAD_BYTES / peak, 4), "peak_source": kind,
+                                  "scope": "whole checkpointed gradient (forward, recompute, adjoint, snapshots)"}}
+    return {"workload": "checkpointed gradient, 500x1500 model (600x1600 padded), nt=%d, snapshots every 50 steps, "
+                        "%d of the 64 surface shots (every %dth), 1500 receivers" % (nt, len(idx), 64 // args.ckpt_shots),
+            "shots": len(idx), "nt": nt, "snapshot_every": 50, "results": res}
+
+
+def plain_gpu_leg(args, dev):
+    """The plain GPU path against the library on one gradient sample: the 200 x 600 workload
+    (30 shots, 300 x 700 padded, 600 receivers) cut to 100 time steps, L = sum of the pressure
+    records x fixed random traces. The plain path is the reference's algorithm as PyTorch tensor
+    operations (the oracle's loop, bit-identical to the reference's records on the CPU) on CUDA
+    tensors, each time chunk under torch.utils.checkpoint as the reference's propagator runs it,
+    with autograd for the gradient."""
+    import adfwi_gb300 as A
+    from adfwi_gb300.synthetic import acoustic_gradient_case
+    from oracle.acoustic import acoustic_forward
+    nt = 100
+    model, survey, _, _ = acoustic_gradient_case(seed=0, device=str(dev), nt=nt)
+    prop = A.AcousticPropagator(model, survey, device=str(dev), memory_budget=60 << 30)
+    cells = prop.src_n * (prop.nz + 2 * prop.nabc) * (prop.nx + 2 * prop.nabc) * nt
+    wts = torch.randn((prop.src_n, nt, prop.rcv_n), generator=torch.Generator().manual_seed(0)).to(dev)
+
+    def ours():
+        model.vp.grad = None
+        (prop.forward()["p"] * wts).sum().backward()
+
+    def plain():
+        model.forward()
+        vp = model.vp.detach().clone().requires_grad_(True)
+        out = acoustic_forward(vp, model.rho.detach(), prop.damp, prop.src_loc[:, 0], prop.src_loc[:, 1],
+                               prop.wavelet, prop.rcv_loc[:, 0], prop.rcv_loc[:, 1], nabc=prop.nabc,
+                               free_surface=False, dx=prop.dx, dz=prop.dz, dt=prop.dt, allow_gpu=True,
+                               checkpoint_chunks=True)
+        (out["p"] * wts).sum().backward()
+
+    t_plain = _device_time(plain, dev, 1, 2)
+    t_ours = _device_time(ours, dev, 2, 5)
+    return {"sample": "30 shots x 300x700 padded x %d steps, forward + gradient" % nt,
+            "plain_gpu_gcell_per_s": round(cells / (t_plain * 1e-3) / 1e9, 3),
+            "library_gcell_per_s": round(cells / (t_ours * 1e-3) / 1e9, 3),
+            "speedup_vs_plain_gpu": round(t_plain / t_ours, 2),
+            "plain_path": "oracle loop (reference arithmetic in PyTorch ops) on CUDA, chunks under "
+                          "torch.utils.checkpoint, autograd backward"}
+
+
 def serving_arm(args, dev):
     """Served stream of mixed-size forward+gradient requests (Poisson arrivals, grids from
     {100x300, 200x600, 300x900, 500x1500}, 1-16 shots, nt in {1000, 2000, 4000}, random layered
@@ -345,26 +564,72 @@ def elastic_arm(args, dev):
     rec = step()
     nzp, nxp = prop.padded_coefficients(model, 4)[0][0].shape
     cells = ns * nzp * nxp * nt
-    torch.cuda.synchronize(dev)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    reps = max(1, min(args.steps, 3))
-    e0.record()
-    for _ in range(reps):
-        step()
-    e1.record()
-    torch.cuda.synchronize(dev)
-    ms = e0.elapsed_time(e1) / reps
+    reps = max(3, min(args.steps, 5))
+    ms = _device_time(step, dev, 1, reps)
     _, plan = prop.plan(None, 4)
     value = cells / (ms * 1e-3) / 1e9
+    # e2e: the five model parameters from pinned host memory in, their gradients back out
+    pars = ("vp", "vs", "rho", "eps", "delta")
+    host_in = {k: getattr(model, k).detach().cpu().pin_memory() for k in pars}
+    host_out = {k: torch.empty_like(host_in[k]).pin_memory() for k in pars}
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        for k in pars:
+            getattr(model, k).data.copy_(host_in[k], non_blocking=True)
+        step()
+        for k in pars:
+            host_out[k].copy_(getattr(model, k).grad, non_blocking=True)
+        torch.cuda.synchronize(dev)
+    e2e = cells * reps / (time.perf_counter() - t0) / 1e9
     peak, peak_kind = peaks()
     achieved = value * EL_GRAD_BYTES
-    return {"workload": "VTI elastic gradient (vp, vs, rho, eps, delta): 200x400, PML 40 + free surface "
-                        "(242x480 padded), 4th order, nt=2000, dt=0.8 ms, 20 shots, 400 receivers, FP32",
-            "value": round(value, 3), "unit": UNIT, "ms_per_gradient": round(ms, 2),
-            "steps": reps, "snapshot_every": plan.snapshot_every, "grid_padded": [int(nzp), int(nxp)],
-            "roofline": {"bound": "hbm", "bytes_per_cell_update": EL_GRAD_BYTES, "achieved": round(achieved, 1),
-                         "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": peak_kind,
-                         "scope": "whole gradient (all elastic kernels), algorithmic bytes per cell-update"}}
+    out = {"workload": "VTI elastic gradient (vp, vs, rho, eps, delta): 200x400, PML 40 + free surface "
+                       "(242x480 padded), 4th order, nt=%d, dt=0.8 ms, 20 shots, 400 receivers, FP32" % nt,
+           "value": round(value, 3), "unit": UNIT, "ms_per_gradient": round(ms, 2),
+           "steps": reps, "snapshot_every": plan.snapshot_every, "grid_padded": [int(nzp), int(nxp)],
+           "e2e": {"value": round(e2e, 3), "unit": UNIT, "h2d_bytes_per_step": sum(v.numel() * 4 for v in host_in.values()),
+                   "d2h_bytes_per_step": sum(v.numel() * 4 for v in host_out.values())},
+           "roofline": {"bound": "hbm", "bytes_per_cell_update": EL_GRAD_BYTES, "achieved": round(achieved, 1),
+                        "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": peak_kind,
+                        "scope": "whole gradient (all elastic kernels), algorithmic bytes per cell-update"}}
+    if not args.no_cpu_baseline:
+        out["cpu_baseline"] = elastic_cpu_sample(args.elastic_cpu_steps)
+    return out
+
+
+def elastic_cpu_sample(n_steps, min_seconds=5.0):
+    """CPU oracle (the reference's elastic loop restated in PyTorch, all host threads) on a bounded
+    sample of the VTI workload: 1 shot x n_steps steps of the 242 x 480 padded grid, forward +
+    autograd backward to vp, vs, rho, eps, delta, repeated until min_seconds of work."""
+    from adfwi_gb300.boundary import bc_pml_xz
+    from adfwi_gb300.synthetic import surface_acquisition, vti_layered
+    from oracle.elastic import elastic_forward
+    from oracle.model import elastic_coefficients
+    threads = os.cpu_count() or 1
+    torch.set_num_threads(threads)
+    rng = np.random.default_rng(0)
+    arrs = vti_layered(200, 400, rng)
+    sv = surface_acquisition(400, n_steps, 8e-4, 15.0, 20, src_z=2, rcv_z=1)
+    bcx, bcz = bc_pml_xz(400, 200, 10.0, 10.0, 40, arrs[0].max(), free_surface=True)
+    loc = sv.source.get_loc()[[10]]
+    rl = sv.receiver.get_loc()
+    done, t_all, reps = 0, 0.0, 0
+    while t_all < min_seconds and reps < 20:
+        pars = [torch.tensor(a.astype(np.float32), requires_grad=True) for a in arrs]
+        t0 = time.perf_counter()
+        co = elastic_coefficients(*pars, "vti")
+        out = elastic_forward(co, loc[:, 0], loc[:, 1], torch.tensor(sv.source.get_wavelet()[:1], dtype=torch.float32),
+                              torch.tensor(sv.source.get_moment_tensor()[:1], dtype=torch.float32), rl[:, 0], rl[:, 1],
+                              nabc=40, free_surface=True, dx=10.0, dz=10.0, dt=8e-4, fd_order=4, abc_type="PML",
+                              bcx=bcx, bcz=bcz, damp=None)
+        (out["vx"].square().sum() + out["vz"].square().sum()).backward()
+        t_all += time.perf_counter() - t0
+        done += 242 * 480 * n_steps
+        reps += 1
+    return {"value": round(done / t_all / 1e9, 5), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "%d x (1 shot x %d steps) of the 242x480 padded VTI gradient, CPU oracle forward + autograd "
+                      "backward, %.1f s" % (reps, n_steps, t_all)}
 
 
 def precision_study(args):
@@ -480,6 +745,11 @@ def main():
     ap.add_argument("--elastic-only", action="store_true", help="run only the VTI-elastic gradient measurement")
     ap.add_argument("--elastic-nt", type=int, default=2000,
                     help="time steps of the elastic workload (2000 measured; fewer for profiling captures)")
+    ap.add_argument("--elastic-cpu-steps", type=int, default=100)
+    ap.add_argument("--no-extra-legs", action="store_true",
+                    help="skip the forward-only, checkpointed, FP64-error and plain-GPU legs")
+    ap.add_argument("--ckpt-nt", type=int, default=6000, help="time steps of the checkpointed 500x1500 leg")
+    ap.add_argument("--ckpt-shots", type=int, default=8, help="shots (of 64) of the checkpointed 500x1500 leg")
     ap.add_argument("--precision", action="store_true",
                     help="run only the snapshot-precision study (BF16 / FP16 / FP32 checkpoints vs FP64)")
     ap.add_argument("--precision-nt", type=int, default=6000)
@@ -499,6 +769,16 @@ def main():
             print(json.dumps(elastic_arm(args, torch.device("cuda", local))), flush=True)
         return
     line = gpu_arm(args, world, rank, local)
+    if world == 1 and not args.no_extra_legs:
+        dev = torch.device("cuda", local)
+        torch.cuda.empty_cache()
+        line["accuracy_vs_fp64"] = fp64_error(args, dev, args.memory_fraction)
+        torch.cuda.empty_cache()
+        line["forward_only"] = forward_legs(args, dev)
+        torch.cuda.empty_cache()
+        line["checkpointed"] = checkpointed_leg(args, dev)
+        torch.cuda.empty_cache()
+        line["plain_gpu"] = plain_gpu_leg(args, dev)
     if world == 1 and not args.no_elastic:
         torch.cuda.empty_cache()
         line["elastic"] = elastic_arm(args, torch.device("cuda", local))

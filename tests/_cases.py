@@ -13,6 +13,8 @@ def golden_files(kind=None):
     out = []
     for f in sorted(glob.glob(os.path.join(GOLDEN, "*.npz"))):
         g = np.load(f)
+        if "kind" not in g.files:
+            continue
         k = str(g["kind"])
         if (kind is None and k in ("acoustic", "elastic")) or k == kind:
             out.append(f)

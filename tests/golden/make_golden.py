@@ -8,7 +8,12 @@ None of those stubs touch the propagator arithmetic:
 torch and numpy.
 
 ``gradproc.npz`` holds the reference's ``smooth2d`` and ``GradProcessor.forward`` outputs on
-seeded inputs. Each propagator fixture holds the inputs of one small case, the reference's record dict
+seeded inputs. ``acoustic_c1_full.npz`` is the 100 x 100 forward-only configuration at its full
+size (PML 50, 10 shots, nt = 1000): its inputs, the reference's forward_wavefield_* maps, every
+10th time sample of the pressure records and the FP64 energy of every record trace (the full
+records would be 12 MB). ``seismicdata_ref.npz`` is a file written by the reference's
+``SeismicData.save``, and ``seismicdata_ours_read_by_ref.npz`` holds what the reference's
+``SeismicData.load`` read back from a file written by this package's ``save``. Each propagator fixture holds the inputs of one small case, the reference's record dict
 (``AcousticPropagator.forward`` / ``ElasticPropagator.forward``), its damping
 arrays, and autograd gradients of a fixed linear functional of the records
 (``sum_k <W_k, rec_k>`` with seeded weights), so that gradient parity does
@@ -233,14 +238,105 @@ def gradproc_cases(ref_root):
     print("gradproc", sorted(out))
 
 
+def c1_full_case(R):
+    """The 100 x 100 forward-only configuration at full size, run by the reference: vp linear
+    1500 -> 3000 m/s with depth plus a +300 m/s Gaussian bump (sigma 8 cells) at the centre, rho
+    set by the model's own Gardner map, dx = 10 m, PML 50, no free surface, nt = 1000, dt = 1 ms,
+    10 Hz Ricker, 10 shots at z = 2 evenly spaced in x, 100 receivers at every x, z = 2."""
+    import torch
+    torch.set_default_dtype(torch.float32)
+    nz = nx = 100
+    z = np.arange(nz)[:, None]
+    x = np.arange(nx)[None, :]
+    vp = 1500.0 + 1500.0 * z / (nz - 1) + np.zeros((1, nx))
+    vp = (vp + 300.0 * np.exp(-((z - nz / 2) ** 2 + (x - nx / 2) ** 2) / (2 * 8.0 ** 2))).astype(np.float32)
+    rho = (np.power(vp, 0.25) * 310).astype(np.float32)
+    model = R["AcousticModel"](0, 0, nx, nz, 10.0, 10.0, vp=vp, rho=rho, free_surface=False, abc_type="PML",
+                               nabc=50, device="cpu", dtype=torch.float32)
+    src_x = np.linspace(0, nx - 1, 12)[1:-1].round().astype(int)
+    src_z = np.full(10, 2, dtype=int)
+    rcv_x = np.arange(nx)
+    rcv_z = np.full(nx, 2, dtype=int)
+    survey, _ = build_survey(R, 1000, 1e-3, 10.0, src_x, src_z, rcv_x, rcv_z)
+    prop = R["AcousticPropagator"](model, survey, device="cpu", dtype=torch.float32)
+    with torch.no_grad():
+        rec = prop.forward()
+    out = dict(kind="acoustic_full", nz=nz, nx=nx, nabc=50, nt=1000, dt=1e-3, dx=10.0, f0=10.0,
+               free_surface=False, vp_in=vp, src_x=src_x, src_z=src_z, rcv_x=rcv_x, rcv_z=rcv_z,
+               damp=prop.damp.numpy(), decimate=10)
+    for k in ("p", "u", "w"):
+        r = rec[k].numpy()
+        out["energy_" + k] = np.sum(r.astype(np.float64) ** 2, axis=1)  # (ns, nr)
+    out["rec_p_dec"] = rec["p"].numpy()[:, ::10, :]
+    for k in ("p", "u", "w"):
+        out["forward_wavefield_" + k] = rec["forward_wavefield_" + k].numpy()
+    np.savez_compressed(os.path.join(HERE, "acoustic_c1_full.npz"), **out)
+    print("acoustic_c1_full", {k: np.asarray(v).shape for k, v in out.items() if isinstance(v, np.ndarray)})
+
+
+def seismic_data_files(R):
+    """A file written by the reference's SeismicData.save, and what its load reads from a file
+    written by this package's SeismicData.save (both from the same seeded survey and records)."""
+    import tempfile
+    import torch
+    from ADFWI.survey import SeismicData as RefSeismicData
+    sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+    import adfwi_gb300 as A
+    sys.path.insert(0, HERE)
+    from seismic_case import seismic_data_case
+
+    # the reference's survey and data
+    sv_ref, recs = seismic_data_case(R["Source"], R["Receiver"], R["Survey"], R["wavelet"])
+    d = RefSeismicData(sv_ref)
+    d.record_data({k: torch.tensor(v) for k, v in recs.items()})
+    d.save(os.path.join(HERE, "seismicdata_ref.npz"))
+    # ours, read back by the reference
+    sv_ours, recs2 = seismic_data_case(A.Source, A.Receiver, A.Survey, A.wavelet)
+    e = A.SeismicData(sv_ours)
+    e.record_data({k: torch.tensor(v) for k, v in recs2.items()})
+    with tempfile.TemporaryDirectory() as tmp:
+        path = os.path.join(tmp, "ours.npz")
+        e.save(path)
+        f = RefSeismicData(sv_ref)
+        f.load(path)
+    out = {"kind": "seismicdata"}
+    for k, v in f.data.items():
+        out["data_" + k] = v
+    for k in ("src_loc", "rcv_loc", "src_num", "rcv_num", "rcv_type", "src_type", "t", "nt", "dt"):
+        out[k] = np.asarray(getattr(f, k))
+    np.savez_compressed(os.path.join(HERE, "seismicdata_ours_read_by_ref.npz"), **out)
+    print("seismicdata", sorted(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
-    ap.add_argument("--only", choices=["gradproc"], default=None, help="regenerate one fixture family only")
+    ap.add_argument("--only", choices=["gradproc", "c1", "seismicdata"], default=None,
+                    help="regenerate one fixture family only")
+    ap.add_argument("--read-with-reference", default=None, metavar="NPZ",
+                    help="load NPZ with the reference's SeismicData.load and print a JSON digest of its records")
     args = ap.parse_args()
     R = import_reference(args.ref)
+    if args.read_with_reference:
+        import json
+        from ADFWI.survey import SeismicData as RefSeismicData
+        sys.path.insert(0, HERE)
+        from seismic_case import seismic_data_case
+        sv, _ = seismic_data_case(R["Source"], R["Receiver"], R["Survey"], R["wavelet"])
+        f = RefSeismicData(sv)
+        f.load(args.read_with_reference)
+        dig = {k: [list(v.shape), str(v.dtype), float(np.float64(v).sum()), float(np.abs(np.float64(v)).sum())]
+               for k, v in f.data.items()}
+        print(json.dumps({"data": dig}))
+        return
     if args.only == "gradproc":
         gradproc_cases(args.ref)
+        return
+    if args.only == "c1":
+        c1_full_case(R)
+        return
+    if args.only == "seismicdata":
+        seismic_data_files(R)
         return
     import torch
     torch.set_num_threads(min(8, os.cpu_count() or 1))
@@ -261,6 +357,8 @@ def main():
     elastic_case(R, "elastic_vti_o6_sincos_fs_f32", nt=70, free_surface=True, fd_order=6,
                  abc_type="sincos", iso=False, segments=1, dtype_name="f32", seed=15, **el)
     gradproc_cases(args.ref)
+    c1_full_case(R)
+    seismic_data_files(R)
     # No FP64 elastic fixture: the reference's DiffCoef (elastic_kernels.py:37-56) builds its
     # right-hand side in the default dtype and its matrix in float32, so the elastic propagator
     # raises "expected scalar type Float but found Double" under a float64 default dtype.

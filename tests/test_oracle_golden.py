@@ -84,3 +84,35 @@ def test_oracle_checkpointed_chunks_match_reference(path):
     loss.backward()
     tol = 1e-12 if dt_ == torch.float64 else 1e-6
     assert rel(vp.grad, g["grad_vp"]) < tol
+
+
+def c1_inputs():
+    """Inputs of the full-size 100 x 100 forward configuration recorded in acoustic_c1_full.npz:
+    vp, the Gardner density the reference's model computes from it (float32 numpy, as
+    acoustic_model.py:111-118), damping, wavelets and geometry."""
+    import os
+    from _cases import GOLDEN
+    from adfwi_gb300.utils import wavelet
+    g = np.load(os.path.join(GOLDEN, "acoustic_c1_full.npz"))
+    vp = g["vp_in"]
+    rho = np.power(vp, 0.25) * 310
+    _, w = wavelet(int(g["nt"]), float(g["dt"]), float(g["f0"]))
+    wav = np.tile(w.astype(np.float32), (len(g["src_x"]), 1))
+    return g, vp, rho.astype(np.float32), wav
+
+
+def test_oracle_matches_reference_on_the_full_size_forward_configuration():
+    """100 x 100, PML 50 (200 x 200 padded), 10 shots, 100 receivers, nt = 1000: every
+    forward_wavefield_* map, every 10th pressure sample and the energy of every p, u, w trace
+    equal the reference's bit for bit."""
+    g, vp, rho, wav = c1_inputs()
+    torch.set_num_threads(max(1, min(16, __import__("os").cpu_count() or 1)))
+    with torch.no_grad():
+        out = acoustic_forward(torch.tensor(vp), torch.tensor(rho), torch.tensor(g["damp"]), g["src_x"], g["src_z"],
+                               torch.tensor(wav), g["rcv_x"], g["rcv_z"], nabc=int(g["nabc"]), free_surface=False,
+                               dx=float(g["dx"]), dz=float(g["dx"]), dt=float(g["dt"]))
+    for k in ("p", "u", "w"):
+        e = np.sum(out[k].numpy().astype(np.float64) ** 2, axis=1)
+        assert np.array_equal(e, g["energy_" + k]), k
+        assert np.array_equal(out["forward_wavefield_" + k].numpy(), g["forward_wavefield_" + k]), k
+    assert np.array_equal(out["p"].numpy()[:, ::int(g["decimate"]), :], g["rec_p_dec"])

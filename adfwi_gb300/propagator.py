@@ -151,7 +151,11 @@ class AcousticPropagator(_PropagatorBase):
         n = self.nabc
         c = _pad_replicate(model.vp, n, n, n, n)
         den = _pad_replicate(model.rho, n, n, n, n)
-        alpha1 = den * c * c * self.dt / self.dz
+        # The divisor is a 0-d tensor on the device: PyTorch's CUDA division by a host scalar
+        # multiplies by its reciprocal, which rounds differently from the reference's division
+        # (1 ulp on about a quarter of the cells); an elementwise division rounds like the CPU.
+        dz = torch.tensor(self.dz, dtype=den.dtype, device=den.device)
+        alpha1 = den * c * c * self.dt / dz
         alpha2 = self.dt / (den * self.dz)
         return alpha1, alpha2
 

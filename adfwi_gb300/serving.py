@@ -311,6 +311,7 @@ class _Shape(object):
         self.vp_d = cv.take((self.nz, self.nx), torch.float32)
         self.rho_d = cv.take((self.nz, self.nx), torch.float32)
         self.wav = cv.take((self.ns, self.nt), torch.float32)
+        self.dx_t = torch.full((), self.dx, dtype=torch.float32, device=device)  # divisor of alpha1
         if self.grad:
             self.obs = cv.take(shp, torch.float32)
             self.adj = cv.take(shp, torch.float32)
@@ -334,7 +335,8 @@ class _Shape(object):
         nb = self.nabc
         c, den = _pad(self.vp_d, nb), _pad(self.rho_d, nb)
         t1 = den * c
-        self.a1.copy_(t1 * c * self.dt / self.dx)
+        # divisor as a device tensor: true division, as the drop-in propagator computes alpha1
+        self.a1.copy_(t1 * c * self.dt / self.dx_t)
         self.a2.copy_(self.dt / (den * self.dx))
         self.plan.run_forward(self.a1, self.a2, self.damp, self.wav, self.grad, workspace=self.ws, records=self.recs,
                               fw=self.fw, stream=h)

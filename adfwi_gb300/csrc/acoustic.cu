@@ -197,7 +197,6 @@ __global__ void mask_coefficients(Geo<T> g, T* cf) {
 
 #include "acoustic_tma.cuh"
 #include "acoustic_vec.cuh"
-#include "acoustic_zm.cuh"
 
 // ----------------------------------------------------------------------------------------
 // Plan, workspace and drivers.
@@ -215,19 +214,10 @@ struct Tiling {
   int ncells;
 };
 
-// Work decomposition of the z-streamed forward step: strips of zm::SW columns, nzr row ranges
-// of lz rows, groups of G shots; receiver tables per strip and row (offsets into tab).
-struct ZTiling {
-  int nstrips, nzr, lz, G, ngroups, nunits, blocks;
-  int64_t o_rrb, o_rcol, o_rid;
-};
-
 struct adfwi_acoustic_plan {
   adfwi_acoustic_desc d;
   int nzp, nxp, fs, zbeg;
-  Tiling t2;             // 16 x 64 tiles of the pipelined adjoint step
-  ZTiling zt;            // strips of the z-streamed forward step
-  ZTiling za;            // strips of the z-streamed adjoint step
+  Tiling t2;             // 16 x 64 tiles of the pipelined forward and adjoint steps
   int K, nseg;           // snapshot interval and number of segments (gradient mode)
   int last_chunk_start;  // first step of the reference's last checkpoint chunk
   int elem;              // bytes per element
@@ -256,8 +246,8 @@ Carve carve(const adfwi_acoustic_plan* p, bool grad, int K) {
   c.coef = take(ac::kNumCoef * pl);
   c.fa = take(3 * ns * pl);
   c.fb = take(3 * ns * pl);
-  c.ilp = take((int64_t)p->zt.ngroups * pl);
-  c.ilu = take((int64_t)p->zt.ngroups * pl);
+  c.ilp = take((int64_t)p->t2.ngroups * pl);
+  c.ilu = take((int64_t)p->t2.ngroups * pl);
   c.tab = take((int64_t)p->tab.size() * 4);
   c.flag = take(256);
   if (grad) {
@@ -270,8 +260,8 @@ Carve carve(const adfwi_acoustic_plan* p, bool grad, int K) {
     c.hd = take((int64_t)K * ns * pl);
     c.la = take(3 * ns * pl);
     c.lb = take(3 * ns * pl);
-    c.g1 = take((int64_t)p->za.ngroups * pl);
-    c.g2 = take((int64_t)p->za.ngroups * pl);
+    c.g1 = take((int64_t)p->t2.ngroups * pl);
+    c.g2 = take((int64_t)p->t2.ngroups * pl);
   }
   c.total = o;
   return c;
@@ -393,33 +383,19 @@ ac2::StepArgs<T> step_args(const adfwi_acoustic_plan* p, int it, const T* cf, in
   return a;
 }
 
-zm::Units zm_units(const ZTiling& z, const unsigned char* ws, const Carve& c) {
-  zm::Units U;
-  U.nstrips = z.nstrips;
-  U.nzr = z.nzr;
-  U.lz = z.lz;
-  U.G = z.G;
-  U.ngroups = z.ngroups;
-  U.nunits = z.nunits;
-  const int32_t* tb = reinterpret_cast<const int32_t*>(ws + c.tab);
-  U.rrow_beg = tb + z.o_rrb;
-  U.rcol = tb + z.o_rcol;
-  U.rid = tb + z.o_rid;
-  return U;
-}
-
 template <typename T>
-int launch_fwd(const adfwi_acoustic_plan* p, const ac::Geo<T>& g, const zm::Units& U, int it, int accum_u,
-               const T* cf, const T* wav, const T* p0, const T* u0, const T* w0, T* p1, T* u1, T* w1, T* d1, T* rp,
-               T* ru, T* rw, T* ilp, T* ilu, int* flag, cudaStream_t st) {
+int launch_fwd(const adfwi_acoustic_plan* p, const ac::Geo<T>& g, int it, int accum_u, const T* cf,
+               const T* wav, const T* p0, const T* u0, const T* w0, T* p1, T* u1, T* w1, T* d1, T* rp, T* ru,
+               T* rw, T* ilp, T* ilu, int* flag, cudaStream_t st) {
   const int64_t ns = p->d.ns;
   ac2::Maps maps;
-  int rc = make_plane_map(&maps.a, u0, sizeof(T), p->L, ns, zm::BW, zm::R);
-  if (!rc) rc = make_plane_map(&maps.b, w0, sizeof(T), p->L, ns, zm::BW, zm::R);
-  if (!rc) rc = make_plane_map(&maps.c, p0, sizeof(T), p->L, ns, zm::BW, zm::R);
+  int rc = make_plane_map(&maps.a, u0, sizeof(T), p->L, ns, ac2::BOXX, ac2::EZ);
+  if (!rc) rc = make_plane_map(&maps.b, w0, sizeof(T), p->L, ns, ac2::BOXX, ac2::WZ);
+  if (!rc) rc = make_plane_map(&maps.c, p0, sizeof(T), p->L, ns, ac2::BOXX, ac2::EZ);
   if (rc) return rc;
   ac2::StepArgs<T> a = step_args<T>(p, it, cf, flag);
   a.accum_u = accum_u;
+  a.stages = vec_stages<T>();
   a.wav = wav;
   a.o0 = p1;
   a.o1 = u1;
@@ -430,32 +406,25 @@ int launch_fwd(const adfwi_acoustic_plan* p, const ac::Geo<T>& g, const zm::Unit
   a.rec_w = rw;
   a.acc0 = ilp;
   a.acc1 = ilu;
-  const int smem = zm::FwdLayout<T>::bytes();
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3((unsigned)p->zt.blocks);
-  cfg.blockDim = dim3(zm::THREADS);
-  cfg.dynamicSmemBytes = (size_t)smem;
-  cfg.stream = st;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  attr[0].val.programmaticStreamSerializationAllowed = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
-  ADFWI_LAUNCH(kAcFwdStep, st, ADFWI_CUDA_TRY(cudaLaunchKernelEx(&cfg, zm::fwd_zmarch<T>, maps, g, a, U)));
+  const int smem = ac2::VecFwdLayout<T>::bytes(a.stages);
+  ADFWI_LAUNCH(kAcFwdStep, st, ADFWI_CUDA_TRY(launch_pdl(ac2::fwd_step_vec<T>, p->t2.fwd_blocks, smem, st, maps, g, a)));
   return kOk;
 }
 
 template <typename T>
-int launch_adj(const adfwi_acoustic_plan* p, const ac::Geo<T>& g, const zm::Units& U, int it, const T* cf,
-               const T* lp0, const T* lu0, const T* lw0, T* lp1, T* lu1, T* lw1, const T* ph, const T* dh, const T* gp,
-               const T* gu, const T* gw, T* g1, T* g2, int* flag, cudaStream_t st) {
+int launch_adj(const adfwi_acoustic_plan* p, const ac::Geo<T>& g, int it, const T* cf, const T* lp0, const T* lu0,
+               const T* lw0, T* lp1, T* lu1, T* lw1, const T* ph, const T* dh, const T* gp, const T* gu, const T* gw,
+               T* g1, T* g2, int* flag, cudaStream_t st) {
   const int64_t ns = p->d.ns;
   ac2::Maps maps;
-  int rc = make_plane_map(&maps.a, lu0, sizeof(T), p->L, ns, zm::BW, zm::R);
-  if (!rc) rc = make_plane_map(&maps.b, lw0, sizeof(T), p->L, ns, zm::BW, zm::R);
-  if (!rc) rc = make_plane_map(&maps.c, ph, sizeof(T), p->L, ns, zm::BW, zm::R);
+  int rc = make_plane_map(&maps.a, lu0, sizeof(T), p->L, ns, ac2::BOXX, ac2::EZ);
+  if (!rc) rc = make_plane_map(&maps.b, lw0, sizeof(T), p->L, ns, ac2::BOXX, ac2::WZ);
+  if (!rc) rc = make_plane_map(&maps.c, lp0, sizeof(T), p->L, ns, ac2::BOXX, ac2::EZ);
+  if (!rc) rc = make_plane_map(&maps.d, ph, sizeof(T), p->L, ns, ac2::BOXX, ac2::EZ);
+  if (!rc) rc = make_plane_map(&maps.e, dh, sizeof(T), p->L, ns, ac2::BOXX, ac2::EZ);
   if (rc) return rc;
   ac2::StepArgs<T> a = step_args<T>(p, it, cf, flag);
+  a.stages = vec_adj_stages<T>();
   a.o0 = lp1;
   a.o1 = lu1;
   a.o2 = lw1;
@@ -464,17 +433,8 @@ int launch_adj(const adfwi_acoustic_plan* p, const ac::Geo<T>& g, const zm::Unit
   a.rec_w = gw;
   a.acc0 = g1;
   a.acc1 = g2;
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3((unsigned)p->za.blocks);
-  cfg.blockDim = dim3(zm::THREADS);
-  cfg.dynamicSmemBytes = (size_t)zm::AdjLayout<T>::bytes();
-  cfg.stream = st;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  attr[0].val.programmaticStreamSerializationAllowed = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
-  ADFWI_LAUNCH(kAcAdjStep, st, ADFWI_CUDA_TRY(cudaLaunchKernelEx(&cfg, zm::adj_zmarch<T>, maps, g, a, U, lp0, dh)));
+  const int smem = ac2::VecAdjLayout<T>::bytes(a.stages);
+  ADFWI_LAUNCH(kAcAdjStep, st, ADFWI_CUDA_TRY(launch_pdl(ac2::adj_step_vec<T>, p->t2.blocks, smem, st, maps, g, a)));
   return kOk;
 }
 
@@ -492,10 +452,10 @@ int set_smem_limits() {
   std::lock_guard<std::mutex> lk(g_smem_mu);
   if ((int)g_smem_done.size() <= dev) g_smem_done.resize(dev + 1, 0);
   if (!(g_smem_done[dev] & bit)) {
-    ADFWI_CUDA_TRY(cudaFuncSetAttribute(zm::fwd_zmarch<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        zm::FwdLayout<T>::bytes()));
-    ADFWI_CUDA_TRY(cudaFuncSetAttribute(zm::adj_zmarch<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        zm::AdjLayout<T>::bytes()));
+    ADFWI_CUDA_TRY(cudaFuncSetAttribute(ac2::fwd_step_vec<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        ac2::VecFwdLayout<T>::bytes(vec_stages<T>())));
+    ADFWI_CUDA_TRY(cudaFuncSetAttribute(ac2::adj_step_vec<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        ac2::VecAdjLayout<T>::bytes(vec_adj_stages<T>())));
     g_smem_done[dev] |= bit;
   }
   return kOk;
@@ -516,7 +476,6 @@ int forward_impl(const adfwi_acoustic_plan* p, const void* alpha1, const void* a
   rc = setup_common<T>(p, ws, c, alpha1, alpha2, damp, st);
   if (rc) return rc;
   ac::Geo<T> g = make_geo<T>(p, ws, c, p->t2);
-  const zm::Units U = zm_units(p->zt, ws, c);
   const int64_t pl = p->L.plane;
   const int64_t ns = p->d.ns;
   const T* cf = reinterpret_cast<const T*>(ws + c.coef);
@@ -551,7 +510,7 @@ int forward_impl(const adfwi_acoustic_plan* p, const void* alpha1, const void* a
       p1 = hp + (int64_t)it * ns * pl;
       d1 = hd + (int64_t)it * ns * pl;
     }
-    rc = launch_fwd<T>(p, g, U, it, it >= p->last_chunk_start ? 1 : 0, cf, wav, p0, cur + ns * pl, cur + 2 * ns * pl,
+    rc = launch_fwd<T>(p, g, it, it >= p->last_chunk_start ? 1 : 0, cf, wav, p0, cur + ns * pl, cur + 2 * ns * pl,
                        p1, nxt + ns * pl, nxt + 2 * ns * pl, d1, static_cast<T*>(rec_p), static_cast<T*>(rec_u),
                        static_cast<T*>(rec_w), ilp, ilu, flag, st);
     if (rc) return rc;
@@ -561,7 +520,7 @@ int forward_impl(const adfwi_acoustic_plan* p, const void* alpha1, const void* a
   if (fw_p || fw_u || fw_w) {
     const int64_t n = (int64_t)p->d.nz * p->d.nx;
     ADFWI_LAUNCH(kAux, st, (ac::illum_finalize<T><<<grid_blocks(n), 256, 0, st>>>(
-                                p->L, p->zt.ngroups, p->d.ns, p->d.nabc, p->d.nz, p->d.nx, ilp, ilu,
+                                p->L, p->t2.ngroups, p->d.ns, p->d.nabc, p->d.nz, p->d.nx, ilp, ilu,
                                 cur + 2 * ns * pl, static_cast<T*>(fw_p), static_cast<T*>(fw_u),
                                 static_cast<T*>(fw_w))));
     ADFWI_CUDA_TRY(cudaGetLastError());
@@ -581,8 +540,6 @@ int backward_impl(const adfwi_acoustic_plan* p, const void* wavelet, const void*
     return kWorkspaceTooSmall;
   }
   ac::Geo<T> g2 = make_geo<T>(p, ws, c, p->t2);
-  const zm::Units U = zm_units(p->zt, ws, c);
-  const zm::Units UA = zm_units(p->za, ws, c);
   const int64_t pl = p->L.plane;
   const int64_t ns = p->d.ns;
   const int nt = p->d.nt;
@@ -604,8 +561,8 @@ int backward_impl(const adfwi_acoustic_plan* p, const void* wavelet, const void*
 
   ADFWI_CUDA_TRY(cudaMemsetAsync(la, 0, 3 * ns * pl * sizeof(T), st));
   ADFWI_CUDA_TRY(cudaMemsetAsync(lb, 0, 3 * ns * pl * sizeof(T), st));
-  ADFWI_CUDA_TRY(cudaMemsetAsync(g1p, 0, (size_t)p->za.ngroups * pl * sizeof(T), st));
-  ADFWI_CUDA_TRY(cudaMemsetAsync(g2p, 0, (size_t)p->za.ngroups * pl * sizeof(T), st));
+  ADFWI_CUDA_TRY(cudaMemsetAsync(g1p, 0, (size_t)p->t2.ngroups * pl * sizeof(T), st));
+  ADFWI_CUDA_TRY(cudaMemsetAsync(g2p, 0, (size_t)p->t2.ngroups * pl * sizeof(T), st));
   if (!full) {
     // the recomputed pressure history is read with its halo by the next step and the adjoint
     rc = zero_frames<T>(hp, (int64_t)K * ns, p->L, st);
@@ -631,7 +588,7 @@ int backward_impl(const adfwi_acoustic_plan* p, const void* wavelet, const void*
       T* nxt = fb;
       for (int it = t0; it < t1; ++it) {
         const T* p0 = it == t0 ? fa : hp + (int64_t)(it - 1 - t0) * ns * pl;
-        rc = launch_fwd<T>(p, g2, U, it, 0, cf, wav, p0, cur + ns * pl, cur + 2 * ns * pl,
+        rc = launch_fwd<T>(p, g2, it, 0, cf, wav, p0, cur + ns * pl, cur + 2 * ns * pl,
                            hp + (int64_t)(it - t0) * ns * pl, nxt + ns * pl, nxt + 2 * ns * pl,
                            hd + (int64_t)(it - t0) * ns * pl, nullptr, nullptr, nullptr, nullptr, nullptr, flag, st);
         if (rc) return rc;
@@ -639,7 +596,7 @@ int backward_impl(const adfwi_acoustic_plan* p, const void* wavelet, const void*
       }
     }
     for (int it = t1 - 1; it >= t0; --it) {
-      rc = launch_adj<T>(p, g2, UA, it, cf, lcur, lcur + ns * pl, lcur + 2 * ns * pl, lnxt, lnxt + ns * pl,
+      rc = launch_adj<T>(p, g2, it, cf, lcur, lcur + ns * pl, lcur + 2 * ns * pl, lnxt, lnxt + ns * pl,
                          lnxt + 2 * ns * pl, hp + (int64_t)(it - t0) * ns * pl, hd + (int64_t)(it - t0) * ns * pl, gp,
                          gu, gw, g1p, g2p, flag, st);
       if (rc) return rc;
@@ -648,9 +605,9 @@ int backward_impl(const adfwi_acoustic_plan* p, const void* wavelet, const void*
     ADFWI_CUDA_TRY(cudaGetLastError());
   }
   const int64_t n = (int64_t)p->nzp * p->nxp;
-  ADFWI_LAUNCH(kAux, st, (ac::reduce_planes<T><<<grid_blocks(n), 256, 0, st>>>(p->L, p->za.ngroups, 0, 0, p->nzp,
+  ADFWI_LAUNCH(kAux, st, (ac::reduce_planes<T><<<grid_blocks(n), 256, 0, st>>>(p->L, p->t2.ngroups, 0, 0, p->nzp,
                                                                                 p->nxp, g1p, static_cast<T*>(ga1))));
-  ADFWI_LAUNCH(kAux, st, (ac::reduce_planes<T><<<grid_blocks(n), 256, 0, st>>>(p->L, p->za.ngroups, 0, 0, p->nzp,
+  ADFWI_LAUNCH(kAux, st, (ac::reduce_planes<T><<<grid_blocks(n), 256, 0, st>>>(p->L, p->t2.ngroups, 0, 0, p->nzp,
                                                                                 p->nxp, g2p, static_cast<T*>(ga2))));
   ADFWI_CUDA_TRY(cudaGetLastError());
   return kOk;
@@ -679,12 +636,9 @@ int resident_adj_blocks() {
                          sizeof(T) == 8 ? 1 : ac2::VAMINB);
 }
 template <typename T>
-int resident_zadj_blocks() {
-  return resident_blocks(zm::adj_zmarch<T>, zm::THREADS, zm::AdjLayout<T>::bytes(), sizeof(T) == 8 ? 1 : 2);
-}
-template <typename T>
 int resident_fwd_blocks() {
-  return resident_blocks(zm::fwd_zmarch<T>, zm::THREADS, zm::FwdLayout<T>::bytes(), sizeof(T) == 8 ? 1 : 2);
+  return resident_blocks(ac2::fwd_step_vec<T>, ac2::VTHREADS, ac2::VecFwdLayout<T>::bytes(vec_stages<T>()),
+                         sizeof(T) == 8 ? 1 : ac2::VMINB);
 }
 
 // Shots per unit for the persistent TMA kernels: balance the units over the resident blocks
@@ -765,77 +719,6 @@ void build_tiling(adfwi_acoustic_plan* p, Tiling* tl, int tz, int tx, int G, con
   t.insert(t.end(), tcr.begin(), tcr.end());
   tl->o_cr = t.size();
   t.insert(t.end(), cr.begin(), cr.end());
-}
-
-// Strips, row ranges and shot groups of a z-streamed step for `blocks` resident blocks. A block
-// takes a contiguous run of units; a unit of G shots and lz rows streams G * (ceil((lz + 4) / 8)
-// + 1) chunks of 8 rows (the first one the halo above). The choice minimises the chunks of the
-// busiest block, weighted by the read-modify-write traffic of the shot-group partial planes
-// (illumination in the forward, coefficient gradients in the adjoint), which falls as 1 / G.
-void choose_ztiling(const adfwi_acoustic_plan* p, ZTiling* z, int blocks, double acc_weight) {
-  const adfwi_acoustic_desc& d = p->d;
-  z->nstrips = (p->nxp + zm::SW - 1) / zm::SW;
-  const int rows = p->nzp - p->zbeg;
-  double best = 1e300;
-  for (int G = 1; G <= std::min(d.ns, 8); ++G) {
-    const int groups = (d.ns + G - 1) / G;
-    for (int nzr = 1; nzr <= std::max(1, rows / 24); ++nzr) {
-      const int lz = (rows + nzr - 1) / nzr;
-      const int nz_used = (rows + lz - 1) / lz;  // ranges that hold rows
-      const long long units = (long long)z->nstrips * nz_used * groups;
-      const long long per = (units + blocks - 1) / blocks;
-      const int S = (lz + 4 + zm::R - 1) / zm::R;
-      const double cost = (double)per * G * (S + 1) * (1.0 + acc_weight / G);
-      if (cost < best - 1e-9) {
-        best = cost;
-        z->G = G;
-        z->lz = lz;
-        z->nzr = nz_used;
-        z->ngroups = groups;
-        z->nunits = (int)units;
-      }
-    }
-  }
-  z->blocks = std::max(1, std::min(blocks, z->nunits));
-}
-
-// Receivers of the z-streamed steps per strip and row (appended to p->tab): offsets
-// (nstrips x (nzp + 1)), columns within the strip and receiver ids, sorted by strip, row and
-// column (the receivers of one cell are consecutive, in receiver order).
-void build_zrcv(adfwi_acoustic_plan* p, const int32_t* rcv_z, const int32_t* rcv_x) {
-  const adfwi_acoustic_desc& d = p->d;
-  const int nstrips = (p->nxp + zm::SW - 1) / zm::SW;
-  std::vector<int32_t>& t = p->tab;
-  struct Rv {
-    int strip, row, col, id;
-  };
-  std::vector<Rv> rv(d.nr);
-  for (int r = 0; r < d.nr; ++r) {
-    const int zr = rcv_z[r] + d.nabc, xr = rcv_x[r] + d.nabc;
-    rv[r] = {xr / zm::SW, zr, xr % zm::SW, r};
-  }
-  std::stable_sort(rv.begin(), rv.end(), [](const Rv& a, const Rv& b) {
-    return a.strip != b.strip ? a.strip < b.strip : (a.row != b.row ? a.row < b.row : a.col < b.col);
-  });
-  const int64_t nrow = (int64_t)p->nzp + 1;
-  std::vector<int32_t> beg((size_t)nstrips * nrow, 0);
-  for (const Rv& r : rv) beg[(size_t)r.strip * nrow + r.row + 1]++;
-  for (int st = 0; st < nstrips; ++st) {
-    int32_t* b = beg.data() + (size_t)st * nrow;
-    if (st > 0) b[0] += beg[(size_t)st * nrow - 1];
-    for (int64_t i = 1; i < nrow; ++i) b[i] += b[i - 1];
-  }
-  int64_t o_rrb = t.size();
-  t.insert(t.end(), beg.begin(), beg.end());
-  int64_t o_rcol = t.size();
-  for (const Rv& r : rv) t.push_back(r.col);
-  int64_t o_rid = t.size();
-  for (const Rv& r : rv) t.push_back(r.id);
-  for (ZTiling* z : {&p->zt, &p->za}) {
-    z->o_rrb = o_rrb;
-    z->o_rcol = o_rcol;
-    z->o_rid = o_rid;
-  }
 }
 
 // ----------------------------------------------------------------------------------------
@@ -941,9 +824,7 @@ int adfwi_acoustic_plan_create(const adfwi_acoustic_desc* desc, const int32_t* s
   p->fs = d.free_surface ? d.nabc : 1;
   p->zbeg = d.free_surface ? p->fs - 1 : 0;
   p->elem = d.dtype == ADFWI_F64 ? 8 : 4;
-  // ghost columns on the right for the z-streamed strips: a strip's staged rows and stores reach
-  // column 120 * nstrips + 7 <= nxp + 126, so at least 128 + 8 ghost columns follow the grid
-  p->L = make_layout(p->nzp, p->nxp, ac2::TZ, zm::BW, p->elem);
+  p->L = make_layout(p->nzp, p->nxp, ac2::TZ, ac2::TX, p->elem);
   // torch.chunk(wavelet, checkpoint_segments): chunks of ceil(nt / segments) steps.
   const int chunk = (d.nt + d.checkpoint_segments - 1) / d.checkpoint_segments;
   const int nchunks = (d.nt + chunk - 1) / chunk;
@@ -978,13 +859,10 @@ int adfwi_acoustic_plan_create(const adfwi_acoustic_desc* desc, const int32_t* s
     const int blocks = p->elem == 8 ? resident_adj_blocks<double>() : resident_adj_blocks<float>();
     const int fblocks = p->elem == 8 ? resident_fwd_blocks<double>() : resident_fwd_blocks<float>();
     int G2 = d.shots_per_block;
-    if (G2 <= 0) G2 = pick_unit_shots(d.ns, ntiles, blocks, blocks);  // the tiles serve the adjoint step
+    if (G2 <= 0) G2 = pick_unit_shots(d.ns, ntiles, fblocks, blocks);
     build_tiling(p, &p->t2, ac2::TZ, ac2::TX, G2, rcv_z, rcv_x);
     p->t2.blocks = std::max(1, std::min(blocks, p->t2.ntiles * p->t2.ngroups));
     p->t2.fwd_blocks = std::max(1, std::min(fblocks, p->t2.ntiles * p->t2.ngroups));
-    choose_ztiling(p, &p->zt, fblocks, 0.3);
-    choose_ztiling(p, &p->za, p->elem == 8 ? resident_zadj_blocks<double>() : resident_zadj_blocks<float>(), 0.5);
-    build_zrcv(p, rcv_z, rcv_x);
   }
   if (t.empty()) t.push_back(0);
 

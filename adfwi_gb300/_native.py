@@ -10,7 +10,7 @@ import os
 _LIB = None
 
 F32, F64 = 0, 1
-SNAP_NATIVE, SNAP_BF16, SNAP_FP16 = 0, 1, 2
+SNAP_NATIVE, SNAP_BF16, SNAP_FP16, SNAP_FP24 = 0, 1, 2, 3
 
 c_int32 = ctypes.c_int32
 c_int64 = ctypes.c_int64

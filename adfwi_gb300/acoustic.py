@@ -14,7 +14,8 @@ import torch
 from . import _native as N
 
 _SNAP = {"native": N.SNAP_NATIVE, "f32": N.SNAP_NATIVE, "fp32": N.SNAP_NATIVE, "float32": N.SNAP_NATIVE,
-         "bf16": N.SNAP_BF16, "bfloat16": N.SNAP_BF16, "fp16": N.SNAP_FP16, "float16": N.SNAP_FP16}
+         "bf16": N.SNAP_BF16, "bfloat16": N.SNAP_BF16, "fp16": N.SNAP_FP16, "float16": N.SNAP_FP16,
+         "fp24": N.SNAP_FP24, "f24": N.SNAP_FP24}
 
 
 def snapshot_code(precision):
@@ -23,7 +24,7 @@ def snapshot_code(precision):
     try:
         return _SNAP[str(precision).lower()]
     except KeyError:
-        raise ValueError("snapshot precision must be one of native, bf16, fp16") from None
+        raise ValueError("snapshot precision must be one of native, bf16, fp16, fp24") from None
 
 
 def dtype_code(dtype):

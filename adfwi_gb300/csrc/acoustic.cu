@@ -253,7 +253,7 @@ Carve carve(const adfwi_acoustic_plan* p, bool grad, int K) {
   if (grad) {
     const int nseg = (p->d.nt + K - 1) / K;
     const bool full = K >= p->d.nt;
-    const int64_t snap_elem = p->d.snapshot_precision == ADFWI_SNAP_NATIVE ? p->elem : 2;
+    const int64_t snap_elem = snapshot_value_bytes(p->d.snapshot_precision, p->elem);
     c.snap = take(full ? 0 : (int64_t)nseg * 3 * ns * p->L.plane * snap_elem);
     c.snap_scale = take(full ? 0 : (int64_t)nseg * 3 * ns * 4);
     c.hp = take((int64_t)K * ns * pl);
@@ -810,7 +810,7 @@ int adfwi_acoustic_plan_create(const adfwi_acoustic_desc* desc, const int32_t* s
   ADFWI_CHECK_ARG(d.nz >= 1 && d.nx >= 1 && d.nabc >= 2, "need nz, nx >= 1 and nabc >= 2");
   ADFWI_CHECK_ARG(d.ns >= 1 && d.nt >= 1 && d.nr >= 0, "need ns >= 1, nt >= 1, nr >= 0");
   ADFWI_CHECK_ARG(d.dtype == ADFWI_F32 || d.dtype == ADFWI_F64, "dtype must be ADFWI_F32 or ADFWI_F64");
-  ADFWI_CHECK_ARG(d.snapshot_precision >= 0 && d.snapshot_precision <= 2, "bad snapshot_precision");
+  ADFWI_CHECK_ARG(d.snapshot_precision >= 0 && d.snapshot_precision <= 3, "bad snapshot_precision");
   ADFWI_CHECK_ARG(d.checkpoint_segments >= 1, "checkpoint_segments must be >= 1");
   ADFWI_CHECK_ARG(src_z && src_x && (d.nr == 0 || (rcv_z && rcv_x)), "null geometry array");
   adfwi_acoustic_plan* p = new (std::nothrow) adfwi_acoustic_plan();

@@ -1330,7 +1330,7 @@ ECarve ecarve(const adfwi_elastic_plan* p, bool grad, int K) {
   if (grad) {
     const bool full = K >= p->d.nt;
     const int nseg = (p->d.nt + K - 1) / K;
-    const int64_t se = p->d.snapshot_precision == ADFWI_SNAP_NATIVE ? p->elem : 2;
+    const int64_t se = snapshot_value_bytes(p->d.snapshot_precision, p->elem);
     const int64_t nstate = p->nstate;
     c.snap = take(full ? 0 : (int64_t)nseg * nstate * ns * p->L.plane * se);
     c.snap_scale = take(full ? 0 : (int64_t)nseg * nstate * ns * 4);
@@ -1686,7 +1686,7 @@ int adfwi_elastic_plan_create(const adfwi_elastic_desc* desc, const int32_t* src
   ADFWI_CHECK_ARG(d.ns >= 1 && d.nt >= 1 && d.nr >= 0, "need ns >= 1, nt >= 1, nr >= 0");
   ADFWI_CHECK_ARG(d.dtype == ADFWI_F32 || d.dtype == ADFWI_F64, "dtype must be ADFWI_F32 or ADFWI_F64");
   ADFWI_CHECK_ARG(d.checkpoint_segments >= 1, "checkpoint_segments must be >= 1");
-  ADFWI_CHECK_ARG(d.snapshot_precision >= 0 && d.snapshot_precision <= 2, "bad snapshot_precision");
+  ADFWI_CHECK_ARG(d.snapshot_precision >= 0 && d.snapshot_precision <= 3, "bad snapshot_precision");
   ADFWI_CHECK_ARG(src_z && src_x && moment_tensor && (d.nr == 0 || (rcv_z && rcv_x)), "null geometry array");
   adfwi_elastic_plan* p = new (std::nothrow) adfwi_elastic_plan();
   if (!p) {

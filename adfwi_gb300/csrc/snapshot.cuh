@@ -4,7 +4,11 @@
 // either verbatim or as 16-bit values with one float max-abs scale per plane:
 //   FP16: q = half(x / maxabs * 2^15)  (2^15 keeps |q| below the fp16 maximum of 65504 and
 //         leaves values down to ~2e-9 of the plane's peak in the normal range);
-//   BF16: q = bf16(x / maxabs).
+//   BF16: q = bf16(x / maxabs);
+// or as 24-bit floats without a scale:
+//   FP24: the float32 value rounded to nearest (ties to even) at 15 mantissa bits, stored as its
+//         upper 16 bits (a bfloat16 plane) and the next 8 bits (a byte plane): the float32
+//         exponent range with a relative spacing of 2^-15, three bytes per value.
 // The stencil arithmetic itself always stays in the wavefield type.
 #pragma once
 #include <cuda_bf16.h>
@@ -83,6 +87,48 @@ __global__ void __launch_bounds__(kSnapThreads) snap_dequantize(const unsigned s
   }
 }
 
+// FP24: snapshot plane pi occupies bytes [3 pi plane, 3 (pi + 1) plane) of the store, its
+// 16-bit upper parts first, then its 8-bit lower parts.
+__device__ __forceinline__ unsigned fp24_round(float v) {
+  const unsigned b = __float_as_uint(v);
+  if ((b & 0x7f800000u) == 0x7f800000u) return b & 0xffffff00u;  // inf / nan: truncate
+  return (b + 0x7fu + ((b >> 8) & 1u)) & 0xffffff00u;         // nearest, ties to even
+}
+
+template <typename T>
+__global__ void snap_q24(const T* __restrict__ src, int64_t nplanes, int64_t plane, unsigned char* __restrict__ dst) {
+  const int64_t n = nplanes * plane;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t pi = e / plane, k = e - pi * plane;
+    const unsigned r = fp24_round((float)src[e]);
+    unsigned char* base = dst + pi * 3 * plane;
+    reinterpret_cast<unsigned short*>(base)[k] = (unsigned short)(r >> 16);
+    base[2 * plane + k] = (unsigned char)((r >> 8) & 0xffu);
+  }
+}
+
+template <typename T>
+__global__ void snap_dq24(const unsigned char* __restrict__ src, int64_t nplanes, int64_t plane, T* __restrict__ dst) {
+  const int64_t n = nplanes * plane;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t pi = e / plane, k = e - pi * plane;
+    const unsigned char* base = src + pi * 3 * plane;
+    const unsigned r = ((unsigned)reinterpret_cast<const unsigned short*>(base)[k] << 16) |
+                       ((unsigned)base[2 * plane + k] << 8);
+    dst[e] = (T)__uint_as_float(r);
+  }
+}
+
+inline unsigned snap_blocks(int64_t n) {
+  const int64_t b = (n + 255) / 256;
+  return (unsigned)(b < 152 * 32 ? (b < 1 ? 1 : b) : 152 * 32);
+}
+
+// Bytes per snapshot value of a precision (scales aside).
+inline int snapshot_value_bytes(int prec, int elem) {
+  return prec == ADFWI_SNAP_NATIVE ? elem : (prec == ADFWI_SNAP_FP24 ? 3 : 2);
+}
+
 // Store planes [0, nplanes) of `src` as snapshot planes [first, first + nplanes).
 template <typename T>
 int snapshot_store(int prec, const T* src, int64_t nplanes, int64_t plane, unsigned char* snap,
@@ -90,6 +136,12 @@ int snapshot_store(int prec, const T* src, int64_t nplanes, int64_t plane, unsig
   if (prec == ADFWI_SNAP_NATIVE) {
     ADFWI_CUDA_TRY(cudaMemcpyAsync(snap + first * plane * (int64_t)sizeof(T), src, nplanes * plane * sizeof(T),
                                    cudaMemcpyDeviceToDevice, st));
+    return kOk;
+  }
+  if (prec == ADFWI_SNAP_FP24) {
+    ADFWI_LAUNCH(kAux, st, (snap_q24<T><<<snap_blocks(nplanes * plane), 256, 0, st>>>(src, nplanes, plane,
+                                                                                    snap + first * 3 * plane)));
+    ADFWI_CUDA_TRY(cudaGetLastError());
     return kOk;
   }
   unsigned short* q = reinterpret_cast<unsigned short*>(snap) + first * plane;
@@ -108,6 +160,12 @@ int snapshot_load(int prec, T* dst, int64_t nplanes, int64_t plane, const unsign
   if (prec == ADFWI_SNAP_NATIVE) {
     ADFWI_CUDA_TRY(cudaMemcpyAsync(dst, snap + first * plane * (int64_t)sizeof(T), nplanes * plane * sizeof(T),
                                    cudaMemcpyDeviceToDevice, st));
+    return kOk;
+  }
+  if (prec == ADFWI_SNAP_FP24) {
+    ADFWI_LAUNCH(kAux, st, (snap_dq24<T><<<snap_blocks(nplanes * plane), 256, 0, st>>>(snap + first * 3 * plane,
+                                                                                     nplanes, plane, dst)));
+    ADFWI_CUDA_TRY(cudaGetLastError());
     return kOk;
   }
   const unsigned short* q = reinterpret_cast<const unsigned short*>(snap) + first * plane;

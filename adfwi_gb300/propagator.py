@@ -9,7 +9,7 @@ delta exactly as in the reference, with the hand-written adjoint in place of aut
 through the time loop.
 
 Options beyond the reference's (all keyword-only, with reference-compatible defaults):
-``snapshot_precision`` ("native", "bf16", "fp16"), ``snapshot_every`` (steps between
+``snapshot_precision`` ("native", "bf16", "fp16", "fp24"), ``snapshot_every`` (steps between
 checkpoint snapshots, 0 = chosen from ``memory_budget``), ``memory_budget`` (bytes for the
 gradient workspace; default half of the free device memory when the plan is built),
 ``shots_per_block`` (0 = automatic).

@@ -402,7 +402,7 @@ def checkpointed_leg(args, dev):
     """Checkpointed gradient on the 500 x 1500 precision configuration (dx = 12.5 m, PML 50 ->
     600 x 1600 padded, nt = 6000, dt = 1 ms, 10 Hz Ricker, snapshots every 50 steps, 1500
     receivers): FP32 stencils with the snapshots in FP32, BF16 and FP16 (one max-abs scale per
-    snapshot, shot and field), timed; errors of records and dL/dvp (L = sum of records x fixed
+    snapshot, shot and field) and FP24 (float32 rounded to a 15-bit mantissa, 3 bytes), timed; errors of records and dL/dvp (L = sum of records x fixed
     random traces) against an FP64 run of the same scheme with FP64 snapshots (untimed)."""
     import adfwi_gb300 as A
     from adfwi_gb300.synthetic import linear_gradient_with_anomaly, surface_acquisition
@@ -413,7 +413,8 @@ def checkpointed_leg(args, dev):
     gen = torch.Generator(device=dev).manual_seed(0)
     wts = torch.randn((len(idx), nt, nx), generator=gen, device=dev, dtype=torch.float64)
     runs = [("fp64", torch.float64, "native"), ("fp32", torch.float32, "native"),
-            ("fp32_bf16", torch.float32, "bf16"), ("fp32_fp16", torch.float32, "fp16")]
+            ("fp32_bf16", torch.float32, "bf16"), ("fp32_fp16", torch.float32, "fp16"),
+            ("fp32_fp24", torch.float32, "fp24")]
     got = {}
     for name, dtype, prec in runs:
         npdt = np.float64 if dtype == torch.float64 else np.float32

@@ -32,6 +32,7 @@ extern "C" {
 #define ADFWI_SNAP_NATIVE 0 /* same type as the wavefields */
 #define ADFWI_SNAP_BF16 1   /* bfloat16 with one max-abs scale per snapshot, shot and field */
 #define ADFWI_SNAP_FP16 2   /* float16 with one max-abs scale per snapshot, shot and field */
+#define ADFWI_SNAP_FP24 3   /* float32 rounded to a 15-bit mantissa, 3 bytes per value, no scale */
 
 /* Status codes. */
 #define ADFWI_OK 0

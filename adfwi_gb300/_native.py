@@ -53,6 +53,9 @@ def _bind(lib):
         "adfwi_acoustic_plan_create": (c_int32, [ctypes.POINTER(AcousticDesc), P, P, P, P,
                                                  ctypes.POINTER(c_void_p)]),
         "adfwi_acoustic_plan_destroy": (None, [P]),
+        "adfwi_acoustic_plan_create_batched": (c_int32, [ctypes.POINTER(AcousticDesc), P, P, P, P, c_int32, P,
+                                                         ctypes.POINTER(c_void_p)]),
+        "adfwi_acoustic_plan_models": (c_int32, [P]),
         "adfwi_acoustic_workspace_bytes": (c_int32, [P, c_int32, ctypes.POINTER(c_int64)]),
         "adfwi_acoustic_snapshot_every": (c_int32, [P, ctypes.POINTER(c_int32)]),
         "adfwi_acoustic_forward": (c_int32, [P, P, P, P, P, P, P, P, P, P, P, c_int32, P, c_int64, P]),

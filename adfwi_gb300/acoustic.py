@@ -44,7 +44,11 @@ class AcousticPlan(object):
 
     def __init__(self, *, nz, nx, nabc, free_surface, src_z, src_x, rcv_z, rcv_x, nt, dt, dtype,
                  checkpoint_segments=1, snapshot_every=0, snapshot_precision="native",
-                 shots_per_block=0, memory_budget=0):
+                 shots_per_block=0, memory_budget=0, shot_model=None):
+        """``shot_model`` (ns ints, non-decreasing) makes a batched plan: several velocity models of
+        this grid shape solved in the same launches, shot s on model shot_model[s]; its
+        coefficient inputs and its illumination / gradient outputs then carry a leading model
+        axis (nmodels, ...)."""
         self.lib = N.lib()
         self.src_z, self.src_x = _i32(src_z), _i32(src_x)
         self.rcv_z, self.rcv_x = _i32(rcv_z), _i32(rcv_x)
@@ -62,11 +66,20 @@ class AcousticPlan(object):
         d.memory_budget = int(memory_budget or 0)
         self.desc = d
         h = ctypes.c_void_p()
-        rc = self.lib.adfwi_acoustic_plan_create(
-            ctypes.byref(d), self.src_z.ctypes.data_as(ctypes.c_void_p),
-            self.src_x.ctypes.data_as(ctypes.c_void_p), self.rcv_z.ctypes.data_as(ctypes.c_void_p),
-            self.rcv_x.ctypes.data_as(ctypes.c_void_p), ctypes.byref(h))
-        N.check(rc, "adfwi_acoustic_plan_create")
+        geo = (ctypes.byref(d), self.src_z.ctypes.data_as(ctypes.c_void_p),
+               self.src_x.ctypes.data_as(ctypes.c_void_p), self.rcv_z.ctypes.data_as(ctypes.c_void_p),
+               self.rcv_x.ctypes.data_as(ctypes.c_void_p))
+        if shot_model is None:
+            self.nm, self.batched = 1, False
+            N.check(self.lib.adfwi_acoustic_plan_create(*geo, ctypes.byref(h)), "adfwi_acoustic_plan_create")
+        else:
+            sm = _i32(shot_model)
+            if len(sm) != self.ns:
+                raise ValueError("shot_model has %d entries for %d shots" % (len(sm), self.ns))
+            self.nm, self.batched = int(sm.max()) + 1, True
+            self._shot_model = sm
+            N.check(self.lib.adfwi_acoustic_plan_create_batched(*geo, self.nm, sm.ctypes.data_as(ctypes.c_void_p),
+                                                                 ctypes.byref(h)), "adfwi_acoustic_plan_create_batched")
         self.handle = h
 
     def __del__(self):
@@ -103,10 +116,14 @@ class AcousticPlan(object):
     def grid_shape(self):
         return (self.nz + 2 * self.nabc, self.nx + 2 * self.nabc)
 
+    def _model_shape(self, shape):
+        """Shape of a per-model array: with a leading model axis for a batched plan."""
+        return (self.nm,) + tuple(shape) if self.batched else tuple(shape)
+
     def run_forward(self, alpha1, alpha2, damp, wavelet, with_gradient, workspace=None, records=None,
                     fw=None, stream=None):
         """Run the forward solve; returns (rec_p, rec_u, rec_w, fw_p, fw_u, fw_w, workspace)."""
-        g = self.grid_shape()
+        g = self._model_shape(self.grid_shape())
         for t, n in ((alpha1, "alpha1"), (alpha2, "alpha2"), (damp, "damp")):
             self._check(t, g, n)
         self._check(wavelet, (self.ns, self.nt), "wavelet")
@@ -118,7 +135,8 @@ class AcousticPlan(object):
             shp = (self.ns, self.nt, self.nr)
             records = tuple(torch.empty(shp, dtype=self.dtype, device=dev) for _ in range(3)) if self.nr else (None,) * 3
         if fw is None:
-            fw = tuple(torch.empty((self.nz, self.nx), dtype=self.dtype, device=dev) for _ in range(3))
+            fw = tuple(torch.empty(self._model_shape((self.nz, self.nx)), dtype=self.dtype, device=dev)
+                       for _ in range(3))
         st = ctypes.c_void_p(stream) if stream is not None else N.stream_handle(dev)
         rc = self.lib.adfwi_acoustic_forward(
             self.handle, N.ptr(alpha1), N.ptr(alpha2), N.ptr(damp), N.ptr(wavelet),

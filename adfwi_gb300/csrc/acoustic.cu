@@ -64,6 +64,8 @@ struct Geo {
   const int* tcell_cell;     // unique receiver cells of a tile, packed like trcv_cell
   const int* tcell_rbeg;     // ncells+1 offsets into cell_rcv
   const int* cell_rcv;       // receiver indices grouped by unique cell
+  const int* grp_beg;        // ngroups+1 offsets: shots of each shot group (a group has one model)
+  const int* grp_model;      // model of each shot group
 };
 
 // Update regions of acoustic_kernels.py:115, 139, 151.
@@ -210,7 +212,7 @@ struct Tiling {
   int G, ngroups;  // shots per unit / units per tile
   int blocks;      // launch width of the adjoint step (persistent kernel)
   int fwd_blocks;  // launch width of the forward step (persistent kernel)
-  int64_t o_trb, o_trc, o_tri, o_tcb, o_tcc, o_tcr, o_cr;
+  int64_t o_trb, o_trc, o_tri, o_tcb, o_tcc, o_tcr, o_cr, o_gb, o_gm;
   int ncells;
 };
 
@@ -221,6 +223,9 @@ struct adfwi_acoustic_plan {
   int K, nseg;           // snapshot interval and number of segments (gradient mode)
   int last_chunk_start;  // first step of the reference's last checkpoint chunk
   int elem;              // bytes per element
+  int nm;                // models of a batched plan (1 otherwise)
+  std::vector<int> model_shot_beg;  // nm+1 offsets: the shots of each model
+  std::vector<int> model_grp_beg;   // nm+1 offsets: the shot groups of each model
   Layout L;
   std::vector<int32_t> tab;  // geometry tables, uploaded into the workspace
   PinnedBytes tab_pin;       // page-locked copy of tab, the source of each upload
@@ -243,7 +248,7 @@ Carve carve(const adfwi_acoustic_plan* p, bool grad, int K) {
   const int64_t ns = p->d.ns;
   int64_t o = 0;
   auto take = [&](int64_t bytes) { int64_t at = o; o += align256(bytes); return at; };
-  c.coef = take(ac::kNumCoef * pl);
+  c.coef = take((int64_t)p->nm * ac::kNumCoef * pl);
   c.fa = take(3 * ns * pl);
   c.fb = take(3 * ns * pl);
   c.ilp = take((int64_t)p->t2.ngroups * pl);
@@ -316,6 +321,8 @@ ac::Geo<T> make_geo(const adfwi_acoustic_plan* p, const unsigned char* ws, const
   g.tcell_cell = tb + t.o_tcc;
   g.tcell_rbeg = tb + t.o_tcr;
   g.cell_rcv = tb + t.o_cr;
+  g.grp_beg = tb + t.o_gb;
+  g.grp_model = tb + t.o_gm;
   return g;
 }
 
@@ -330,15 +337,17 @@ int setup_common(const adfwi_acoustic_plan* p, unsigned char* ws, const Carve& c
   ADFWI_CUDA_TRY(cudaMemsetAsync(ws + c.flag, 0, 256, st));
   ADFWI_CUDA_TRY(cudaMemcpyAsync(ws + c.tab, p->tab_pin.ptr, p->tab.size() * 4, cudaMemcpyHostToDevice, st));
   const int64_t n = (int64_t)p->nzp * p->nxp;
-  T* cf = reinterpret_cast<T*>(ws + c.coef);
   const void* src[3] = {alpha1, alpha2, damp};
-  for (int q = 0; q < 3; ++q) {
-    ADFWI_LAUNCH(kAux, st, (ac::pack_plane<T><<<grid_blocks(n), 256, 0, st>>>(
-                                p->L, p->nzp, p->nxp, static_cast<const T*>(src[q]),
-                                reinterpret_cast<T*>(reinterpret_cast<unsigned char*>(cf) + q * pl))));
-  }
   ac::Geo<T> g = make_geo<T>(p, ws, c, p->t2);
-  ADFWI_LAUNCH(kAux, st, (ac::mask_coefficients<T><<<grid_blocks(n), 256, 0, st>>>(g, cf)));
+  for (int m = 0; m < p->nm; ++m) {  // model m's (nzp, nxp) planes into its coefficient block
+    T* cf = reinterpret_cast<T*>(ws + c.coef + (int64_t)m * ac::kNumCoef * pl);
+    for (int q = 0; q < 3; ++q) {
+      ADFWI_LAUNCH(kAux, st, (ac::pack_plane<T><<<grid_blocks(n), 256, 0, st>>>(
+                                  p->L, p->nzp, p->nxp, static_cast<const T*>(src[q]) + (int64_t)m * n,
+                                  reinterpret_cast<T*>(reinterpret_cast<unsigned char*>(cf) + q * pl))));
+    }
+    ADFWI_LAUNCH(kAux, st, (ac::mask_coefficients<T><<<grid_blocks(n), 256, 0, st>>>(g, cf)));
+  }
   ADFWI_CUDA_TRY(cudaGetLastError());
   return kOk;
 }
@@ -379,6 +388,7 @@ ac2::StepArgs<T> step_args(const adfwi_acoustic_plan* p, int it, const T* cf, in
   a.ngroups = p->t2.ngroups;
   a.ntiles = p->t2.ntiles;
   a.cf = cf;
+  a.cf_stride = (int64_t)ac::kNumCoef * p->L.plane;
   a.flag = flag;
   return a;
 }
@@ -519,10 +529,14 @@ int forward_impl(const adfwi_acoustic_plan* p, const void* alpha1, const void* a
   ADFWI_CUDA_TRY(cudaGetLastError());
   if (fw_p || fw_u || fw_w) {
     const int64_t n = (int64_t)p->d.nz * p->d.nx;
-    ADFWI_LAUNCH(kAux, st, (ac::illum_finalize<T><<<grid_blocks(n), 256, 0, st>>>(
-                                p->L, p->t2.ngroups, p->d.ns, p->d.nabc, p->d.nz, p->d.nx, ilp, ilu,
-                                cur + 2 * ns * pl, static_cast<T*>(fw_p), static_cast<T*>(fw_u),
-                                static_cast<T*>(fw_w))));
+    auto at = [&](void* f, int m) { return f ? static_cast<T*>(f) + (int64_t)m * n : nullptr; };
+    for (int m = 0; m < p->nm; ++m) {  // model m: its groups' partial planes and its shots' last w
+      const int g0 = p->model_grp_beg[m], s0 = p->model_shot_beg[m];
+      ADFWI_LAUNCH(kAux, st, (ac::illum_finalize<T><<<grid_blocks(n), 256, 0, st>>>(
+                                  p->L, p->model_grp_beg[m + 1] - g0, p->model_shot_beg[m + 1] - s0, p->d.nabc,
+                                  p->d.nz, p->d.nx, ilp + (int64_t)g0 * pl, ilu + (int64_t)g0 * pl,
+                                  cur + 2 * ns * pl + (int64_t)s0 * pl, at(fw_p, m), at(fw_u, m), at(fw_w, m))));
+    }
     ADFWI_CUDA_TRY(cudaGetLastError());
   }
   return kOk;
@@ -605,10 +619,13 @@ int backward_impl(const adfwi_acoustic_plan* p, const void* wavelet, const void*
     ADFWI_CUDA_TRY(cudaGetLastError());
   }
   const int64_t n = (int64_t)p->nzp * p->nxp;
-  ADFWI_LAUNCH(kAux, st, (ac::reduce_planes<T><<<grid_blocks(n), 256, 0, st>>>(p->L, p->t2.ngroups, 0, 0, p->nzp,
-                                                                                p->nxp, g1p, static_cast<T*>(ga1))));
-  ADFWI_LAUNCH(kAux, st, (ac::reduce_planes<T><<<grid_blocks(n), 256, 0, st>>>(p->L, p->t2.ngroups, 0, 0, p->nzp,
-                                                                                p->nxp, g2p, static_cast<T*>(ga2))));
+  for (int m = 0; m < p->nm; ++m) {  // model m's gradients: the sum over its groups' partial planes
+    const int g0 = p->model_grp_beg[m], ng = p->model_grp_beg[m + 1] - g0;
+    ADFWI_LAUNCH(kAux, st, (ac::reduce_planes<T><<<grid_blocks(n), 256, 0, st>>>(
+                                p->L, ng, 0, 0, p->nzp, p->nxp, g1p + (int64_t)g0 * pl, static_cast<T*>(ga1) + m * n)));
+    ADFWI_LAUNCH(kAux, st, (ac::reduce_planes<T><<<grid_blocks(n), 256, 0, st>>>(
+                                p->L, ng, 0, 0, p->nzp, p->nxp, g2p + (int64_t)g0 * pl, static_cast<T*>(ga2) + m * n)));
+  }
   ADFWI_CUDA_TRY(cudaGetLastError());
   return kOk;
 }
@@ -644,11 +661,15 @@ int resident_fwd_blocks() {
 // Shots per unit for the persistent TMA kernels: balance the units over the resident blocks
 // (the block with the most units sets the time) against the per-unit flush of the partial
 // accumulator planes (about half an item's worth of traffic).
-int pick_unit_shots(int ns, int ntiles, int blocks_fwd, int blocks_adj) {
+int pick_unit_shots(const std::vector<int>& model_shot_beg, int ntiles, int blocks_fwd, int blocks_adj) {
+  const int nm = (int)model_shot_beg.size() - 1;
+  int maxns = 1;
+  for (int m = 0; m < nm; ++m) maxns = std::max(maxns, model_shot_beg[m + 1] - model_shot_beg[m]);
   int best = 1;
   double best_cost = 1e30;
-  for (int G = 1; G <= ns; ++G) {
-    const int groups = (ns + G - 1) / G;
+  for (int G = 1; G <= maxns; ++G) {
+    int groups = 0;
+    for (int m = 0; m < nm; ++m) groups += (model_shot_beg[m + 1] - model_shot_beg[m] + G - 1) / G;
     const long long units = (long long)ntiles * groups;
     const long long pf = (units + blocks_fwd - 1) / blocks_fwd;
     const long long pa = (units + blocks_adj - 1) / blocks_adj;
@@ -672,8 +693,22 @@ void build_tiling(adfwi_acoustic_plan* p, Tiling* tl, int tz, int tx, int G, con
   tl->tiles_z = (p->nzp - p->zbeg + tz - 1) / tz;
   tl->ntiles = tl->tiles_x * tl->tiles_z;
   tl->G = std::max(1, std::min(G, d.ns));
-  tl->ngroups = (d.ns + tl->G - 1) / tl->G;
   tl->blocks = 0;
+  // shot groups of at most G shots, never across two models
+  std::vector<int32_t> gb(1, 0), gm;
+  p->model_grp_beg.assign(1, 0);
+  for (int m = 0; m < p->nm; ++m) {
+    for (int s = p->model_shot_beg[m]; s < p->model_shot_beg[m + 1]; s += tl->G) {
+      gb.push_back(std::min(s + tl->G, p->model_shot_beg[m + 1]));
+      gm.push_back(m);
+    }
+    p->model_grp_beg.push_back((int)gm.size());
+  }
+  tl->ngroups = (int)gm.size();
+  tl->o_gb = t.size();
+  t.insert(t.end(), gb.begin(), gb.end());
+  tl->o_gm = t.size();
+  t.insert(t.end(), gm.begin(), gm.end());
   struct R {
     int tile, cell, id;
   };
@@ -802,11 +837,34 @@ int adfwi_acoustic_noalloc_status(const adfwi_acoustic_plan* p, int32_t* status,
   return kOk;
 }
 
-int adfwi_acoustic_plan_create(const adfwi_acoustic_desc* desc, const int32_t* src_z, const int32_t* src_x,
-                               const int32_t* rcv_z, const int32_t* rcv_x, adfwi_acoustic_plan** out) {
+}  // extern "C"
+
+namespace {
+
+int plan_create_impl(const adfwi_acoustic_desc* desc, const int32_t* src_z, const int32_t* src_x,
+                     const int32_t* rcv_z, const int32_t* rcv_x, int32_t nmodels, const int32_t* shot_model,
+                     adfwi_acoustic_plan** out) {
   ADFWI_CHECK_ARG(desc && out, "null descriptor or output pointer");
   *out = nullptr;
   const adfwi_acoustic_desc& d = *desc;
+  ADFWI_CHECK_ARG(nmodels >= 1, "need nmodels >= 1");
+  ADFWI_CHECK_ARG(d.ns >= 1, "need ns >= 1");
+  std::vector<int> model_shot_beg(nmodels + 1, 0);
+  if (shot_model != nullptr) {
+    // shots of one model are consecutive, models in order, every model has a shot
+    for (int s = 0; s < d.ns; ++s) {
+      ADFWI_CHECK_ARG(shot_model[s] >= 0 && shot_model[s] < nmodels && (s == 0 || shot_model[s] >= shot_model[s - 1]),
+                      "shot_model must be non-decreasing in [0, nmodels) (shot %d)", s);
+      model_shot_beg[shot_model[s] + 1]++;
+    }
+    for (int m = 0; m < nmodels; ++m) {
+      ADFWI_CHECK_ARG(model_shot_beg[m + 1] > 0, "model %d has no shot", m);
+      model_shot_beg[m + 1] += model_shot_beg[m];
+    }
+  } else {
+    ADFWI_CHECK_ARG(nmodels == 1, "shot_model is required for several models");
+    model_shot_beg[1] = d.ns;
+  }
   ADFWI_CHECK_ARG(d.nz >= 1 && d.nx >= 1 && d.nabc >= 2, "need nz, nx >= 1 and nabc >= 2");
   ADFWI_CHECK_ARG(d.ns >= 1 && d.nt >= 1 && d.nr >= 0, "need ns >= 1, nt >= 1, nr >= 0");
   ADFWI_CHECK_ARG(d.dtype == ADFWI_F32 || d.dtype == ADFWI_F64, "dtype must be ADFWI_F32 or ADFWI_F64");
@@ -819,6 +877,8 @@ int adfwi_acoustic_plan_create(const adfwi_acoustic_desc* desc, const int32_t* s
     return kBadArgument;
   }
   p->d = d;
+  p->nm = nmodels;
+  p->model_shot_beg = model_shot_beg;
   p->nzp = d.nz + 2 * d.nabc;
   p->nxp = d.nx + 2 * d.nabc;
   p->fs = d.free_surface ? d.nabc : 1;
@@ -859,7 +919,7 @@ int adfwi_acoustic_plan_create(const adfwi_acoustic_desc* desc, const int32_t* s
     const int blocks = p->elem == 8 ? resident_adj_blocks<double>() : resident_adj_blocks<float>();
     const int fblocks = p->elem == 8 ? resident_fwd_blocks<double>() : resident_fwd_blocks<float>();
     int G2 = d.shots_per_block;
-    if (G2 <= 0) G2 = pick_unit_shots(d.ns, ntiles, fblocks, blocks);
+    if (G2 <= 0) G2 = pick_unit_shots(p->model_shot_beg, ntiles, fblocks, blocks);
     build_tiling(p, &p->t2, ac2::TZ, ac2::TX, G2, rcv_z, rcv_x);
     p->t2.blocks = std::max(1, std::min(blocks, p->t2.ntiles * p->t2.ngroups));
     p->t2.fwd_blocks = std::max(1, std::min(fblocks, p->t2.ntiles * p->t2.ngroups));
@@ -875,6 +935,27 @@ int adfwi_acoustic_plan_create(const adfwi_acoustic_desc* desc, const int32_t* s
   *out = p;
   return kOk;
 }
+
+}  // namespace
+
+extern "C" {
+
+int adfwi_acoustic_plan_create(const adfwi_acoustic_desc* desc, const int32_t* src_z, const int32_t* src_x,
+                               const int32_t* rcv_z, const int32_t* rcv_x, adfwi_acoustic_plan** out) {
+  return plan_create_impl(desc, src_z, src_x, rcv_z, rcv_x, 1, nullptr, out);
+}
+
+int adfwi_acoustic_plan_create_batched(const adfwi_acoustic_desc* desc, const int32_t* src_z,
+                                       const int32_t* src_x, const int32_t* rcv_z, const int32_t* rcv_x,
+                                       int32_t nmodels, const int32_t* shot_model, adfwi_acoustic_plan** out) {
+  if (shot_model == nullptr) {
+    set_error("adfwi_acoustic_plan_create_batched: null shot_model");
+    return kBadArgument;
+  }
+  return plan_create_impl(desc, src_z, src_x, rcv_z, rcv_x, nmodels, shot_model, out);
+}
+
+int32_t adfwi_acoustic_plan_models(const adfwi_acoustic_plan* plan) { return plan ? plan->nm : 0; }
 
 void adfwi_acoustic_plan_destroy(adfwi_acoustic_plan* plan) { delete plan; }
 

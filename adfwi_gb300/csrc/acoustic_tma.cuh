@@ -2,9 +2,11 @@
 // themselves are in acoustic_vec.cuh).
 //
 // Work of one launch = all (tile, shot) items of one time step. A persistent block owns a
-// contiguous range of "units" (one 16 x 64 tile x one group of G shots; tile-major), so every
-// accumulator a unit produces (illumination, coefficient gradients) belongs to one block and
-// is flushed once, deterministically, into the group's partial plane.
+// contiguous range of "units" (one 16 x 64 tile x one group of at most G shots; tile-major), so
+// every accumulator a unit produces (illumination, coefficient gradients) belongs to one block
+// and is flushed once, deterministically, into the group's partial plane. The shots of a group
+// share one velocity model: a batched plan solves several models of one grid shape in the same
+// launches, each with its own coefficient block and its own groups.
 //
 // Inside a block, one producer warp has one lane issue, per item, the TMA tile loads of
 // every wavefield plane the item reads into the next free pipeline stage and arm the stage's
@@ -62,7 +64,8 @@ template <typename T>
 struct StepArgs {
   int it, G, ngroups, ntiles, accum_u, stages;
   const T* wav;
-  const T* cf;  // coefficient block (masked planes kA1M .. kB3)
+  const T* cf;  // coefficient block of model 0 (masked planes kA1M .. kB3); model m at cf + m * cf_stride
+  int64_t cf_stride;
   T* o0;        // forward: p1 / adjoint: lp1
   T* o1;        // forward: u1 / adjoint: lu1
   T* o2;        // forward: w1 / adjoint: lw1
@@ -90,7 +93,7 @@ __device__ __forceinline__ void produce(const Maps& maps, const ac::Geo<T>& g, c
     const int tile = un / a.ngroups, grp = un - tile * a.ngroups;
     const int i0 = g.zbeg + (tile / g.tiles_x) * TZ, j0 = (tile % g.tiles_x) * TX;
     const int x = j0 - 4 + GX;
-    const int s_beg = grp * a.G, s_end = min(g.ns, s_beg + a.G);
+    const int s_beg = g.grp_beg[grp], s_end = g.grp_beg[grp + 1];
     bool stop = false;
     for (int sh = s_beg; sh < s_end; ++sh, ++k) {
       const int st = k % S;

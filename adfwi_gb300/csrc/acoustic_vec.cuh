@@ -120,7 +120,7 @@ __device__ __forceinline__ void relay(const ac::Geo<T>& g, const StepArgs<T>& a,
   int k = 0;
   for (int un = u_beg; un < u_end && !aborted(h); ++un) {
     const int tile = un / a.ngroups, grp = un - tile * a.ngroups;
-    const int s_beg = grp * a.G, s_end = min(g.ns, s_beg + a.G);
+    const int s_beg = g.grp_beg[grp], s_end = g.grp_beg[grp + 1];
     if (!relayed(tile)) {
       k += s_end - s_beg;
       continue;
@@ -234,7 +234,6 @@ __global__ void __launch_bounds__(VTHREADS, VMINB)
   T* SPB1 = reinterpret_cast<T*>(gs + LY::kSP);
   const Layout L = g.L;
   const int64_t PL = L.plane;
-  const T* cf = a.cf;
 
   // halo task: rows 2*erp, 2*erp+1 of the p halo, box columns 4*ecg .. 4*ecg+3
   const bool has_ext = gt < EXT_TASKS;
@@ -249,13 +248,15 @@ __global__ void __launch_bounds__(VTHREADS, VMINB)
   T a2u[4], b2[4], a2w[4], b3[4];
   unsigned twin = 0;       // illumination-window bits of the tile cells
   bool trow = false, tfs = false;
-  int prev_tile = -1, sel = 0, k = 0;
+  int prev_tile = -1, prev_model = -1, sel = 0, k = 0;
 
   for (int un = u_beg; un < u_end; ++un) {
     const int tile = un / a.ngroups, sgrp = un - tile * a.ngroups;
-    const int s_beg = sgrp * a.G, s_end = min(g.ns, s_beg + a.G);
+    const int s_beg = g.grp_beg[sgrp], s_end = g.grp_beg[sgrp + 1];
+    const int model = g.grp_model[sgrp];
     const int i0 = g.zbeg + (tile / g.tiles_x) * TZ, j0 = (tile % g.tiles_x) * TX;
-    if (tile != prev_tile) {
+    if (tile != prev_tile || model != prev_model) {
+      const T* cf = a.cf + (int64_t)model * a.cf_stride;
 #pragma unroll
       for (int q = 0; q < 2; ++q) {
         const int r = 2 * erp + q;
@@ -297,6 +298,7 @@ __global__ void __launch_bounds__(VTHREADS, VMINB)
           if (trow && jb + c < L.nxp && ac::in_window(g, i, jb + c)) twin |= 1u << c;
       }
       prev_tile = tile;
+      prev_model = model;
     }
     const int rb = g.tile_rcv_beg[tile], re_ = g.tile_rcv_beg[tile + 1];
     const int64_t go = (int64_t)sgrp * PL;
@@ -577,7 +579,6 @@ __global__ void __launch_bounds__(VTHREADS, VAMINB)
   T* OW = reinterpret_cast<T*>(scr + LY::kSO);
   const Layout L = g.L;
   const int64_t PL = L.plane;
-  const T* cf = a.cf;
 
   const bool has_ext = gt < EXT_TASKS;
   const int erp = gt / CGE, ecg = gt - erp * CGE;
@@ -592,7 +593,8 @@ __global__ void __launch_bounds__(VTHREADS, VAMINB)
   for (int un = u_beg; un < u_end; ++un) {
     const int tile = un / a.ngroups, sgrp = un - tile * a.ngroups;
     const int i0 = g.zbeg + (tile / g.tiles_x) * TZ, j0 = (tile % g.tiles_x) * TX;
-    const int s_beg = sgrp * a.G, s_end = min(g.ns, s_beg + a.G);
+    const int s_beg = g.grp_beg[sgrp], s_end = g.grp_beg[sgrp + 1];
+    const T* cf = a.cf + (int64_t)g.grp_model[sgrp] * a.cf_stride;
     const int cb = g.tile_cell_beg[tile], ce = g.tile_cell_beg[tile + 1];
     if (tile != prev_tile) {
 #pragma unroll

@@ -72,6 +72,21 @@ int adfwi_acoustic_plan_create(const adfwi_acoustic_desc* desc, const int32_t* s
                                const int32_t* rcv_x, adfwi_acoustic_plan** plan);
 void adfwi_acoustic_plan_destroy(adfwi_acoustic_plan* plan);
 
+/* Batched plan: `nmodels` velocity models of one grid shape solved in the same launches (no
+ * counterpart in the reference, whose propagator solves one model per call; this is what the
+ * continuous-batching server packs requests into). shot_model (HOST, ns) gives each shot's
+ * model, non-decreasing, every model with at least one shot; receivers are shared. The
+ * forward / backward of a batched plan take alpha1, alpha2, damp as (nmodels, nz+2nabc,
+ * nx+2nabc) arrays, write fw_p/u/w as (nmodels, nz, nx) and grad_alpha1/2 as (nmodels,
+ * nz+2nabc, nx+2nabc); records stay (ns, nt, nr) in shot order. Per shot the arithmetic is
+ * that of a single-model plan. */
+int adfwi_acoustic_plan_create_batched(const adfwi_acoustic_desc* desc, const int32_t* src_z,
+                                       const int32_t* src_x, const int32_t* rcv_z,
+                                       const int32_t* rcv_x, int32_t nmodels,
+                                       const int32_t* shot_model, adfwi_acoustic_plan** plan);
+/* Models of a plan (1 for adfwi_acoustic_plan_create). */
+int32_t adfwi_acoustic_plan_models(const adfwi_acoustic_plan* plan);
+
 /* Workspace bytes for a forward solve (with_gradient = 0) or for a forward solve that keeps
  * what adfwi_acoustic_backward needs (with_gradient = 1). Used for HBM-budget admission. */
 int adfwi_acoustic_workspace_bytes(const adfwi_acoustic_plan* plan, int32_t with_gradient,

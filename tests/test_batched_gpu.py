@@ -1,0 +1,62 @@
+"""Batched acoustic plans against single-model solves (GPU).
+
+A batched plan solves several velocity models of one grid shape in the same launches: each
+shot group reads its own model's coefficient block. Per shot the arithmetic is that of a
+single-model plan, so the records are bit-identical to solving each model alone; the
+forward-wavefield maps and the coefficient gradients are sums over a model's shot groups, whose
+grouping may differ from the single-model plan's, so they agree to rounding (1e-6 in float32,
+1e-12 in float64).
+"""
+import numpy as np
+import pytest
+import torch
+
+import adfwi_gb300 as A
+from adfwi_gb300.acoustic import AcousticPlan
+from _cases import acoustic_problem, rel
+
+pytestmark = pytest.mark.gpu
+
+
+def _model_inputs(seed, ns, dtype, free_surface):
+    model, survey, prop = acoustic_problem(A, seed=seed, ns=ns, nt=150, dtype=dtype, free_surface=free_surface)
+    model.forward()
+    a1, a2 = (t.detach().contiguous() for t in prop.coefficients(model))
+    return prop, a1, a2, prop.damp.contiguous(), prop.wavelet.contiguous()
+
+
+@pytest.mark.parametrize("dtype,tol", [(torch.float32, 1e-6), (torch.float64, 1e-12)])
+@pytest.mark.parametrize("free_surface", [False, True])
+@pytest.mark.parametrize("snapshot_every", [0, 23])
+def test_batched_solve_equals_single_model_solves(dtype, tol, free_surface, snapshot_every):
+    cases = [_model_inputs(seed, ns, dtype, free_surface) for seed, ns in ((3, 2), (4, 1), (5, 3))]
+    p0 = cases[0][0]
+    src_z = np.concatenate([c[0].src_loc[:, 1] for c in cases])
+    src_x = np.concatenate([c[0].src_loc[:, 0] for c in cases])
+    shot_model = np.concatenate([np.full(c[0].src_n, m) for m, c in enumerate(cases)])
+    kw = dict(nz=p0.nz, nx=p0.nx, nabc=p0.nabc, free_surface=free_surface, rcv_z=p0.rcv_loc[:, 1],
+              rcv_x=p0.rcv_loc[:, 0], nt=p0.nt, dt=p0.dt, dtype=dtype, snapshot_every=snapshot_every)
+    batched = AcousticPlan(src_z=src_z, src_x=src_x, shot_model=shot_model, **kw)
+    assert batched.nm == 3
+    stack = lambda k: torch.stack([c[k] for c in cases]).contiguous()  # noqa: E731
+    a1, a2, damp = stack(1), stack(2), stack(3)
+    wav = torch.cat([c[4] for c in cases]).contiguous()
+    out = batched.run_forward(a1, a2, damp, wav, True)
+    gen = torch.Generator().manual_seed(9)
+    w = torch.randn(out[0].shape, generator=gen, dtype=dtype).cuda()
+    ga1, ga2 = batched.run_backward(a1, a2, damp, wav, (w, None, None), out[6])
+    assert batched.status(out[6], True) == 0
+    s0 = 0
+    for m, (prop, b1, b2, bd, bw) in enumerate(cases):
+        single = AcousticPlan(src_z=prop.src_loc[:, 1], src_x=prop.src_loc[:, 0], **kw)
+        o = single.run_forward(b1, b2, bd, bw, True)
+        s1 = s0 + prop.src_n
+        g1, g2 = single.run_backward(b1, b2, bd, bw, (w[s0:s1].contiguous(), None, None), o[6])
+        for q in range(3):
+            assert torch.equal(out[q][s0:s1], o[q]), (m, q)
+        for q in range(3, 6):
+            assert rel(out[q][m], o[q]) <= tol, (m, q, rel(out[q][m], o[q]))
+        assert rel(ga1[m], g1) <= tol, (m, rel(ga1[m], g1))
+        assert rel(ga2[m], g2) <= tol, (m, rel(ga2[m], g2))
+        s0 = s1
+

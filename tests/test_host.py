@@ -163,3 +163,18 @@ def test_propagator_refuses_cpu_device():
     rcv.add_receiver(4, 1, "pr")
     with pytest.raises(RuntimeError, match="CUDA"):
         A.AcousticPropagator(m, A.Survey(src, rcv), device="cpu")
+
+
+def test_batched_plan_geometry_on_the_host(native_lib):
+    """A batched plan (several models, shots grouped by model) builds on the host and sizes a
+    workspace with one coefficient block per model; unordered shot models are rejected."""
+    from adfwi_gb300.acoustic import AcousticPlan
+    kw = dict(nz=20, nx=30, nabc=8, free_surface=False, rcv_z=[2], rcv_x=[4], nt=10, dt=1e-3, dtype=torch.float32)
+    one = AcousticPlan(src_z=[1, 1, 1], src_x=[3, 9, 15], **kw)
+    two = AcousticPlan(src_z=[1, 1, 1], src_x=[3, 9, 15], shot_model=[0, 0, 1], **kw)
+    assert two.nm == 2 and native_lib.adfwi_acoustic_plan_models(two.handle) == 2
+    assert two.workspace_bytes(False) > one.workspace_bytes(False)
+    with pytest.raises(RuntimeError, match="non-decreasing"):
+        AcousticPlan(src_z=[1, 1, 1], src_x=[3, 9, 15], shot_model=[1, 0, 0], **kw)
+    with pytest.raises(RuntimeError, match="has no shot"):
+        AcousticPlan(src_z=[1, 1], src_x=[3, 9], shot_model=[0, 2], **kw)

@@ -683,7 +683,7 @@ int pick_unit_shots(const std::vector<int>& model_shot_beg, int ntiles, int bloc
 }
 
 // Tile the grid and build the receiver tables of that tiling (appended to p->tab).
-void build_tiling(adfwi_acoustic_plan* p, Tiling* tl, int tz, int tx, int G, const int32_t* rcv_z,
+void build_tiling(adfwi_acoustic_plan* p, Tiling* tl, int tz, int tx, const std::vector<int>& Gm, const int32_t* rcv_z,
                   const int32_t* rcv_x) {
   const adfwi_acoustic_desc& d = p->d;
   std::vector<int32_t>& t = p->tab;
@@ -692,14 +692,16 @@ void build_tiling(adfwi_acoustic_plan* p, Tiling* tl, int tz, int tx, int G, con
   tl->tiles_x = (p->nxp + tx - 1) / tx;
   tl->tiles_z = (p->nzp - p->zbeg + tz - 1) / tz;
   tl->ntiles = tl->tiles_x * tl->tiles_z;
-  tl->G = std::max(1, std::min(G, d.ns));
+  tl->G = 1;
   tl->blocks = 0;
-  // shot groups of at most G shots, never across two models
+  // shot groups of at most Gm[m] shots of model m, never across two models
   std::vector<int32_t> gb(1, 0), gm;
   p->model_grp_beg.assign(1, 0);
   for (int m = 0; m < p->nm; ++m) {
-    for (int s = p->model_shot_beg[m]; s < p->model_shot_beg[m + 1]; s += tl->G) {
-      gb.push_back(std::min(s + tl->G, p->model_shot_beg[m + 1]));
+    const int G = std::max(1, Gm[m]);
+    tl->G = std::max(tl->G, G);
+    for (int s = p->model_shot_beg[m]; s < p->model_shot_beg[m + 1]; s += G) {
+      gb.push_back(std::min(s + G, p->model_shot_beg[m + 1]));
       gm.push_back(m);
     }
     p->model_grp_beg.push_back((int)gm.size());
@@ -918,9 +920,14 @@ int plan_create_impl(const adfwi_acoustic_desc* desc, const int32_t* src_z, cons
     const int ntiles = ((p->nxp + ac2::TX - 1) / ac2::TX) * ((p->nzp - p->zbeg + ac2::TZ - 1) / ac2::TZ);
     const int blocks = p->elem == 8 ? resident_adj_blocks<double>() : resident_adj_blocks<float>();
     const int fblocks = p->elem == 8 ? resident_fwd_blocks<double>() : resident_fwd_blocks<float>();
-    int G2 = d.shots_per_block;
-    if (G2 <= 0) G2 = pick_unit_shots(p->model_shot_beg, ntiles, fblocks, blocks);
-    build_tiling(p, &p->t2, ac2::TZ, ac2::TX, G2, rcv_z, rcv_x);
+    // shots per group of each model: as a plan of that model alone would choose them, so a
+    // model's partial sums (and so its results) do not depend on the other models of a batch
+    std::vector<int> Gm(p->nm);
+    for (int m = 0; m < p->nm; ++m) {
+      const std::vector<int> alone = {0, p->model_shot_beg[m + 1] - p->model_shot_beg[m]};
+      Gm[m] = d.shots_per_block > 0 ? d.shots_per_block : pick_unit_shots(alone, ntiles, fblocks, blocks);
+    }
+    build_tiling(p, &p->t2, ac2::TZ, ac2::TX, Gm, rcv_z, rcv_x);
     p->t2.blocks = std::max(1, std::min(blocks, p->t2.ntiles * p->t2.ngroups));
     p->t2.fwd_blocks = std::max(1, std::min(fblocks, p->t2.ntiles * p->t2.ngroups));
   }

@@ -1,17 +1,19 @@
 """Continuous-batching server for iso-acoustic forward and gradient solves of mixed sizes.
 
 Requests (a model, its shots and, for a gradient solve, its observed data) arrive at any
-time. The server admits a request as soon as a solve slot is free and its device memory fits
-the HBM budget, runs every admitted solve on its own CUDA stream so that the solves of
-different requests overlap on the GPU (the persistent stencil kernels of a small grid fill
-only part of the 152 SMs, and one request's host-side preparation hides behind the others'
-kernels), and reports per-request latency (arrival to result) beside throughput.
+time. When a solve slot is free, the server packs the oldest waiting request with the later
+waiting requests of its bucket (same grid, time axis, wavelet, receivers and snapshot
+interval) into one batched plan, whose persistent step kernels advance every shot of every
+packed request in the same launches (each request on its own velocity model); it admits the
+batch as soon as its device memory fits the HBM budget, runs every admitted batch on its own
+CUDA stream so that batches overlap on the GPU, and reports per-request latency (arrival to
+result) beside throughput.
 
-Memory. The budget is one device arena allocated once. Each admitted request takes one
+Memory. The budget is one device arena allocated once. Each admitted batch takes one
 contiguous, 256-byte aligned range of it (first fit) holding everything of its solve that
 scales with the problem: the snapshot workspace, the three record arrays, the observed data
-and its adjoint source, and the coefficient, damping, wavelet and gradient planes. The range
-stays resident until the request completes. Admission is therefore exact (a request starts
+and its adjoint source, and the coefficient, damping, wavelet and gradient planes of each of
+its models. The range stays resident until the batch completes. Admission is therefore exact (a request starts
 only when its range can be carved), and no solve allocates or frees its large buffers through
 a caching allocator (which synchronises the whole device when it runs out of cached blocks).
 Short-lived temporaries of the misfit go through PyTorch's allocator and are covered by the
@@ -19,13 +21,17 @@ reserve left outside the arena.
 
 Scheduling is first-come-first-served with backfill: a waiting request that fits may start
 before an older one that does not fit yet, until the oldest has waited ``max_wait_s``; from
-then on requests start strictly in arrival order so large requests cannot starve. A request
-larger than the whole arena is rejected at submission.
+then on requests start strictly in arrival order so large requests cannot starve. A batch
+that does not fit sheds its newest members first. A request larger than the whole arena, or
+whose geometry its plan rejects, fails at submission; a cancelled future withdraws its request
+while it waits; a failing batch fails only its own requests' futures.
 
-Determinism. A request's snapshot interval depends only on its own shape (every plan gets
-the same ``per_request_budget``), the kernels are deterministic (fixed-order reductions, no
-atomics), and the misfit uses fixed-order reductions, so a request returns bit-identical
-records, loss and gradient whether it runs alone or in a mix.
+Determinism. A request's snapshot interval depends only on its own shape (every request gets
+the same ``per_request_budget``, and the interval is part of its bucket), a batched plan groups
+each request's shots as a plan of that request alone would, the kernels are deterministic
+(fixed-order reductions, no atomics), and each request's misfit runs over its own traces with
+fixed-order reductions, so a request returns bit-identical records, loss and gradient whether
+it runs alone, in a batch or next to other batches.
 """
 import collections
 import threading
@@ -251,65 +257,126 @@ class _Carver(object):
 
 
 # ------------------------------------------------------------------------------------------
-# one solve shape: plan, arena buffers, and (after its second use) a captured CUDA graph
+# batches: requests of one bucket packed into one batched plan, with its arena buffers and
+# (after the second use of the same composition) a captured CUDA graph
 # ------------------------------------------------------------------------------------------
-def _shape_key(req, grad, snapshot_precision, per_request_budget, silent_rel):
-    i64 = lambda a: np.asarray(a, dtype=np.int64).tobytes()  # noqa: E731
+def _i64(a):
+    return np.asarray(a, dtype=np.int64).tobytes()
+
+
+def _alone_plan(req, snapshot_precision, per_request_budget):
+    """The plan of ``req`` solved alone (host only): checks its geometry."""
+    vp = np.asarray(req.vp)
+    if vp.ndim != 2:
+        raise ValueError("vp must be a 2-D (nz, nx) array")
+    nz, nx = vp.shape
+    return AcousticPlan(nz=nz, nx=nx, nabc=req.nabc, free_surface=req.free_surface, src_z=req.src_z,
+                        src_x=req.src_x, rcv_z=req.rcv_z, rcv_x=req.rcv_x, nt=req.nt, dt=req.dt,
+                        dtype=torch.float32, snapshot_precision=snapshot_precision, memory_budget=per_request_budget)
+
+
+def _shape_key(req, grad, snapshot_precision, silent_rel):
+    """Requests that may share launches: same mode, grid, spacing, time axis, wavelet, absorbing
+    frame and receivers (their sources and models may differ)."""
     return (bool(grad), tuple(np.shape(req.vp)), float(req.dx), int(req.nt), float(req.dt), float(req.f0),
-            int(req.nabc), bool(req.free_surface), i64(req.src_z), i64(req.src_x), i64(req.rcv_z), i64(req.rcv_x),
-            str(snapshot_precision), int(per_request_budget), float(silent_rel))
+            int(req.nabc), bool(req.free_surface), _i64(req.rcv_z), _i64(req.rcv_x), str(snapshot_precision),
+            float(silent_rel))
 
 
-class _Shape(object):
-    """Everything of a solve that depends only on its shape (grid, geometry, nt, dt, f0, mode):
-    the plan, the arena range with its buffers, the wavelet and damping geometry, and the CUDA
-    graph of the whole device-side solve once the shape has been solved twice.
+def bucket_snapshot_every(req, snapshot_precision, batch_budget, max_batch_shots):
+    """Snapshot interval of every solve of ``req``'s bucket: the one a batch of ``max_batch_shots``
+    shots of this shape gets under ``batch_budget`` bytes. Fixing it per bucket keeps a request's
+    result independent of the batch it is packed into (host only)."""
+    vp = np.asarray(req.vp)
+    nz, nx = vp.shape
+    n = int(max_batch_shots)
+    return AcousticPlan(nz=nz, nx=nx, nabc=req.nabc, free_surface=req.free_surface,
+                        src_z=np.full(n, int(np.asarray(req.src_z)[0])), src_x=np.full(n, int(np.asarray(req.src_x)[0])),
+                        rcv_z=req.rcv_z, rcv_x=req.rcv_x, nt=req.nt, dt=req.dt, dtype=torch.float32,
+                        snapshot_precision=snapshot_precision, memory_budget=batch_budget).snapshot_every
 
-    The device-side solve (``_enqueue``) takes the model, its density, its damping frame and
-    the observed data from fixed buffers (the host computes density and damping exactly as
+
+def _batch_signature(bucket, reqs):
+    return (bucket,) + tuple((len(r.src_x), _i64(r.src_z), _i64(r.src_x)) for r in reqs)
+
+
+def request_bytes(req, snapshot_precision, per_request_budget, silent_rel=1e-6, max_batch_shots=32):
+    """Device bytes of ``req`` solved alone by a server with these settings (host only)."""
+    K = bucket_snapshot_every(req, snapshot_precision, per_request_budget, max_batch_shots)
+    grad = req.obs is not None
+    return _Batch([req], _shape_key(req, grad, snapshot_precision, silent_rel) + (K,), K, snapshot_precision,
+                  silent_rel).nbytes
+
+
+def _pad_models(v, n):
+    """Edge-replicate padding by n cells of a stack of models (nm, nz, nx)."""
+    return torch.nn.functional.pad(v[:, None], (n, n, n, n), mode="replicate")[:, 0]
+
+
+class _Batch(object):
+    """Requests of one bucket solved together: one batched plan (one model per request, the
+    requests' shots in order), one arena range with every buffer of the solve, and the CUDA
+    graph of the whole device-side solve once the same composition has been solved twice.
+
+    Each request's shots are grouped as a plan of its model alone groups them and every request
+    keeps its own snapshot interval (part of the bucket), so a request's records, loss and
+    gradient are bit-identical whether it is solved alone or packed with others.
+
+    The device-side solve (``_enqueue``) takes the models, their densities, their damping frames
+    and the observed data from fixed buffers (the host computes density and damping exactly as
     AcousticModel / AcousticPropagator do) and does every other step on the GPU -- the padded
-    coefficients, forward, misfit, adjoint and the chain rule to dL/dvp -- so one captured graph
-    replays it for any model of the shape."""
+    coefficients, forward, the per-request misfits, adjoint and the chain rule to dL/dvp -- so
+    one captured graph replays it for any models of the same composition."""
 
-    def __init__(self, req, snapshot_precision, per_request_budget, silent_rel):
-        vp = np.asarray(req.vp, dtype=np.float32)
-        if vp.ndim != 2:
-            raise ValueError("vp must be a 2-D (nz, nx) array")
-        self.nz, self.nx = vp.shape
-        self.ns, self.nr = len(req.src_x), len(req.rcv_x)
-        self.grad = req.obs is not None
-        if self.grad and tuple(np.shape(req.obs)) != (self.ns, req.nt, self.nr):
-            raise ValueError("obs has shape %s, expected %s" % (np.shape(req.obs), (self.ns, req.nt, self.nr)))
-        self.nt, self.dt, self.dx, self.f0, self.nabc = int(req.nt), float(req.dt), float(req.dx), float(req.f0), \
-            int(req.nabc)
+    def __init__(self, reqs, bucket, snapshot_every, snapshot_precision, silent_rel):
+        r0 = reqs[0]
+        self.nz, self.nx = np.shape(r0.vp)
+        self.nm = len(reqs)
+        self.ns_r = [len(r.src_x) for r in reqs]
+        self.ranges = []
+        s0 = 0
+        for n in self.ns_r:
+            self.ranges.append((s0, s0 + n))
+            s0 += n
+        self.ns, self.nr = s0, len(r0.rcv_x)
+        self.grad = bucket[0]
+        self.nt, self.dt, self.dx, self.f0, self.nabc = int(r0.nt), float(r0.dt), float(r0.dx), float(r0.f0), \
+            int(r0.nabc)
         self.silent_rel = float(silent_rel)
-        self.key = _shape_key(req, self.grad, snapshot_precision, per_request_budget, silent_rel)
-        self.plan = AcousticPlan(nz=self.nz, nx=self.nx, nabc=req.nabc, free_surface=req.free_surface,
-                                 src_z=req.src_z, src_x=req.src_x, rcv_z=req.rcv_z, rcv_x=req.rcv_x, nt=req.nt,
-                                 dt=req.dt, dtype=torch.float32, snapshot_precision=snapshot_precision,
-                                 memory_budget=per_request_budget)
+        self.bucket = bucket
+        self.key = _batch_signature(bucket, reqs)
+        shot_model = np.concatenate([np.full(n, m) for m, n in enumerate(self.ns_r)])
+        self.plan = AcousticPlan(nz=self.nz, nx=self.nx, nabc=self.nabc, free_surface=r0.free_surface,
+                                 src_z=np.concatenate([np.asarray(r.src_z) for r in reqs]),
+                                 src_x=np.concatenate([np.asarray(r.src_x) for r in reqs]), rcv_z=r0.rcv_z,
+                                 rcv_x=r0.rcv_x, nt=self.nt, dt=self.dt, dtype=torch.float32,
+                                 snapshot_precision=snapshot_precision, snapshot_every=snapshot_every,
+                                 shot_model=shot_model)
         self.ws_bytes = self.plan.workspace_bytes(self.grad)
         self.nzp, self.nxp = self.plan.grid_shape()
         rec = self.ns * self.nt * self.nr * 4
-        grid = self.nzp * self.nxp * 4
+        grid = self.nm * self.nzp * self.nxp * 4
+        model = self.nm * self.nz * self.nx * 4
         self.nbytes = (_aligned(self.ws_bytes) + 3 * _aligned(rec) + (2 * _aligned(rec) if self.grad else 0)
-                       + 3 * _aligned(grid) + 5 * _aligned(self.nz * self.nx * 4) + _aligned(self.ns * self.nt * 4))
-        self.cells = self.ns * self.nzp * self.nxp * self.nt
+                       + 3 * _aligned(grid) + 5 * _aligned(model) + _aligned(self.ns * self.nt * 4))
+        self.cells = [n * self.nzp * self.nxp * self.nt for n in self.ns_r]
         self.off = self.n = None
         self.bound = False
         self.graph = None
         self.uses = 0
 
-    # -- arena buffers and the shape's constant data (once per arena range)
+    # -- arena buffers and the batch's constant data (once per arena range)
     def _bind(self, arena, device):
         cv = _Carver(arena, self.off, self.off + self.n)
         shp = (self.ns, self.nt, self.nr)
+        gshp = (self.nm, self.nzp, self.nxp)
+        mshp = (self.nm, self.nz, self.nx)
         self.ws = cv.take((self.ws_bytes,), torch.uint8)
         self.recs = tuple(cv.take(shp, torch.float32) for _ in range(3))
-        self.a1, self.a2, self.damp = (cv.take((self.nzp, self.nxp), torch.float32) for _ in range(3))
-        self.fw = tuple(cv.take((self.nz, self.nx), torch.float32) for _ in range(3))
-        self.vp_d = cv.take((self.nz, self.nx), torch.float32)
-        self.rho_d = cv.take((self.nz, self.nx), torch.float32)
+        self.a1, self.a2, self.damp = (cv.take(gshp, torch.float32) for _ in range(3))
+        self.fw = tuple(cv.take(mshp, torch.float32) for _ in range(3))
+        self.vp_d = cv.take(mshp, torch.float32)
+        self.rho_d = cv.take(mshp, torch.float32)
         self.wav = cv.take((self.ns, self.nt), torch.float32)
         self.dx_t = torch.full((), self.dx, dtype=torch.float32, device=device)  # divisor of alpha1
         if self.grad:
@@ -319,21 +386,25 @@ class _Shape(object):
         self.wav.copy_(torch.from_numpy(np.ascontiguousarray(np.tile(w, (self.ns, 1)), dtype=np.float32)))
         self.bound = True
 
-    def _load(self, req):
-        """Copy this request's model, its Gardner density (310 vp^0.25, evaluated on the host in
-        float32 as AcousticModel.forward does) and its observed data into the fixed buffers."""
-        vp = np.ascontiguousarray(req.vp, dtype=np.float32)
-        self.vp_d.copy_(torch.from_numpy(vp))
-        self.rho_d.copy_(torch.from_numpy(np.power(vp, 0.25) * 310))
-        self.damp.copy_(torch.from_numpy(np.ascontiguousarray(
-            bc_pml(self.nx, self.nz, self.dx, self.dx, self.nabc, vp.max(), free_surface=False), dtype=np.float32)))
-        if self.grad:
-            self.obs.copy_(torch.from_numpy(np.ascontiguousarray(req.obs, dtype=np.float32)))
+    def _load(self, reqs):
+        """Copy the requests' models, their Gardner densities (310 vp^0.25, evaluated on the host
+        in float32 as AcousticModel.forward does), damping frames and observed data into the fixed
+        buffers."""
+        for m, req in enumerate(reqs):
+            vp = np.ascontiguousarray(req.vp, dtype=np.float32)
+            self.vp_d[m].copy_(torch.from_numpy(vp))
+            self.rho_d[m].copy_(torch.from_numpy(np.power(vp, 0.25) * 310))
+            self.damp[m].copy_(torch.from_numpy(np.ascontiguousarray(
+                bc_pml(self.nx, self.nz, self.dx, self.dx, self.nabc, vp.max(), free_surface=False),
+                dtype=np.float32)))
+            if self.grad:
+                s0, s1 = self.ranges[m]
+                self.obs[s0:s1].copy_(torch.from_numpy(np.ascontiguousarray(req.obs, dtype=np.float32)))
 
     def _enqueue(self, h):
         """The whole solve on the current stream (handle h): device work only, no host sync."""
         nb = self.nabc
-        c, den = _pad(self.vp_d, nb), _pad(self.rho_d, nb)
+        c, den = _pad_models(self.vp_d, nb), _pad_models(self.rho_d, nb)
         t1 = den * c
         # divisor as a device tensor: true division, as the drop-in propagator computes alpha1
         self.a1.copy_(t1 * c * self.dt / self.dx_t)
@@ -342,22 +413,25 @@ class _Shape(object):
                               fw=self.fw, stream=h)
         if not self.grad:
             return
-        self.out_loss, _ = l2_misfit_and_adjoint(self.recs[0], self.obs, self.dt, silent_rel=self.silent_rel, stream=h,
-                                                 adj=self.adj)
+        self.out_loss = []
+        for s0, s1 in self.ranges:  # each request's misfit over its own traces
+            loss, _ = l2_misfit_and_adjoint(self.recs[0][s0:s1], self.obs[s0:s1], self.dt, silent_rel=self.silent_rel,
+                                            stream=h, adj=self.adj[s0:s1])
+            self.out_loss.append(loss)
         ga1, _ = self.plan.run_backward(self.a1, self.a2, self.damp, self.wav, (self.adj, None, None), self.ws,
                                         stream=h)
         # alpha1 = ((den c) c) dt / dx; alpha2 and rho do not depend on vp
         g_t2 = ga1 * (self.dt / self.dx)
-        self.out_grad = fold_replicate_pad(g_t2 * t1 + g_t2 * c * den, nb)
+        self.out_grad = [fold_replicate_pad(g_t2[m] * t1[m] + g_t2[m] * c[m] * den[m], nb) for m in range(self.nm)]
 
-    def run(self, req, arena, stream, capture_stream, device, use_graphs):
-        """Solve ``req`` in this shape's arena range and wait for it; returns (loss, grad, records)."""
+    def run(self, reqs, arena, stream, capture_stream, device, use_graphs):
+        """Solve ``reqs`` in this batch's arena range and wait; returns [(loss, grad, records)]."""
         if not self.bound:
             self._bind(arena, device)
         with torch.cuda.stream(stream):
-            self._load(req)
+            self._load(reqs)
         if use_graphs and self.graph is None and self.uses >= 1:
-            # second solve of this shape: capture the device-side solve once, replay it from now on
+            # second solve of this composition: capture the device-side solve once, replay it from now on
             capture_stream.wait_stream(stream)
             g = torch.cuda.CUDAGraph()
             with torch.cuda.stream(capture_stream):
@@ -375,26 +449,62 @@ class _Shape(object):
                 self._enqueue(stream.cuda_stream)
             code = self.plan.status(self.ws, self.grad, stream=stream.cuda_stream)
             if code != 0:
-                raise RuntimeError("solve %d: a pipeline wait timed out on the GPU (status %d)" % (req.rid, code))
+                raise RuntimeError("solve of requests %s: a pipeline wait timed out on the GPU (status %d)"
+                                   % ([r.rid for r in reqs], code))
             self.uses += 1
             if not self.grad:
-                return None, None, self.recs[0].cpu().numpy()
-            return float(self.out_loss.cpu()), self.out_grad.cpu().numpy(), None
+                rec = self.recs[0].cpu().numpy()
+                return [(None, None, rec[s0:s1]) for s0, s1 in self.ranges]
+            losses = torch.stack(self.out_loss).cpu().numpy()
+            grads = torch.stack(self.out_grad).cpu().numpy()
+            return [(float(losses[m]), grads[m], None) for m in range(self.nm)]
 
 
 # ------------------------------------------------------------------------------------------
 # server
 # ------------------------------------------------------------------------------------------
+class _Entry(object):
+    """A queued request: arrival time, the request, its future, its bucket and shot count."""
+    __slots__ = ("t", "req", "fut", "bucket", "shots", "snapshot_every")
+
+    def __init__(self, t, req, fut, bucket, shots, snapshot_every):
+        self.t, self.req, self.fut, self.bucket, self.shots, self.snapshot_every = t, req, fut, bucket, shots, \
+            snapshot_every
+
+
+def form_batch(queue, i, max_shots, max_requests):
+    """Entries of ``queue`` (arrival order) that join ``queue[i]`` in one batch: later entries of
+    the same bucket, in arrival order, while the batch keeps to ``max_shots`` shots and
+    ``max_requests`` requests. Returns their indices, ``i`` first."""
+    head = queue[i]
+    idx, shots = [i], head.shots
+    for j in range(i + 1, len(queue)):
+        if len(idx) >= max_requests:
+            break
+        e = queue[j]
+        if e.bucket == head.bucket and shots + e.shots <= max_shots:
+            idx.append(j)
+            shots += e.shots
+    return idx
+
+
 class SolveServer(object):
-    """Admit, overlap and complete solves under an HBM budget (module docstring).
+    """Admit, batch, overlap and complete solves under an HBM budget (module docstring).
 
-    ``graphs``: keep each solved shape (plan, arena range, buffers) after its request completes
-    and capture the device-side solve in a CUDA graph at its second use; later requests of the
-    same shape copy in their model and data and replay the graph. Idle shapes keep their arena
-    ranges until admission needs the room (least recently used first)."""
+    Continuous batching: when a slot is free, the oldest waiting request is packed with the later
+    waiting requests of its bucket (same grid, time axis, wavelet, receivers and snapshot
+    interval; ``max_batch_shots`` shots and ``max_batch_requests`` requests at most) into one
+    batched plan, whose launches advance all their shots together; batches on different slots
+    overlap on the GPU. A request's result does not depend on its batch.
 
-    def __init__(self, device="cuda:0", hbm_budget=150 << 30, slots=4, snapshot_precision="bf16",
-                 per_request_budget=None, max_wait_s=2.0, reserve=None, silent_rel=1e-6, graphs=True):
+    ``graphs``: keep each solved batch (plan, arena range, buffers) after it completes and
+    capture its device-side solve in a CUDA graph at its second use; later batches of the same
+    composition copy in their models and data and replay the graph. Idle batches keep their
+    arena ranges until admission needs the room (least recently used first)."""
+
+    def __init__(self, device="cuda:0", hbm_budget=150 << 30, slots=4, snapshot_precision="fp24",
+                 per_request_budget=None, max_wait_s=2.0, reserve=None, silent_rel=1e-6, graphs=True,
+                 max_batch_shots=32, max_batch_requests=16):
         if not torch.cuda.is_available():
             raise RuntimeError("SolveServer needs a CUDA device (adfwi_gb300 has no CPU implementation)")
         self.device = torch.device(device)
@@ -404,22 +514,30 @@ class SolveServer(object):
         self.arena = torch.empty(self.book.capacity, dtype=torch.uint8, device=self.device)
         self.slots = int(slots)
         self.snapshot_precision = snapshot_precision
+        # device bytes that one batch of max_batch_shots shots may take (sets each bucket's
+        # snapshot interval)
         self.per_request_budget = int(per_request_budget if per_request_budget is not None
                                       else max(1 << 30, self.book.capacity // max(1, self.slots)))
         self.max_wait_s = float(max_wait_s)
         self.silent_rel = float(silent_rel)
         self.graphs = bool(graphs)
+        self.max_batch_shots = int(max_batch_shots)
+        self.max_batch_requests = int(max_batch_requests)
         self._cv = threading.Condition()
-        self._queue = []      # (t_arrival, (shape, request), future), arrival order
-        self._ready = []      # (t_arrival, shape, request, future, t_admit)
-        self._idle = collections.OrderedDict()  # id(shape) -> shape, least recently used first
+        self._queue = []      # _Entry, arrival order
+        self._ready = []      # (batch, [entries], t_admit)
+        self._idle = collections.OrderedDict()  # id(batch) -> batch, least recently used first
+        self._planned = collections.OrderedDict()  # signature -> planned batch without a range yet
+        self._bucket_K = {}   # shape key -> snapshot interval of the bucket
         self._running = 0
         self._closed = False
         self._next_id = 0
         self.completed: List[SolveResult] = []
         self.failed = 0
+        self.cancelled = 0
         self.peak_running = 0
         self.graph_replays = 0
+        self.batches = 0
         self._streams = [torch.cuda.Stream(device=self.device) for _ in range(self.slots)]
         self._capture_streams = [torch.cuda.Stream(device=self.device) for _ in range(self.slots)]
         self._workers = [threading.Thread(target=self._worker, args=(k,), daemon=True, name="adfwi-solve-%d" % k)
@@ -429,17 +547,30 @@ class SolveServer(object):
 
     # -------------------------------------------------------------- client side
     def submit(self, req: SolveRequest, t_arrival=None) -> Future:
-        """Queue a request; the future resolves to a SolveResult (or raises the solve's error)."""
+        """Queue a request; the future resolves to a SolveResult (or raises the solve's error).
+        Cancelling the future before its solve starts withdraws the request."""
         fut = Future()
         t = time.perf_counter() if t_arrival is None else t_arrival
+        grad = req.obs is not None
         try:
-            shape = _Shape(req, self.snapshot_precision, self.per_request_budget, self.silent_rel)
+            alone = _alone_plan(req, self.snapshot_precision, self.per_request_budget)
+            if grad and tuple(np.shape(req.obs)) != (alone.ns, req.nt, alone.nr):
+                raise ValueError("obs has shape %s, expected %s" % (np.shape(req.obs), (alone.ns, req.nt, alone.nr)))
+            skey = _shape_key(req, grad, self.snapshot_precision, self.silent_rel)
+            with self._cv:
+                K = self._bucket_K.get(skey)
+            if K is None:
+                K = bucket_snapshot_every(req, self.snapshot_precision, self.per_request_budget, self.max_batch_shots)
+                with self._cv:
+                    self._bucket_K[skey] = K
+            bucket = skey + (K,)
+            need = _Batch([req], bucket, K, self.snapshot_precision, self.silent_rel).nbytes
         except Exception as e:
             fut.set_exception(e)
             return fut
-        if shape.nbytes > self.book.capacity:
+        if need > self.book.capacity:
             fut.set_exception(MemoryError("request %d needs %d bytes of device memory, more than the %d-byte arena"
-                                          % (req.rid, shape.nbytes, self.book.capacity)))
+                                          % (req.rid, need, self.book.capacity)))
             return fut
         with self._cv:
             if self._closed:
@@ -447,7 +578,7 @@ class SolveServer(object):
             if req.rid < 0:
                 req.rid = self._next_id
             self._next_id += 1
-            self._queue.append((t, (shape, req), fut))
+            self._queue.append(_Entry(t, req, fut, bucket, len(req.src_x), K))
             self._admit_locked()
             self._cv.notify_all()
         return fut
@@ -460,8 +591,8 @@ class SolveServer(object):
             for w in self._workers:
                 w.join()
         with self._cv:
-            for shape in list(self._idle.values()):
-                self.book.free(shape.off, shape.n)
+            for batch in list(self._idle.values()):
+                self.book.free(batch.off, batch.n)
             self._idle.clear()
 
     def __enter__(self):
@@ -474,7 +605,9 @@ class SolveServer(object):
         with self._cv:
             self.completed = []
             self.failed = 0
+            self.cancelled = 0
             self.graph_replays = 0
+            self.batches = 0
             self.peak_running = self._running
             self.book.peak = self.book.used
 
@@ -486,24 +619,25 @@ class SolveServer(object):
         t0 = min(r.t_arrival for r in done)
         t1 = max(r.t_done for r in done)
         cells = sum(r.cell_updates for r in done)
-        return {"requests": len(done), "failed": self.failed, "p50_s": float(np.percentile(lat, 50)),
-                "p99_s": float(np.percentile(lat, 99)), "mean_s": float(lat.mean()), "makespan_s": t1 - t0,
-                "gcell_per_s": cells / (t1 - t0) / 1e9, "peak_arena_bytes": self.book.peak,
-                "arena_bytes": self.book.capacity, "peak_concurrency": self.peak_running,
-                "graph_replays": self.graph_replays}
+        return {"requests": len(done), "failed": self.failed, "cancelled": self.cancelled,
+                "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+                "mean_s": float(lat.mean()), "makespan_s": t1 - t0, "gcell_per_s": cells / (t1 - t0) / 1e9,
+                "peak_arena_bytes": self.book.peak, "arena_bytes": self.book.capacity,
+                "peak_concurrency": self.peak_running, "graph_replays": self.graph_replays, "batches": self.batches,
+                "requests_per_batch": len(done) / max(1, self.batches)}
 
     # -------------------------------------------------------------- scheduling
     def _take_idle(self, key):
-        for sid, shape in self._idle.items():
-            if shape.key == key:
-                del self._idle[sid]
-                return shape
+        for bid, batch in self._idle.items():
+            if batch.key == key:
+                del self._idle[bid]
+                return batch
         return None
 
     def _alloc_evicting(self, nbytes):
         got = self.book.alloc(nbytes)
         while got is None and self._idle:
-            _, old = self._idle.popitem(last=False)  # least recently used idle shape
+            _, old = self._idle.popitem(last=False)  # least recently used idle batch
             self.book.free(old.off, old.n)
             got = self.book.alloc(nbytes)
         return got
@@ -512,24 +646,60 @@ class SolveServer(object):
         now = time.perf_counter()
         free = self.slots - self._running - len(self._ready)
         q = self._queue
-        strict = bool(q) and now - q[0][0] > self.max_wait_s
+        # withdrawn requests leave the queue
+        keep = [e for e in q if not e.fut.cancelled()]
+        self.cancelled += len(q) - len(keep)
+        q[:] = keep
+        strict = bool(q) and now - q[0].t > self.max_wait_s
         i = 0
         while i < len(q) and free > 0:
-            t, (shape, req), fut = q[i]
-            cached = self._take_idle(shape.key)
-            if cached is not None:
-                shape = cached
-            else:
-                got = self._alloc_evicting(shape.nbytes)
-                if got is None:
-                    if strict:
-                        break  # the oldest request has waited too long: nothing may pass it
-                    i += 1
-                    continue
-                shape.off, shape.n = got
-            del q[i]
-            self._ready.append((t, shape, req, fut, now))
+            idx = form_batch(q, i, self.max_batch_shots, self.max_batch_requests)
+            admitted, dropped = None, False
+            while idx and admitted is None:  # shed the newest members until the batch's range fits
+                members = [q[j] for j in idx]
+                reqs = [e.req for e in members]
+                key = _batch_signature(members[0].bucket, reqs)
+                batch = self._take_idle(key)
+                if batch is None:
+                    batch = self._planned.pop(key, None)
+                    if batch is None:
+                        try:
+                            batch = _Batch(reqs, members[0].bucket, members[0].snapshot_every,
+                                           self.snapshot_precision, self.silent_rel)
+                        except Exception as e:  # a batch that cannot be planned: its head fails alone
+                            if len(idx) == 1:
+                                q[i].fut.set_exception(e)
+                                del q[i]
+                                self.failed += 1
+                                dropped = True
+                                break
+                            idx = idx[:1]
+                            continue
+                    got = self._alloc_evicting(batch.nbytes)
+                    if got is None:
+                        self._remember_planned(key, batch)
+                        idx = idx[:-1]
+                        continue
+                    batch.off, batch.n = got
+                admitted = (batch, members)
+            if dropped:
+                continue
+            if admitted is None:
+                if strict:
+                    break  # the oldest request has waited too long: nothing may pass it
+                i += 1
+                continue
+            for j in sorted(idx, reverse=True):
+                del q[j]
+            self._ready.append((admitted[0], admitted[1], now))
             free -= 1
+
+    def _remember_planned(self, key, batch):
+        """Keep a planned batch that did not fit yet (host tables only), so that the next
+        admission attempt does not plan it again."""
+        self._planned[key] = batch
+        while len(self._planned) > 64:
+            self._planned.popitem(last=False)
 
     def _worker(self, k):
         stream, cstream = self._streams[k], self._capture_streams[k]
@@ -542,39 +712,45 @@ class SolveServer(object):
                     if self._closed and not self._queue:
                         return
                     self._cv.wait(timeout=0.05)
-                t_arr, shape, req, fut, t_admit = self._ready.pop(0)
+                batch, members, t_admit = self._ready.pop(0)
                 self._running += 1
                 self.peak_running = max(self.peak_running, self._running)
-            res = err = None
+            out = err = None
             replayed = False
             try:
-                loss, grad, rec = shape.run(req, self.arena, stream, cstream, self.device, self.graphs)
-                replayed = shape.graph is not None  # this solve ran as a graph replay (its shape's second use on)
-                res = SolveResult(req.rid, loss, grad, rec, t_arr, t_admit, time.perf_counter(), shape.cells,
-                                  shape.n, shape.plan.snapshot_every)
-            except Exception as e:  # the others keep running; the future carries the error
+                out = batch.run([e.req for e in members], self.arena, stream, cstream, self.device, self.graphs)
+                replayed = batch.graph is not None  # this solve ran as a graph replay (its composition's second use on)
+            except Exception as e:  # the other batches keep running; the futures carry the error
                 err = e
+            t_done = time.perf_counter()
             try:
                 stream.synchronize()  # the range may be reused only once this solve's work is done
             except Exception as e:
                 err = err or e
+            results = []
+            if err is None:
+                for m, (e, (loss, grad, rec)) in enumerate(zip(members, out)):
+                    results.append(SolveResult(e.req.rid, loss, grad, rec, e.t, t_admit, t_done, batch.cells[m],
+                                               batch.n, batch.plan.snapshot_every))
             with self._cv:
                 self._running -= 1
                 if self.graphs and err is None:
-                    self._idle[id(shape)] = shape  # keep the shape (and its graph) for the next request like it
+                    self._idle[id(batch)] = batch  # keep the batch (and its graph) for the next one like it
                 else:
-                    self.book.free(shape.off, shape.n)
-                if res is not None and err is None:
-                    self.completed.append(res)
+                    self.book.free(batch.off, batch.n)
+                if err is None:
+                    self.completed.extend(results)
                     self.graph_replays += int(replayed)
+                    self.batches += 1
                 else:
-                    self.failed += 1
+                    self.failed += len(members)
                 self._admit_locked()
                 self._cv.notify_all()
-            if err is None:
-                fut.set_result(res)
-            else:
-                fut.set_exception(err)
+            for m, e in enumerate(members):
+                if err is None:
+                    e.fut.set_result(results[m])
+                else:
+                    e.fut.set_exception(err)
 
 
 def replay(server, timed_requests):

@@ -507,37 +507,49 @@ def plain_gpu_leg(args, dev):
 def serving_arm(args, dev):
     """Served stream of mixed-size forward+gradient requests (Poisson arrivals, grids from
     {100x300, 200x600, 300x900, 500x1500}, 1-16 shots, nt in {1000, 2000, 4000}, random layered
-    vp, FP32 stencils with BF16 snapshots, PML 50, 150 GB HBM admission budget): the
-    continuous-batching server against the same stream solved one request at a time."""
+    vp, FP32 stencils with FP24 snapshots, PML 50, 150 GB HBM admission budget): the
+    continuous-batching server (same-bucket requests packed into shared launches, batches
+    overlapped on several streams) at each arrival rate, against the same stream solved one
+    request at a time (one slot, no packing) at the highest rate."""
     from adfwi_gb300 import serving as S
-    stream = S.synthetic_stream(args.serve_requests, args.serve_rate, seed=0)
-    timed = [(t, req) for t, _, req in stream]
+    rates = [float(r) for r in str(args.serve_rates).split(",") if r]
     budget = 150 << 30
-    out = {}
+    out = {"served": {}}
     results = {}
     per_req = None
-    for name, slots in (("served", args.serve_slots), ("one_at_a_time", 1)):
-        with S.SolveServer(device=dev, hbm_budget=budget, slots=slots, snapshot_precision="bf16",
-                           per_request_budget=per_req) as srv:
+    stream = S.synthetic_stream(args.serve_requests, max(rates), seed=0)
+    modes = [("served@%g" % r, r, args.serve_slots, 32) for r in rates] + [("one_at_a_time", max(rates), 1, 1)]
+    for name, rate, slots, mbr in modes:
+        timed = [(t * max(rates) / rate, req) for t, _, req in stream]  # the same requests, arrivals rescaled
+        with S.SolveServer(device=dev, hbm_budget=budget, slots=slots, snapshot_precision="fp24",
+                           per_request_budget=per_req, max_batch_requests=mbr) as srv:
             per_req = srv.per_request_budget
             if not results:
                 S.observed_data(srv, stream)  # observed data of the true models (setup, untimed)
-                srv.reset_stats()
+            srv.reset_stats()
             results[name] = S.replay(srv, timed)
             st = srv.stats()
-        out[name] = {"p50_s": round(st["p50_s"], 4), "p99_s": round(st["p99_s"], 4), "mean_s": round(st["mean_s"], 4),
-                     "throughput_gcell_per_s": round(st["gcell_per_s"], 3),
-                     "requests_per_s": round(st["requests"] / st["makespan_s"], 3), "slots": slots,
-                     "peak_concurrency": st["peak_concurrency"], "peak_arena_gb": round(st["peak_arena_bytes"] / 2 ** 30, 2),
-                     "graph_replays": st["graph_replays"]}
+        rec = {"arrival_rate_per_s": rate, "p50_s": round(st["p50_s"], 4), "p99_s": round(st["p99_s"], 4),
+               "mean_s": round(st["mean_s"], 4), "throughput_gcell_per_s": round(st["gcell_per_s"], 3),
+               "requests_per_s": round(st["requests"] / st["makespan_s"], 3), "slots": slots,
+               "batches": st["batches"], "requests_per_batch": round(st["requests_per_batch"], 2),
+               "peak_concurrency": st["peak_concurrency"], "peak_arena_gb": round(st["peak_arena_bytes"] / 2 ** 30, 2),
+               "graph_replays": st["graph_replays"]}
+        if name == "one_at_a_time":
+            out[name] = rec
+        else:
+            out["served"][name] = rec
+    ref = results["one_at_a_time"]
     same = all(a.loss == b.loss and np.array_equal(a.grad, b.grad)
-               for a, b in zip(results["served"], results["one_at_a_time"]))
-    out.update({"requests": len(timed), "arrival_rate_per_s": args.serve_rate, "hbm_budget_gb": budget / 2 ** 30,
+               for name in results for a, b in zip(results[name], ref))
+    top = out["served"]["served@%g" % max(rates)]
+    out.update({"requests": args.serve_requests, "hbm_budget_gb": budget / 2 ** 30,
                 "arena_gb": round(srv.book.capacity / 2 ** 30, 2), "per_request_budget_gb": round(per_req / 2 ** 30, 2),
-                "bit_identical_alone_vs_mix": bool(same),
-                "speedup_vs_one_at_a_time": round(out["served"]["throughput_gcell_per_s"]
+                "snapshot_precision": "fp24", "bit_identical_alone_vs_mix": bool(same),
+                "graph_replays": sum(v["graph_replays"] for v in out["served"].values()),
+                "speedup_vs_one_at_a_time": round(top["throughput_gcell_per_s"]
                                                   / out["one_at_a_time"]["throughput_gcell_per_s"], 3),
-                "sample": "first %d requests of the seeded 2000-request stream" % len(timed)})
+                "sample": "first %d requests of the seeded 2000-request stream" % args.serve_requests})
     return out
 
 
@@ -740,7 +752,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--serve-requests", type=int, default=48,
                     help="requests of the served mixed-size stream (0 skips the serving measurement)")
-    ap.add_argument("--serve-rate", type=float, default=50.0, help="Poisson arrival rate of the served stream (1/s)")
+    ap.add_argument("--serve-rates", default="10,500",
+                    help="Poisson arrival rates of the served stream (1/s), comma separated")
     ap.add_argument("--serve-slots", type=int, default=4, help="concurrent solves of the server")
     ap.add_argument("--no-elastic", action="store_true", help="skip the VTI-elastic gradient measurement")
     ap.add_argument("--elastic-only", action="store_true", help="run only the VTI-elastic gradient measurement")

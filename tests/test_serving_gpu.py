@@ -1,5 +1,6 @@
 """Solve server on the GPU: results equal the drop-in propagator's, each request's result
-is bit-identical alone and in a mix, and admission keeps to the HBM budget."""
+is bit-identical alone, in a batch and in a mix, admission keeps to the HBM budget, and a
+failing or withdrawn request leaves the others' results unchanged."""
 import numpy as np
 import pytest
 import torch
@@ -78,7 +79,7 @@ SHAPES = [(48, 80, 2, 300), (64, 128, 3, 500), (40, 64, 1, 400), (80, 96, 4, 300
 
 
 def test_each_result_is_the_same_alone_and_in_the_mix(native_lib):
-    budget = 256 << 20  # small per-solve budget: the longer solves keep BF16 snapshots
+    budget = 256 << 20  # small per-solve budget: the longer solves keep FP24 snapshots
     reqs = [_request(100 + k, *shape) for k, shape in enumerate(SHAPES)]
     with S.SolveServer(hbm_budget=2 << 30, slots=1, per_request_budget=budget) as srv:
         for req, vp_true in reqs:
@@ -101,7 +102,7 @@ def test_admission_keeps_to_the_budget(native_lib):
     req, vp_true = _request(7, 48, 80, 2, 300)
     with S.SolveServer(hbm_budget=1 << 30, slots=1) as srv:
         _with_obs(srv, req, vp_true)
-    need = S._Shape(req, "bf16", 64 << 20, 1e-6).nbytes
+    need = S.request_bytes(req, "fp24", 64 << 20, 1e-6)
     # room for one solve at a time: the second waits for the first to free its range
     with S.SolveServer(hbm_budget=int(need * 1.5), reserve=0, slots=2, per_request_budget=64 << 20) as srv:
         futs = [srv.submit(req) for _ in range(3)]
@@ -143,7 +144,7 @@ def test_idle_shapes_are_evicted_for_room(native_lib):
     with S.SolveServer(hbm_budget=1 << 30, slots=1) as srv:
         _with_obs(srv, ra, va)
         _with_obs(srv, rb, vb)
-    need = max(S._Shape(r, "bf16", 64 << 20, 1e-6).nbytes for r in (ra, rb))
+    need = max(S.request_bytes(r, "fp24", 64 << 20, 1e-6) for r in (ra, rb))
     with S.SolveServer(hbm_budget=int(need * 1.5), reserve=0, slots=1, per_request_budget=64 << 20,
                        graphs=False) as srv:
         ref = [srv.submit(r).result() for r in (ra, rb)]
@@ -152,3 +153,58 @@ def test_idle_shapes_are_evicted_for_room(native_lib):
         assert srv.stats()["peak_arena_bytes"] <= srv.book.capacity
     for e, g in zip(ref + ref, got):
         assert e.loss == g.loss and np.array_equal(e.grad, g.grad)
+
+
+def _blocker():
+    """A long forward solve (another bucket) that holds a server's only slot while other
+    requests queue up behind it."""
+    return _request(299, 48, 80, 1, 20000, true=True)[0]
+
+
+def test_batched_requests_equal_their_solves_alone(native_lib):
+    """Requests of one bucket (same grid, nt, receivers) with different models and shot counts
+    are packed into shared launches; each result is bit-identical to the request solved alone."""
+    reqs = [_request(200 + k, 48, 80, ns, 300) for k, ns in enumerate((2, 1, 3, 2))]
+    with S.SolveServer(hbm_budget=2 << 30, slots=1, graphs=False) as srv:
+        for req, vp_true in reqs:
+            _with_obs(srv, req, vp_true)
+    with S.SolveServer(hbm_budget=2 << 30, slots=1, graphs=False, max_batch_requests=1) as srv:
+        alone = [srv.submit(req).result() for req, _ in reqs]
+        assert srv.stats()["requests_per_batch"] == 1
+    with S.SolveServer(hbm_budget=2 << 30, slots=1, graphs=False) as srv:
+        blocker = srv.submit(_blocker())  # occupies the slot while the others queue up
+        futs = [srv.submit(req) for req, _ in reqs]
+        blocker.result()
+        batched = [f.result() for f in futs]
+        st = srv.stats()
+    assert st["batches"] == 2 and st["requests_per_batch"] == 2.5  # the blocker, then one batch of four
+    for a, b in zip(alone, batched):
+        assert a.rid == b.rid and a.loss == b.loss and np.array_equal(a.grad, b.grad)
+
+
+def test_failing_and_withdrawn_requests_leave_the_others_unchanged(native_lib):
+    """A request whose plan rejects its geometry fails at submission, a request withdrawn by
+    cancelling its future while it waits never runs, and the requests around them return what
+    they return alone."""
+    reqs = [_request(300 + k, 48, 80, 2, 300) for k in range(3)]
+    with S.SolveServer(hbm_budget=2 << 30, slots=1, graphs=False) as srv:
+        for req, vp_true in reqs:
+            _with_obs(srv, req, vp_true)
+        alone = [srv.submit(req).result() for req, _ in reqs]
+    bad = S.SolveRequest(vp=reqs[0][0].vp, dx=10.0, nt=300, dt=1e-3, f0=18.0, src_z=np.array([2]),
+                         src_x=np.array([10 ** 6]), rcv_z=np.full(80, 2), rcv_x=np.arange(80), nabc=16)
+    with S.SolveServer(hbm_budget=2 << 30, slots=1, graphs=False) as srv:
+        blocker = srv.submit(_blocker())
+        first = srv.submit(reqs[0][0])
+        failed = srv.submit(bad)
+        withdrawn = srv.submit(reqs[1][0])
+        assert withdrawn.cancel()  # still queued behind the blocker
+        last = srv.submit(reqs[2][0])
+        blocker.result()
+        got = [first.result(), last.result()]
+        st = srv.stats()
+    with pytest.raises(RuntimeError):
+        failed.result()
+    assert withdrawn.cancelled() and st["cancelled"] == 1 and st["requests"] == 3
+    for a, b in zip((alone[0], alone[2]), got):
+        assert a.loss == b.loss and np.array_equal(a.grad, b.grad)

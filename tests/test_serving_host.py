@@ -119,3 +119,15 @@ def test_synthetic_stream_is_seeded_and_shaped():
         assert r.meta["shape"] in S.GRIDS and 1 <= r.meta["shots"] <= 16 and r.nt in (1000, 2000, 4000)
         assert r.vp.shape == tv.shape == r.meta["shape"] and len(r.src_x) == r.meta["shots"]
         assert np.all(np.diff(tv.mean(axis=1)) >= -1e-3)  # velocity grows with depth on average
+
+
+def test_form_batch_packs_the_oldest_requests_of_one_bucket():
+    """The oldest waiting request is packed with the later requests of its bucket, in arrival
+    order, within the shot and request caps; other buckets wait for their own batch."""
+    E = S._Entry
+    q = [E(0.0, "a", None, "B1", 4, 10), E(0.1, "b", None, "B2", 8, 10), E(0.2, "c", None, "B1", 8, 10),
+         E(0.3, "d", None, "B1", 30, 10), E(0.4, "e", None, "B1", 2, 10), E(0.5, "f", None, "B1", 1, 10)]
+    assert S.form_batch(q, 0, 32, 16) == [0, 2, 4, 5]      # d would pass 32 shots: skipped, later ones join
+    assert S.form_batch(q, 0, 32, 2) == [0, 2]             # request cap
+    assert S.form_batch(q, 1, 32, 16) == [1]               # alone in its bucket
+    assert S.form_batch(q, 3, 32, 16) == [3, 4]            # 30 + 2 shots

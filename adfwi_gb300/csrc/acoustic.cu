@@ -659,8 +659,10 @@ int resident_fwd_blocks() {
 }
 
 // Shots per unit for the persistent TMA kernels: balance the units over the resident blocks
-// (the block with the most units sets the time) against the per-unit flush of the partial
-// accumulator planes (about half an item's worth of traffic).
+// (the block with the most units sets the time) against the per-unit costs (the coefficient
+// loads, and the load and flush of the partial accumulator planes), weighted as 1.5 items: the
+// weight that reproduces the measured optimum of a sweep of 1, 2, 4 and 8 shots per unit on the
+// 600 x 1600 grid with 8 and 32 shots.
 int pick_unit_shots(const std::vector<int>& model_shot_beg, int ntiles, int blocks_fwd, int blocks_adj) {
   const int nm = (int)model_shot_beg.size() - 1;
   int maxns = 1;
@@ -673,7 +675,7 @@ int pick_unit_shots(const std::vector<int>& model_shot_beg, int ntiles, int bloc
     const long long units = (long long)ntiles * groups;
     const long long pf = (units + blocks_fwd - 1) / blocks_fwd;
     const long long pa = (units + blocks_adj - 1) / blocks_adj;
-    const double cost = (double)(pf + 2 * pa) * (G + 0.5);  // the adjoint step takes about twice as long
+    const double cost = (double)(pf + 2 * pa) * (G + 1.5);  // the adjoint step takes about twice as long
     if (cost < best_cost - 1e-9) {
       best_cost = cost;
       best = G;

@@ -153,6 +153,35 @@ class AcousticPlan(object):
                                                int(bool(with_gradient)), ctypes.byref(v), st), "adfwi_acoustic_status")
         return v.value
 
+    def l2_loss(self, syn, obs, workspace, silent_rel=0.0, normalise_obs=False, stream=None):
+        """Normalised L2 misfit of the forward's p records ``syn`` against ``obs`` (ns, nt, nr): each
+        model's loss as FP64 device values (nmodels,); keeps the per-trace factors in the gradient
+        ``workspace`` for run_backward_l2."""
+        shp = (self.ns, self.nt, self.nr)
+        self._check(syn, shp, "syn")
+        obs = obs.to(dtype=self.dtype).contiguous()
+        self._check(obs, shp, "obs")
+        loss = torch.empty((self.nm,), dtype=torch.float64, device=syn.device)
+        st = ctypes.c_void_p(stream) if stream is not None else N.stream_handle(syn.device)
+        N.check(self.lib.adfwi_acoustic_l2_loss(self.handle, N.ptr(syn), N.ptr(obs), float(silent_rel),
+                                                int(bool(normalise_obs)), N.ptr(loss), N.ptr(workspace),
+                                                workspace.numel(), st), "adfwi_acoustic_l2_loss")
+        return loss
+
+    def run_backward_l2(self, alpha1, wavelet, syn, obs, workspace, grad_scale, normalise_obs=False, stream=None):
+        """Adjoint solve whose p-record source is the misfit of l2_loss (formed as it is injected)
+        times ``grad_scale`` (a one-element FP64 device tensor); returns (dL/d alpha1, dL/d alpha2)."""
+        obs = obs.to(dtype=self.dtype).contiguous()
+        gs = grad_scale.to(dtype=torch.float64).reshape(1).contiguous()
+        ga1 = torch.empty_like(alpha1)
+        ga2 = torch.empty_like(alpha1)
+        st = ctypes.c_void_p(stream) if stream is not None else N.stream_handle(alpha1.device)
+        N.check(self.lib.adfwi_acoustic_backward_l2(self.handle, N.ptr(wavelet), N.ptr(syn), N.ptr(obs),
+                                                    int(bool(normalise_obs)), N.ptr(gs), N.ptr(ga1), N.ptr(ga2),
+                                                    N.ptr(workspace), workspace.numel(), st),
+                "adfwi_acoustic_backward_l2")
+        return ga1, ga2
+
     def run_backward(self, alpha1, alpha2, damp, wavelet, grads, workspace, stream=None):
         """Adjoint solve after run_forward(with_gradient=True); returns (dL/d alpha1, dL/d alpha2)."""
         shp = (self.ns, self.nt, self.nr)
@@ -213,3 +242,36 @@ class AcousticSolve(torch.autograd.Function):
         _raise_on_status(ctx.plan.status(ctx.ws, True))
         ctx.ws = None  # release the snapshot workspace as soon as the adjoint has consumed it
         return ga1, ga2, None, None, None
+
+
+class AcousticL2Solve(torch.autograd.Function):
+    """loss, records, forward wavefields = normalised L2 misfit of the solve's p records against
+    ``obs``; backward = the hand-written adjoint with the misfit's adjoint source formed inside it
+    (no (ns, nt, nr) source array). The misfit is ADFWI/fwi/misfit/L2.py:26-29 on traces divided
+    by their peak (ADFWI/fwi/acoustic_fwi.py:149-150; ``normalise_obs`` divides obs too, else obs
+    is taken as given, already normalised); the records come back without gradient."""
+
+    @staticmethod
+    def forward(ctx, alpha1, alpha2, damp, wavelet, obs, plan, silent_rel, normalise_obs):
+        if plan.nm != 1:
+            raise ValueError("AcousticL2Solve takes a single-model plan")
+        alpha1, alpha2, damp, wavelet = (t.contiguous() for t in (alpha1, alpha2, damp, wavelet))
+        obs = obs.to(dtype=plan.dtype).contiguous()
+        rp, ru, rw, fp, fu, fw, ws = plan.run_forward(alpha1, alpha2, damp, wavelet, True)
+        loss = plan.l2_loss(rp, obs, ws, silent_rel, normalise_obs)[0]
+        ctx.plan, ctx.ws, ctx.norm = plan, ws, normalise_obs
+        ctx.save_for_backward(alpha1, wavelet, rp, obs)
+        ctx.mark_non_differentiable(rp, ru, rw, fp, fu, fw)
+        return loss, rp, ru, rw, fp, fu, fw
+
+    @staticmethod
+    def backward(ctx, gloss, *_):
+        alpha1, wavelet, rp, obs = ctx.saved_tensors
+        if ctx.ws is None:
+            raise RuntimeError("AcousticL2Solve.backward: the snapshots were already used by an earlier backward")
+        if gloss is None:
+            gloss = torch.ones((), dtype=torch.float64, device=alpha1.device)
+        ga1, ga2 = ctx.plan.run_backward_l2(alpha1, wavelet, rp, obs, ctx.ws, gloss, ctx.norm)
+        _raise_on_status(ctx.plan.status(ctx.ws, True))
+        ctx.ws = None
+        return ga1, ga2, None, None, None, None, None, None

@@ -30,6 +30,7 @@
 #include "../../include/adfwi_gb300.h"
 #include "common.cuh"
 #include "frames.cuh"
+#include "l2.cuh"
 #include "snapshot.cuh"
 #include "tma.cuh"
 
@@ -66,7 +67,29 @@ struct Geo {
   const int* cell_rcv;       // receiver indices grouped by unique cell
   const int* grp_beg;        // ngroups+1 offsets: shots of each shot group (a group has one model)
   const int* grp_model;      // model of each shot group
+  // Fused misfit: when fz_tr is set, the dL/d p-records handed to the adjoint are the
+  // normalised L2 misfit's adjoint source, formed from the synthetic records (the p-record
+  // gradient pointer then holds them) and fz_obs with the per-trace factors fz_tr.
+  const T* fz_obs;
+  const l2::TraceFactors<T>* fz_tr;
+  const double* fz_gmul;     // device scale of the source (the objective's gradient w.r.t. the loss)
+  int fz_norm_obs;
 };
+
+// dL/d p-record of shot sh, step t, receiver rid: from the gradient array gp, or formed from the
+// records (gp) and the observed data with the misfit's factors when the misfit is fused.
+// (a call, not inlined: the FP64 source arithmetic stays out of the step kernels' registers)
+template <typename T>
+__device__ __noinline__ T fused_source(const l2::TraceFactors<T>* tr, const T* syn, const T* obs, const double* gmul,
+                                       int norm_obs, int64_t trace, int64_t o, int t) {
+  return l2::source(tr[trace], syn[o], obs[o], t, norm_obs, *gmul);
+}
+template <typename T>
+__device__ __forceinline__ T grad_rec_p(const Geo<T>& g, const T* gp, int sh, int t, int rid) {
+  const int64_t o = ((int64_t)sh * g.nt + t) * g.nr + rid;
+  if (g.fz_tr == nullptr) return gp[o];
+  return fused_source(g.fz_tr, gp, g.fz_obs, g.fz_gmul, g.fz_norm_obs, (int64_t)sh * g.nr + rid, o, t);
+}
 
 // Update regions of acoustic_kernels.py:115, 139, 151.
 template <typename T>
@@ -109,7 +132,7 @@ __global__ void adj_seed(Geo<T> g, int ntiles, int tz, int tx, const T* __restri
     T ap = T(0), au = T(0), aw = T(0);
     for (int m = g.tcell_rbeg[q]; m < g.tcell_rbeg[q + 1]; ++m) {
       int64_t o = rowbase + g.cell_rcv[m];
-      if (gr_p) ap += gr_p[o];
+      if (gr_p) ap += grad_rec_p(g, gr_p, sh, g.nt - 1, g.cell_rcv[m]);
       if (gr_u) au += gr_u[o];
       if (gr_w) aw += gr_w[o];
     }
@@ -237,6 +260,7 @@ namespace {
 struct Carve {
   int64_t coef, fa, fb, ilp, ilu, tab, flag;  // forward
   int64_t snap, snap_scale, hp, hd, la, lb, g1, g2;  // gradient extras
+  int64_t mst, mpk, mnorm, mfac;                     // fused misfit: trace stats, gather peaks, norms, factors
   int64_t total;
 };
 
@@ -267,6 +291,12 @@ Carve carve(const adfwi_acoustic_plan* p, bool grad, int K) {
     c.lb = take(3 * ns * pl);
     c.g1 = take((int64_t)p->t2.ngroups * pl);
     c.g2 = take((int64_t)p->t2.ngroups * pl);
+    const int64_t traces = (int64_t)ns * std::max(1, p->d.nr);
+    const bool f64 = p->elem == 8;
+    c.mst = take(traces * (f64 ? (int64_t)sizeof(l2::TraceStats<double>) : (int64_t)sizeof(l2::TraceStats<float>)));
+    c.mpk = take(2 * ns * 8);
+    c.mnorm = take(traces * 8);
+    c.mfac = take(traces * (f64 ? (int64_t)sizeof(l2::TraceFactors<double>) : (int64_t)sizeof(l2::TraceFactors<float>)));
   }
   c.total = o;
   return c;
@@ -323,6 +353,10 @@ ac::Geo<T> make_geo(const adfwi_acoustic_plan* p, const unsigned char* ws, const
   g.cell_rcv = tb + t.o_cr;
   g.grp_beg = tb + t.o_gb;
   g.grp_model = tb + t.o_gm;
+  g.fz_obs = nullptr;
+  g.fz_tr = nullptr;
+  g.fz_gmul = nullptr;
+  g.fz_norm_obs = 0;
   return g;
 }
 
@@ -542,9 +576,19 @@ int forward_impl(const adfwi_acoustic_plan* p, const void* alpha1, const void* a
   return kOk;
 }
 
+// The normalised L2 misfit fused into the adjoint: the dL/d p-records are formed from the
+// records (passed as the p-record gradient) and the observed data with the factors that
+// l2_loss_impl left in the workspace, scaled by *gmul.
+struct FusedL2 {
+  const void* obs;
+  const double* gmul;
+  int norm_obs;
+};
+
 template <typename T>
 int backward_impl(const adfwi_acoustic_plan* p, const void* wavelet, const void* grp, const void* gru,
-                  const void* grw, void* ga1, void* ga2, unsigned char* ws, int64_t ws_bytes, cudaStream_t st) {
+                  const void* grw, void* ga1, void* ga2, unsigned char* ws, int64_t ws_bytes, cudaStream_t st,
+                  const FusedL2* fz = nullptr) {
   int rc = set_smem_limits<T>();
   if (rc) return rc;
   const int K = p->K;
@@ -554,6 +598,12 @@ int backward_impl(const adfwi_acoustic_plan* p, const void* wavelet, const void*
     return kWorkspaceTooSmall;
   }
   ac::Geo<T> g2 = make_geo<T>(p, ws, c, p->t2);
+  if (fz != nullptr) {
+    g2.fz_obs = static_cast<const T*>(fz->obs);
+    g2.fz_tr = reinterpret_cast<const l2::TraceFactors<T>*>(ws + c.mfac);
+    g2.fz_gmul = fz->gmul;
+    g2.fz_norm_obs = fz->norm_obs;
+  }
   const int64_t pl = p->L.plane;
   const int64_t ns = p->d.ns;
   const int nt = p->d.nt;
@@ -625,6 +675,38 @@ int backward_impl(const adfwi_acoustic_plan* p, const void* wavelet, const void*
                                 p->L, ng, 0, 0, p->nzp, p->nxp, g1p + (int64_t)g0 * pl, static_cast<T*>(ga1) + m * n)));
     ADFWI_LAUNCH(kAux, st, (ac::reduce_planes<T><<<grid_blocks(n), 256, 0, st>>>(
                                 p->L, ng, 0, 0, p->nzp, p->nxp, g2p + (int64_t)g0 * pl, static_cast<T*>(ga2) + m * n)));
+  }
+  ADFWI_CUDA_TRY(cudaGetLastError());
+  return kOk;
+}
+
+// Normalised L2 misfit of the records `syn` against `obs` (the misfit of adfwi_l2_misfit) into
+// the gradient workspace's factor arrays, and each model's loss: the sum of its traces' norms.
+template <typename T>
+int l2_loss_impl(const adfwi_acoustic_plan* p, const void* syn, const void* obs, double silent_rel, int flags,
+                 double* loss, unsigned char* ws, int64_t ws_bytes, cudaStream_t st) {
+  const Carve c = carve(p, true, p->K);
+  if (ws_bytes < c.total) {
+    set_error("workspace too small: %lld bytes given, %lld needed", (long long)ws_bytes, (long long)c.total);
+    return kWorkspaceTooSmall;
+  }
+  const int ns = p->d.ns, nt = p->d.nt, nr = p->d.nr;
+  auto* stats = reinterpret_cast<l2::TraceStats<T>*>(ws + c.mst);
+  auto* gsyn = reinterpret_cast<l2::PeakWord<T>*>(ws + c.mpk);
+  auto* gobs = gsyn + ns;
+  auto* norms = reinterpret_cast<double*>(ws + c.mnorm);
+  auto* fac = reinterpret_cast<l2::TraceFactors<T>*>(ws + c.mfac);
+  ADFWI_CUDA_TRY(cudaMemsetAsync(ws + c.mpk, 0, 2 * (size_t)ns * 8, st));  // peaks start at +0
+  const dim3 grid((unsigned)((nr + l2::kThreads - 1) / l2::kThreads), (unsigned)ns);
+  const T* sy = static_cast<const T*>(syn);
+  const T* ob = static_cast<const T*>(obs);
+  ADFWI_LAUNCH(kAux, st, (l2::peaks<T><<<grid, l2::kThreads, 0, st>>>(ns, nt, nr, sy, ob, stats, gsyn, gobs)));
+  ADFWI_LAUNCH(kAux, st, (l2::factors<T><<<grid, l2::kThreads, 0, st>>>(ns, nt, nr, p->d.dt, silent_rel, flags & 1, sy,
+                                                                          ob, stats, gsyn, gobs, fac, norms)));
+  for (int m = 0; m < p->nm; ++m) {
+    const int s0 = p->model_shot_beg[m], s1 = p->model_shot_beg[m + 1];
+    ADFWI_LAUNCH(kAux, st, (l2::sum_norms<<<1, l2::kThreads, 0, st>>>((int64_t)(s1 - s0) * nr,
+                                                                       norms + (int64_t)s0 * nr, loss + m)));
   }
   ADFWI_CUDA_TRY(cudaGetLastError());
   return kOk;
@@ -1026,6 +1108,34 @@ int adfwi_acoustic_backward(const adfwi_acoustic_plan* p, const void* alpha1, co
                                  workspace_bytes, st);
   return backward_impl<float>(p, wavelet, grad_rec_p, grad_rec_u, grad_rec_w, grad_alpha1, grad_alpha2, ws,
                               workspace_bytes, st);
+}
+
+int adfwi_acoustic_l2_loss(const adfwi_acoustic_plan* p, const void* syn, const void* obs, double silent_rel,
+                           int32_t flags, double* loss, void* workspace, int64_t workspace_bytes, void* stream) {
+  ADFWI_CHECK_ARG(p && syn && obs && loss && workspace, "null argument");
+  ADFWI_CHECK_ARG(p->d.nr > 0, "the plan has no receivers");
+  ADFWI_CHECK_ARG(silent_rel >= 0.0, "silent_rel must be non-negative");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  unsigned char* ws = static_cast<unsigned char*>(workspace);
+  if (p->d.dtype == ADFWI_F64)
+    return l2_loss_impl<double>(p, syn, obs, silent_rel, flags, loss, ws, workspace_bytes, st);
+  return l2_loss_impl<float>(p, syn, obs, silent_rel, flags, loss, ws, workspace_bytes, st);
+}
+
+int adfwi_acoustic_backward_l2(const adfwi_acoustic_plan* p, const void* wavelet, const void* syn, const void* obs,
+                               int32_t flags, const double* grad_scale, void* grad_alpha1, void* grad_alpha2,
+                               void* workspace, int64_t workspace_bytes, void* stream) {
+  ADFWI_CHECK_ARG(p && wavelet && syn && obs && grad_scale && grad_alpha1 && grad_alpha2 && workspace,
+                  "null argument");
+  ADFWI_CHECK_ARG(p->d.nr > 0, "the plan has no receivers");
+  const FusedL2 fz{obs, grad_scale, flags & 1};
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  unsigned char* ws = static_cast<unsigned char*>(workspace);
+  if (p->d.dtype == ADFWI_F64)
+    return backward_impl<double>(p, wavelet, syn, nullptr, nullptr, grad_alpha1, grad_alpha2, ws, workspace_bytes, st,
+                                 &fz);
+  return backward_impl<float>(p, wavelet, syn, nullptr, nullptr, grad_alpha1, grad_alpha2, ws, workspace_bytes, st,
+                              &fz);
 }
 
 }  // extern "C"

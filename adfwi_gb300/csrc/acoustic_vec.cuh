@@ -539,13 +539,13 @@ __global__ void __launch_bounds__(VTHREADS, VAMINB)
               }
             },
             [&](int tile, int sh) {
-              const int64_t rowbase = ((int64_t)sh * g.nt + (a.it - 1)) * g.nr, so = (int64_t)sh * L.plane;
+              const int64_t so = (int64_t)sh * L.plane;
               if (!walk) {
                 T v[2], o[2];
 #pragma unroll
                 for (int m = 0; m < 2; ++m)
                   if (m < cn) {
-                    v[m] = a.rec_p[rowbase + rid[m]];
+                    v[m] = ac::grad_rec_p(g, a.rec_p, sh, a.it - 1, rid[m]);
                     o[m] = a.o0[so + coff[m]];
                   }
 #pragma unroll
@@ -559,7 +559,8 @@ __global__ void __launch_bounds__(VTHREADS, VAMINB)
                 for (int q = cb + lane - 1; q < ce; q += 31) {
                   const int cell = g.tcell_cell[q];
                   T ap = T(0);
-                  for (int mm = g.tcell_rbeg[q]; mm < g.tcell_rbeg[q + 1]; ++mm) ap += a.rec_p[rowbase + g.cell_rcv[mm]];
+                  for (int mm = g.tcell_rbeg[q]; mm < g.tcell_rbeg[q + 1]; ++mm)
+                    ap += ac::grad_rec_p(g, a.rec_p, sh, a.it - 1, g.cell_rcv[mm]);
                   T* o = a.o0 + so + L.off(i0 + (cell >> 16), j0 + (cell & 0xffff));
                   *o = *o + ap;
                 }
@@ -809,7 +810,7 @@ __global__ void __launch_bounds__(VTHREADS, VAMINB)
             T ap = T(0), au = T(0), aw = T(0);
             for (int mm = g.tcell_rbeg[q]; mm < g.tcell_rbeg[q + 1]; ++mm) {
               const int64_t o = rowbase + g.cell_rcv[mm];
-              if (a.rec_p) ap += a.rec_p[o];
+              if (a.rec_p) ap += ac::grad_rec_p(g, a.rec_p, sh, a.it - 1, g.cell_rcv[mm]);
               if (a.rec_u) au += a.rec_u[o];
               if (a.rec_w) aw += a.rec_w[o];
             }

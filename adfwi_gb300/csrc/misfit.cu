@@ -8,18 +8,10 @@
 // each and write the adjoint source once; every sum over time and over traces is FP64 in a
 // fixed order, so the loss and the adjoint source are deterministic.
 //
-// Records are (ns, nt, nr) row-major: one thread owns one trace (s, r) and walks its nt
-// samples with stride nr, so a warp reads 32 consecutive receivers per sample (coalesced).
-//
-//   peaks:    per trace max |syn| (its first arg-max and sign) and max |obs|; per shot the
-//             peak of both gathers (atomicMax on the bit patterns of non-negative floats:
-//             exact and order-independent);
-//   adjoint:  per trace, silent traces (peak <= silent_rel x the gather's peak; the reference
-//             uses silent_rel = 0) are zero; S2 = sum_t rsd^2, S3 = sum_t rsd * syn with
-//             rsd = obs/m_obs - syn/m_syn in the data type (as the reference rounds it) and the
-//             sums in FP64; n = sqrt(S2 dt); dL/dsyn_t = -rsd_t dt / (n m_syn), plus the max's
-//             share dt S3 / (n m_syn^2) sign at the arg-max sample; n goes to a per-trace array;
-//   loss:     one block sums the per-trace norms in a fixed order.
+// The per-trace statistics, factors and adjoint-source sample are in l2.cuh (shared with the
+// acoustic adjoint step, which forms the pressure records' adjoint source on the fly); here
+// three kernels read the records a few times each and write the adjoint source once, and one
+// block sums the per-trace norms in a fixed order.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -27,56 +19,12 @@
 
 #include "../../include/adfwi_gb300.h"
 #include "common.cuh"
+#include "l2.cuh"
 
 namespace adfwi {
 namespace mf {
 
-constexpr int kThreads = 256;
-
-template <typename T>
-struct TraceStats {
-  T m_syn;     // max |syn|
-  int arg;     // first sample where |syn| = m_syn
-  int neg;     // syn[arg] < 0
-  T m_obs;     // max |obs|
-};
-
-__device__ __forceinline__ void atomic_max_nonneg(unsigned* addr, float v) { atomicMax(addr, __float_as_uint(v)); }
-__device__ __forceinline__ void atomic_max_nonneg(unsigned long long* addr, double v) {
-  atomicMax(addr, (unsigned long long)__double_as_longlong(v));
-}
-__device__ __forceinline__ float peak_value(const unsigned* p) { return __uint_as_float(*p); }
-__device__ __forceinline__ double peak_value(const unsigned long long* p) { return __longlong_as_double((long long)*p); }
-
-template <typename T>
-using PeakWord = typename std::conditional<sizeof(T) == 8, unsigned long long, unsigned>::type;
-
-template <typename T>
-__global__ void __launch_bounds__(kThreads) peaks(int ns, int nt, int nr, const T* __restrict__ syn,
-                                                  const T* __restrict__ obs, TraceStats<T>* __restrict__ st,
-                                                  PeakWord<T>* __restrict__ gsyn, PeakWord<T>* __restrict__ gobs) {
-  const int r = blockIdx.x * blockDim.x + threadIdx.x, s = blockIdx.y;
-  if (r >= nr) return;
-  const T* ps = syn + (int64_t)s * nt * nr + r;
-  const T* po = obs + (int64_t)s * nt * nr + r;
-  T ms = T(0), mo = T(0);
-  int arg = 0, neg = 0;
-  for (int t = 0; t < nt; ++t) {
-    const T v = ps[(int64_t)t * nr];
-    const T a = v < T(0) ? -v : v;
-    if (a > ms) {
-      ms = a;
-      arg = t;
-      neg = v < T(0);
-    }
-    const T o = po[(int64_t)t * nr];
-    const T ao = o < T(0) ? -o : o;
-    mo = ao > mo ? ao : mo;
-  }
-  st[(int64_t)s * nr + r] = TraceStats<T>{ms, arg, neg, mo};
-  atomic_max_nonneg(gsyn + s, ms);
-  atomic_max_nonneg(gobs + s, mo);
-}
+using namespace l2;
 
 template <typename T>
 __global__ void __launch_bounds__(kThreads) adjoint(int ns, int nt, int nr, double dt, double silent_rel,
@@ -87,53 +35,15 @@ __global__ void __launch_bounds__(kThreads) adjoint(int ns, int nt, int nr, doub
                                                     double* __restrict__ norms) {
   const int r = blockIdx.x * blockDim.x + threadIdx.x, s = blockIdx.y;
   if (r >= nr) return;
-  const TraceStats<T> q = st[(int64_t)s * nr + r];
-  const bool live = q.m_syn > T(0) && (double)q.m_syn > silent_rel * (double)peak_value(gsyn + s);
-  const bool olive = !normalise_obs || (q.m_obs > T(0) && (double)q.m_obs > silent_rel * (double)peak_value(gobs + s));
+  const int64_t tr = (int64_t)s * nr + r;
   const T* ps = syn + (int64_t)s * nt * nr + r;
   const T* po = obs + (int64_t)s * nt * nr + r;
+  double n;
+  const TraceFactors<T> f = trace_factors(st[tr], (double)peak_value(gsyn + s), (double)peak_value(gobs + s), ps, po,
+                                          nt, nr, dt, silent_rel, normalise_obs, &n);
+  norms[tr] = n;
   T* pa = adj + (int64_t)s * nt * nr + r;
-  double s2 = 0.0, s3 = 0.0;
-  for (int t = 0; t < nt; ++t) {
-    const T v = ps[(int64_t)t * nr];
-    const T o = po[(int64_t)t * nr];
-    const T on = !normalise_obs ? o : (olive ? o / q.m_obs : T(0));
-    const T sn = live ? v / q.m_syn : T(0);
-    const double d = (double)(on - sn);
-    s2 += d * d;
-    s3 += d * (double)v;
-  }
-  const double n = sqrt(s2 * dt);
-  norms[(int64_t)s * nr + r] = n;
-  const bool grad = live && n > 0.0;
-  const double scale = grad ? -dt / (n * (double)q.m_syn) : 0.0;
-  const double corr = grad ? dt * s3 / (n * (double)q.m_syn * (double)q.m_syn) * (q.neg ? -1.0 : 1.0) : 0.0;
-  for (int t = 0; t < nt; ++t) {
-    double g = 0.0;
-    if (grad) {
-      const T v = ps[(int64_t)t * nr];
-      const T o = po[(int64_t)t * nr];
-      const T on = !normalise_obs ? o : (olive ? o / q.m_obs : T(0));
-      const T sn = v / q.m_syn;
-      g = (double)(on - sn) * scale;
-      if (t == q.arg) g += corr;
-    }
-    pa[(int64_t)t * nr] = (T)g;
-  }
-}
-
-__global__ void __launch_bounds__(kThreads) sum_norms(int64_t n, const double* __restrict__ norms,
-                                                      double* __restrict__ loss) {
-  __shared__ double part[kThreads];
-  double acc = 0.0;
-  for (int64_t e = threadIdx.x; e < n; e += kThreads) acc += norms[e];
-  part[threadIdx.x] = acc;
-  __syncthreads();
-  for (int w = kThreads / 2; w > 0; w >>= 1) {
-    if (threadIdx.x < w) part[threadIdx.x] += part[threadIdx.x + w];
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) *loss = part[0];
+  for (int t = 0; t < nt; ++t) pa[(int64_t)t * nr] = source(f, ps[(int64_t)t * nr], po[(int64_t)t * nr], t, normalise_obs);
 }
 
 int64_t align256(int64_t x) { return (x + 255) / 256 * 256; }

@@ -45,7 +45,6 @@ import torch
 
 from .acoustic import AcousticPlan
 from .boundary import bc_pml
-from .misfit import l2_misfit_and_adjoint
 from .utils import wavelet as _wavelet
 
 _ALIGN = 256
@@ -357,8 +356,8 @@ class _Batch(object):
         rec = self.ns * self.nt * self.nr * 4
         grid = self.nm * self.nzp * self.nxp * 4
         model = self.nm * self.nz * self.nx * 4
-        self.nbytes = (_aligned(self.ws_bytes) + 3 * _aligned(rec) + (2 * _aligned(rec) if self.grad else 0)
-                       + 3 * _aligned(grid) + 5 * _aligned(model) + _aligned(self.ns * self.nt * 4))
+        self.nbytes = (_aligned(self.ws_bytes) + 3 * _aligned(rec) + (_aligned(rec) if self.grad else 0)
+                       + 3 * _aligned(grid) + 5 * _aligned(model) + _aligned(self.ns * self.nt * 4) + 2 * _ALIGN)
         self.cells = [n * self.nzp * self.nxp * self.nt for n in self.ns_r]
         self.off = self.n = None
         self.bound = False
@@ -379,9 +378,10 @@ class _Batch(object):
         self.rho_d = cv.take(mshp, torch.float32)
         self.wav = cv.take((self.ns, self.nt), torch.float32)
         self.dx_t = torch.full((), self.dx, dtype=torch.float32, device=device)  # divisor of alpha1
+        self.one = cv.take((1,), torch.float64)  # scale of the misfit's adjoint source
+        self.one.fill_(1.0)
         if self.grad:
             self.obs = cv.take(shp, torch.float32)
-            self.adj = cv.take(shp, torch.float32)
         _, w = _wavelet(self.nt, self.dt, self.f0)
         self.wav.copy_(torch.from_numpy(np.ascontiguousarray(np.tile(w, (self.ns, 1)), dtype=np.float32)))
         self.bound = True
@@ -413,13 +413,11 @@ class _Batch(object):
                               fw=self.fw, stream=h)
         if not self.grad:
             return
-        self.out_loss = []
-        for s0, s1 in self.ranges:  # each request's misfit over its own traces
-            loss, _ = l2_misfit_and_adjoint(self.recs[0][s0:s1], self.obs[s0:s1], self.dt, silent_rel=self.silent_rel,
-                                            stream=h, adj=self.adj[s0:s1])
-            self.out_loss.append(loss)
-        ga1, _ = self.plan.run_backward(self.a1, self.a2, self.damp, self.wav, (self.adj, None, None), self.ws,
-                                        stream=h)
+        # each request's misfit over its own traces; the adjoint forms their sources as it
+        # injects them (no (ns, nt, nr) source array)
+        self.out_loss = self.plan.l2_loss(self.recs[0], self.obs, self.ws, self.silent_rel, True, stream=h)
+        ga1, _ = self.plan.run_backward_l2(self.a1, self.wav, self.recs[0], self.obs, self.ws, self.one, True,
+                                           stream=h)
         # alpha1 = ((den c) c) dt / dx; alpha2 and rho do not depend on vp
         g_t2 = ga1 * (self.dt / self.dx)
         self.out_grad = [fold_replicate_pad(g_t2[m] * t1[m] + g_t2[m] * c[m] * den[m], nb) for m in range(self.nm)]
@@ -455,7 +453,7 @@ class _Batch(object):
             if not self.grad:
                 rec = self.recs[0].cpu().numpy()
                 return [(None, None, rec[s0:s1]) for s0, s1 in self.ranges]
-            losses = torch.stack(self.out_loss).cpu().numpy()
+            losses = self.out_loss.cpu().numpy()
             grads = torch.stack(self.out_grad).cpu().numpy()
             return [(float(losses[m]), grads[m], None) for m in range(self.nm)]
 

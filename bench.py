@@ -5,7 +5,8 @@ Workload (one "step"): one full-waveform-inversion gradient evaluation on the 20
 layered/faulted iso-acoustic model (dx = 20 m, PML 50 -> 300 x 700 padded cells), 30 surface
 shots, 600 receivers, nt = 3000, dt = 1.5 ms, 8 Hz Ricker, FP32: forward solve on the smoothed
 starting model, per-trace normalisation and the L2 misfit against data observed on the true
-model, then the hand-written checkpointed adjoint back to dL/dvp. Inputs are seeded synthetic
+model (the misfit fused into the adjoint's receiver injection), then the hand-written
+checkpointed adjoint back to dL/dvp. Inputs are seeded synthetic
 stand-ins with those shapes and distributions (no public dataset).
 
 Metric: Gcell-updates/s = shots * nzp * nxp * nt / time per gradient step.
@@ -162,18 +163,9 @@ def max_over_ranks(x, world, device):
     return float(t.item())
 
 
-def l2_misfit(syn, obs, dt):
-    """Misfit_waveform_L2 (ADFWI/fwi/misfit/L2.py:26-29) on max-normalised traces
-    (ADFWI/fwi/acoustic_fwi.py:149-150): sum over traces of sqrt(sum_t r^2 dt)."""
-    syn = syn / torch.max(torch.abs(syn), dim=1, keepdim=True).values
-    rsd = obs - syn
-    return torch.sum(torch.sqrt(torch.sum(rsd * rsd * dt, dim=1)))
-
-
 def gpu_arm(args, world, rank, local):
     import adfwi_gb300 as A
     from adfwi_gb300 import _native as N
-    from adfwi_gb300.misfit import l2_misfit as cuda_l2_misfit
     from adfwi_gb300.synthetic import acoustic_gradient_case
 
     dev = torch.device("cuda", local)
@@ -194,10 +186,9 @@ def gpu_arm(args, world, rank, local):
     def step(obs_dev):
         model.vp.data.copy_(vp0)
         model.vp.grad = None
-        rec = prop.forward()
-        # normalised L2 (the CUDA misfit: trace peaks, FP64 sums and the adjoint source in one
-        # pass set; obs is normalised once at setup, as acoustic_fwi.py does)
-        loss = cuda_l2_misfit(rec["p"], obs_dev, dt, silent_rel=0.0, normalise_obs=False)
+        # forward solve + normalised L2 misfit (obs normalised once at setup, as acoustic_fwi.py
+        # does), then the adjoint with the misfit's adjoint source formed inside it
+        loss, _ = prop.forward_l2(obs_dev)
         loss.backward()
         return loss
 
@@ -320,7 +311,6 @@ def fp64_error(args, dev, memory_fraction):
     """Error of the headline FP32 gradient (and records, loss) against an FP64 run of the same
     scheme on the same inputs (untimed): the 200 x 600 workload in both precisions."""
     import adfwi_gb300 as A
-    from adfwi_gb300.misfit import l2_misfit as cuda_l2_misfit
     from adfwi_gb300.synthetic import acoustic_gradient_case
     res = {}
     for dtype in (torch.float64, torch.float32):
@@ -333,8 +323,7 @@ def fp64_error(args, dev, memory_fraction):
             obs = prop.forward()["p"]
             obs = (obs / torch.max(torch.abs(obs), dim=1, keepdim=True).values).contiguous()
         model.vp.data.copy_(torch.as_tensor(vp_init, device=dev))
-        rec = prop.forward()
-        loss = cuda_l2_misfit(rec["p"], obs, prop.dt, silent_rel=0.0, normalise_obs=False)
+        loss, rec = prop.forward_l2(obs)
         loss.backward()
         res[dtype] = (rec["p"].detach().double(), model.vp.grad.detach().double(), float(loss),
                       prop.plan()[1].snapshot_every)

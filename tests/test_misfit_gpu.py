@@ -57,3 +57,46 @@ def test_fused_misfit_is_deterministic():
     a = l2_misfit_and_adjoint(syn, obs, 1e-3)
     b = l2_misfit_and_adjoint(syn, obs, 1e-3)
     assert float(a[0]) == float(b[0]) and torch.equal(a[1], b[1])
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
+@pytest.mark.parametrize("silent_rel,normalise_obs", [(0.0, False), (1e-3, True)])
+@pytest.mark.parametrize("snapshot_every", [0, 31])
+def test_misfit_fused_into_the_adjoint_equals_the_two_pass_gradient(dtype, silent_rel, normalise_obs,
+                                                                    snapshot_every):
+    """The adjoint with the misfit's source formed as it is injected (adfwi_acoustic_l2_loss +
+    adfwi_acoustic_backward_l2) gives the same loss and the same coefficient gradients, bit for
+    bit, as the two-pass form: adfwi_l2_misfit writing the (ns, nt, nr) source, then
+    adfwi_acoustic_backward reading it."""
+    import adfwi_gb300 as A
+    from _cases import acoustic_problem
+    model, survey, prop = acoustic_problem(A, dtype=dtype, ns=3, nt=200, seed=8, free_surface=True,
+                                           snapshot_every=snapshot_every)
+    model.forward()
+    a1, a2 = (t.detach().contiguous() for t in prop.coefficients(model))
+    _, plan = prop.plan()
+    damp, wav = prop.damp.contiguous(), prop.wavelet.contiguous()
+    g = torch.Generator().manual_seed(2)
+    obs = (torch.randn((plan.ns, plan.nt, plan.nr), generator=g, dtype=dtype) * 1e-3).cuda()
+    # two-pass
+    rp, _, _, _, _, _, ws = plan.run_forward(a1, a2, damp, wav, True)
+    loss0, adj = l2_misfit_and_adjoint(rp, obs, plan_dt(prop), silent_rel=silent_rel, normalise_obs=normalise_obs)
+    g1, g2 = plan.run_backward(a1, a2, damp, wav, (adj, None, None), ws)
+    # fused
+    rpf, _, _, _, _, _, wsf = plan.run_forward(a1, a2, damp, wav, True)
+    loss1 = plan.l2_loss(rpf, obs, wsf, silent_rel, normalise_obs)
+    one = torch.ones(1, dtype=torch.float64, device="cuda")
+    f1, f2 = plan.run_backward_l2(a1, wav, rpf, obs, wsf, one, normalise_obs)
+    assert plan.status(wsf, True) == 0
+    assert torch.equal(rp, rpf)
+    assert float(loss0) == float(loss1[0])
+    assert torch.equal(g1, f1) and torch.equal(g2, f2)
+    # the scale of the source scales the gradient
+    rpf, _, _, _, _, _, wsf = plan.run_forward(a1, a2, damp, wav, True)
+    plan.l2_loss(rpf, obs, wsf, silent_rel, normalise_obs)
+    h1, _ = plan.run_backward_l2(a1, wav, rpf, obs, wsf, 2.0 * one, normalise_obs)
+    assert float((h1 - 2.0 * f1).norm() / (2.0 * f1).norm()) <= (1e-6 if dtype == torch.float32 else 1e-14)
+
+
+def plan_dt(prop):
+    return prop.dt

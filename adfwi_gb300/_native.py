@@ -62,6 +62,7 @@ def _bind(lib):
         "adfwi_acoustic_backward": (c_int32, [P, P, P, P, P, P, P, P, P, P, P, c_int64, P]),
         "adfwi_acoustic_status": (c_int32, [P, P, c_int64, c_int32, ctypes.POINTER(c_int32), P]),
         "adfwi_acoustic_l2_loss": (c_int32, [P, P, P, ctypes.c_double, c_int32, P, P, c_int64, P]),
+        "adfwi_acoustic_l2_sources": (c_int32, [P, P, P, c_int32, P, P, P, c_int64, P]),
         "adfwi_acoustic_backward_l2": (c_int32, [P, P, P, P, c_int32, P, P, P, P, c_int64, P]),
         "adfwi_acoustic_noalloc_status": (c_int32, [P, ctypes.POINTER(c_int32), P]),
         "adfwi_last_error": (c_int32, [ctypes.c_char_p, ctypes.c_size_t]),

@@ -156,7 +156,7 @@ class AcousticPlan(object):
     def l2_loss(self, syn, obs, workspace, silent_rel=0.0, normalise_obs=False, stream=None):
         """Normalised L2 misfit of the forward's p records ``syn`` against ``obs`` (ns, nt, nr): each
         model's loss as FP64 device values (nmodels,); keeps the per-trace factors in the gradient
-        ``workspace`` for run_backward_l2."""
+        ``workspace`` for l2_sources or run_backward_l2."""
         shp = (self.ns, self.nt, self.nr)
         self._check(syn, shp, "syn")
         obs = obs.to(dtype=self.dtype).contiguous()
@@ -167,6 +167,21 @@ class AcousticPlan(object):
                                                 int(bool(normalise_obs)), N.ptr(loss), N.ptr(workspace),
                                                 workspace.numel(), st), "adfwi_acoustic_l2_loss")
         return loss
+
+    def l2_sources(self, syn, obs, workspace, grad_scale, normalise_obs=False, adj=None, stream=None):
+        """The adjoint source of l2_loss's misfit times ``grad_scale`` (a one-element FP64 device
+        tensor) as an (ns, nt, nr) array (``adj`` may name the output buffer), for run_backward's
+        p-record gradient."""
+        obs = obs.to(dtype=self.dtype).contiguous()
+        gs = grad_scale.to(dtype=torch.float64).reshape(1).contiguous()
+        if adj is None:
+            adj = torch.empty_like(syn)
+        self._check(adj, (self.ns, self.nt, self.nr), "adj")
+        st = ctypes.c_void_p(stream) if stream is not None else N.stream_handle(syn.device)
+        N.check(self.lib.adfwi_acoustic_l2_sources(self.handle, N.ptr(syn), N.ptr(obs), int(bool(normalise_obs)),
+                                                   N.ptr(gs), N.ptr(adj), N.ptr(workspace), workspace.numel(), st),
+                "adfwi_acoustic_l2_sources")
+        return adj
 
     def run_backward_l2(self, alpha1, wavelet, syn, obs, workspace, grad_scale, normalise_obs=False, stream=None):
         """Adjoint solve whose p-record source is the misfit of l2_loss (formed as it is injected)
@@ -244,34 +259,50 @@ class AcousticSolve(torch.autograd.Function):
         return ga1, ga2, None, None, None
 
 
+ADJOINT_SOURCES = ("array", "inject")
+
+
 class AcousticL2Solve(torch.autograd.Function):
     """loss, records, forward wavefields = normalised L2 misfit of the solve's p records against
-    ``obs``; backward = the hand-written adjoint with the misfit's adjoint source formed inside it
-    (no (ns, nt, nr) source array). The misfit is ADFWI/fwi/misfit/L2.py:26-29 on traces divided
-    by their peak (ADFWI/fwi/acoustic_fwi.py:149-150; ``normalise_obs`` divides obs too, else obs
-    is taken as given, already normalised); the records come back without gradient."""
+    ``obs``; backward = the hand-written adjoint driven by the misfit's adjoint source. The misfit
+    is ADFWI/fwi/misfit/L2.py:26-29 on traces divided by their peak
+    (ADFWI/fwi/acoustic_fwi.py:149-150; ``normalise_obs`` divides obs too, else obs is taken as
+    given, already normalised); the records come back without gradient.
+
+    ``adjoint_source``: "array" writes the source as an (ns, nt, nr) array in one
+    bandwidth-bound pass that the adjoint reads (the faster form on GB300); "inject" forms each
+    sample inside the adjoint step as it is injected, with no array (the lanes that inject the
+    receivers then pace their tiles: about 10-15% more time per adjoint step on the 300 x 700,
+    30-shot workload). Both give the same bits."""
 
     @staticmethod
-    def forward(ctx, alpha1, alpha2, damp, wavelet, obs, plan, silent_rel, normalise_obs):
+    def forward(ctx, alpha1, alpha2, damp, wavelet, obs, plan, silent_rel, normalise_obs, adjoint_source="array"):
+        if adjoint_source not in ADJOINT_SOURCES:
+            raise ValueError("adjoint_source must be one of %s, got %r" % (ADJOINT_SOURCES, adjoint_source))
         if plan.nm != 1:
             raise ValueError("AcousticL2Solve takes a single-model plan")
         alpha1, alpha2, damp, wavelet = (t.contiguous() for t in (alpha1, alpha2, damp, wavelet))
         obs = obs.to(dtype=plan.dtype).contiguous()
         rp, ru, rw, fp, fu, fw, ws = plan.run_forward(alpha1, alpha2, damp, wavelet, True)
         loss = plan.l2_loss(rp, obs, ws, silent_rel, normalise_obs)[0]
-        ctx.plan, ctx.ws, ctx.norm = plan, ws, normalise_obs
-        ctx.save_for_backward(alpha1, wavelet, rp, obs)
+        ctx.plan, ctx.ws, ctx.norm, ctx.source = plan, ws, normalise_obs, adjoint_source
+        ctx.save_for_backward(alpha1, alpha2, damp, wavelet, rp, obs)
         ctx.mark_non_differentiable(rp, ru, rw, fp, fu, fw)
         return loss, rp, ru, rw, fp, fu, fw
 
     @staticmethod
     def backward(ctx, gloss, *_):
-        alpha1, wavelet, rp, obs = ctx.saved_tensors
+        alpha1, alpha2, damp, wavelet, rp, obs = ctx.saved_tensors
         if ctx.ws is None:
             raise RuntimeError("AcousticL2Solve.backward: the snapshots were already used by an earlier backward")
         if gloss is None:
             gloss = torch.ones((), dtype=torch.float64, device=alpha1.device)
-        ga1, ga2 = ctx.plan.run_backward_l2(alpha1, wavelet, rp, obs, ctx.ws, gloss, ctx.norm)
+        if ctx.source == "array":
+            adj = ctx.plan.l2_sources(rp, obs, ctx.ws, gloss, ctx.norm)
+            ga1, ga2 = ctx.plan.run_backward(alpha1, alpha2, damp, wavelet, (adj, None, None), ctx.ws)
+            del adj
+        else:
+            ga1, ga2 = ctx.plan.run_backward_l2(alpha1, wavelet, rp, obs, ctx.ws, gloss, ctx.norm)
         _raise_on_status(ctx.plan.status(ctx.ws, True))
         ctx.ws = None
-        return ga1, ga2, None, None, None, None, None, None
+        return ga1, ga2, None, None, None, None, None, None, None

@@ -77,18 +77,38 @@ struct Geo {
 };
 
 // dL/d p-record of shot sh, step t, receiver rid: from the gradient array gp, or formed from the
-// records (gp) and the observed data with the misfit's factors when the misfit is fused.
-// (a call, not inlined: the FP64 source arithmetic stays out of the step kernels' registers)
+// records (gp) and the observed data with the misfit's factors when the misfit is fused. In two
+// parts, the loads (RecPIn) and the value from them, so that a caller handling several
+// receivers issues every load before the arithmetic (the IEEE divisions of the source have an
+// out-of-line slow path, across which later loads are not hoisted).
+// (gmul: the source's scale, read once by the caller with fused_scale)
 template <typename T>
-__device__ __noinline__ T fused_source(const l2::TraceFactors<T>* tr, const T* syn, const T* obs, const double* gmul,
-                                       int norm_obs, int64_t trace, int64_t o, int t) {
-  return l2::source(tr[trace], syn[o], obs[o], t, norm_obs, *gmul);
+struct RecPIn {
+  T v, o;
+  l2::TraceFactors<T> f;
+};
+template <typename T>
+__device__ __forceinline__ RecPIn<T> grad_rec_p_load(const Geo<T>& g, const T* gp, int sh, int t, int rid) {
+  RecPIn<T> r;
+  const int64_t o = ((int64_t)sh * g.nt + t) * g.nr + rid;
+  r.v = gp[o];
+  if (g.fz_tr != nullptr) {
+    r.o = g.fz_obs[o];
+    r.f = g.fz_tr[(int64_t)sh * g.nr + rid];
+  }
+  return r;
 }
 template <typename T>
-__device__ __forceinline__ T grad_rec_p(const Geo<T>& g, const T* gp, int sh, int t, int rid) {
-  const int64_t o = ((int64_t)sh * g.nt + t) * g.nr + rid;
-  if (g.fz_tr == nullptr) return gp[o];
-  return fused_source(g.fz_tr, gp, g.fz_obs, g.fz_gmul, g.fz_norm_obs, (int64_t)sh * g.nr + rid, o, t);
+__device__ __forceinline__ T grad_rec_p_value(const Geo<T>& g, const RecPIn<T>& r, int t, T gmul) {
+  return g.fz_tr == nullptr ? r.v : l2::source(r.f, r.v, r.o, t, g.fz_norm_obs, gmul);
+}
+template <typename T>
+__device__ __forceinline__ T grad_rec_p(const Geo<T>& g, const T* gp, int sh, int t, int rid, T gmul) {
+  return grad_rec_p_value(g, grad_rec_p_load(g, gp, sh, t, rid), t, gmul);
+}
+template <typename T>
+__device__ __forceinline__ T fused_scale(const Geo<T>& g) {
+  return g.fz_gmul != nullptr ? (T)*g.fz_gmul : T(1);
 }
 
 // Update regions of acoustic_kernels.py:115, 139, 151.
@@ -130,9 +150,10 @@ __global__ void adj_seed(Geo<T> g, int ntiles, int tz, int tx, const T* __restri
     int i = g.zbeg + (tile / g.tiles_x) * tz + (cell >> 16);
     int j = (tile % g.tiles_x) * tx + (cell & 0xffff);
     T ap = T(0), au = T(0), aw = T(0);
+    const T gmul = fused_scale(g);
     for (int m = g.tcell_rbeg[q]; m < g.tcell_rbeg[q + 1]; ++m) {
       int64_t o = rowbase + g.cell_rcv[m];
-      if (gr_p) ap += grad_rec_p(g, gr_p, sh, g.nt - 1, g.cell_rcv[m]);
+      if (gr_p) ap += grad_rec_p(g, gr_p, sh, g.nt - 1, g.cell_rcv[m], gmul);
       if (gr_u) au += gr_u[o];
       if (gr_w) aw += gr_w[o];
     }
@@ -697,17 +718,36 @@ int l2_loss_impl(const adfwi_acoustic_plan* p, const void* syn, const void* obs,
   auto* norms = reinterpret_cast<double*>(ws + c.mnorm);
   auto* fac = reinterpret_cast<l2::TraceFactors<T>*>(ws + c.mfac);
   ADFWI_CUDA_TRY(cudaMemsetAsync(ws + c.mpk, 0, 2 * (size_t)ns * 8, st));  // peaks start at +0
-  const dim3 grid((unsigned)((nr + l2::kThreads - 1) / l2::kThreads), (unsigned)ns);
+  const dim3 grid = l2::grid(ns, nr);
   const T* sy = static_cast<const T*>(syn);
   const T* ob = static_cast<const T*>(obs);
-  ADFWI_LAUNCH(kAux, st, (l2::peaks<T><<<grid, l2::kThreads, 0, st>>>(ns, nt, nr, sy, ob, stats, gsyn, gobs)));
-  ADFWI_LAUNCH(kAux, st, (l2::factors<T><<<grid, l2::kThreads, 0, st>>>(ns, nt, nr, p->d.dt, silent_rel, flags & 1, sy,
-                                                                          ob, stats, gsyn, gobs, fac, norms)));
+  ADFWI_LAUNCH(kAux, st, (l2::peaks<T><<<grid, l2::block(), 0, st>>>(ns, nt, nr, sy, ob, stats, gsyn, gobs)));
+  ADFWI_LAUNCH(kAux, st, (l2::factors<T><<<grid, l2::block(), 0, st>>>(ns, nt, nr, p->d.dt, silent_rel, flags & 1, sy,
+                                                                         ob, stats, gsyn, gobs, fac, norms)));
   for (int m = 0; m < p->nm; ++m) {
     const int s0 = p->model_shot_beg[m], s1 = p->model_shot_beg[m + 1];
     ADFWI_LAUNCH(kAux, st, (l2::sum_norms<<<1, l2::kThreads, 0, st>>>((int64_t)(s1 - s0) * nr,
                                                                        norms + (int64_t)s0 * nr, loss + m)));
   }
+  ADFWI_CUDA_TRY(cudaGetLastError());
+  return kOk;
+}
+
+// The misfit's adjoint source of every record sample into adj (ns, nt, nr), times *gmul, from
+// the factors l2_loss_impl left in the workspace.
+template <typename T>
+int l2_sources_impl(const adfwi_acoustic_plan* p, const void* syn, const void* obs, int flags, const double* gmul,
+                    void* adj, unsigned char* ws, int64_t ws_bytes, cudaStream_t st) {
+  const Carve c = carve(p, true, p->K);
+  if (ws_bytes < c.total) {
+    set_error("workspace too small: %lld bytes given, %lld needed", (long long)ws_bytes, (long long)c.total);
+    return kWorkspaceTooSmall;
+  }
+  const int ns = p->d.ns, nt = p->d.nt, nr = p->d.nr;
+  const auto* fac = reinterpret_cast<const l2::TraceFactors<T>*>(ws + c.mfac);
+  ADFWI_LAUNCH(kAux, st, (l2::sources<T><<<l2::grid(ns, nr), l2::block(), 0, st>>>(
+                             ns, nt, nr, flags & 1, static_cast<const T*>(syn), static_cast<const T*>(obs), fac, gmul,
+                             static_cast<T*>(adj))));
   ADFWI_CUDA_TRY(cudaGetLastError());
   return kOk;
 }
@@ -1120,6 +1160,18 @@ int adfwi_acoustic_l2_loss(const adfwi_acoustic_plan* p, const void* syn, const 
   if (p->d.dtype == ADFWI_F64)
     return l2_loss_impl<double>(p, syn, obs, silent_rel, flags, loss, ws, workspace_bytes, st);
   return l2_loss_impl<float>(p, syn, obs, silent_rel, flags, loss, ws, workspace_bytes, st);
+}
+
+int adfwi_acoustic_l2_sources(const adfwi_acoustic_plan* p, const void* syn, const void* obs, int32_t flags,
+                              const double* grad_scale, void* adj, void* workspace, int64_t workspace_bytes,
+                              void* stream) {
+  ADFWI_CHECK_ARG(p && syn && obs && grad_scale && adj && workspace, "null argument");
+  ADFWI_CHECK_ARG(p->d.nr > 0, "the plan has no receivers");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  unsigned char* ws = static_cast<unsigned char*>(workspace);
+  if (p->d.dtype == ADFWI_F64)
+    return l2_sources_impl<double>(p, syn, obs, flags, grad_scale, adj, ws, workspace_bytes, st);
+  return l2_sources_impl<float>(p, syn, obs, flags, grad_scale, adj, ws, workspace_bytes, st);
 }
 
 int adfwi_acoustic_backward_l2(const adfwi_acoustic_plan* p, const void* wavelet, const void* syn, const void* obs,

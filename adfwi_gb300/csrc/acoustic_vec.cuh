@@ -50,6 +50,7 @@ __device__ __forceinline__ unsigned char* aligned_smem128(unsigned char* raw) {
   return raw + ((128u - (smem_u32(raw) & 127u)) & 127u);
 }
 constexpr int kVecSmemFixed = 1024 + 128;
+constexpr int RC = 3;  // receiver cells a relay lane keeps in registers for a unit (31 RC per tile)
 
 __device__ __forceinline__ void ld4(const float* p, float (&r)[4]) {
   const float4 q = *reinterpret_cast<const float4*>(p);
@@ -173,13 +174,13 @@ __global__ void __launch_bounds__(VTHREADS, VMINB)
       produce<T, 3>(maps, g, a, h, ih, stage0, LY::kStage, LY::kStageTx, ymap, u_beg, u_end, true);
     } else if (recording) {
       // records of step it (acoustic_kernels.py:167-169) from the item's stored p, u, w; a lane
-      // keeps the cells and ids of its receivers rb + lane - 1 + 31 m (m < 2) for the unit
+      // keeps the cells and ids of its receivers rb + lane - 1 + 31 m (m < RC) for the unit
       const Layout L = g.L;
       T* rp = const_cast<T*>(a.rec_p);
       T* ru = const_cast<T*>(a.rec_u);
       T* rw = const_cast<T*>(a.rec_w);
-      int64_t coff[2] = {0, 0};
-      int rid[2] = {0, 0}, rn = 0, rb = 0, re = 0, i0 = 0, j0 = 0;
+      int64_t coff[RC] = {};
+      int rid[RC] = {}, rn = 0, rb = 0, re = 0, i0 = 0, j0 = 0;
       relay(g, a, h, u_beg, u_end, lane, [&](int tile) { return g.tile_rcv_beg[tile + 1] > g.tile_rcv_beg[tile]; },
             [&](int tile) {
               rb = g.tile_rcv_beg[tile];
@@ -188,7 +189,7 @@ __global__ void __launch_bounds__(VTHREADS, VMINB)
               j0 = (tile % g.tiles_x) * TX;
               rn = 0;
 #pragma unroll
-              for (int m = 0; m < 2; ++m) {
+              for (int m = 0; m < RC; ++m) {
                 const int q = rb + lane - 1 + 31 * m;
                 if (q < re) {
                   const int cell = g.trcv_cell[q];
@@ -200,22 +201,22 @@ __global__ void __launch_bounds__(VTHREADS, VMINB)
             },
             [&](int tile, int sh) {
               const int64_t rowbase = ((int64_t)sh * g.nt + a.it) * g.nr, so = (int64_t)sh * L.plane;
-              T vp[2], vu[2], vw[2];
+              T vp[RC], vu[RC], vw[RC];
 #pragma unroll
-              for (int m = 0; m < 2; ++m)
+              for (int m = 0; m < RC; ++m)
                 if (m < rn) {
                   vp[m] = a.o0[so + coff[m]];
                   vu[m] = a.o1[so + coff[m]];
                   vw[m] = a.o2[so + coff[m]];
                 }
 #pragma unroll
-              for (int m = 0; m < 2; ++m)
+              for (int m = 0; m < RC; ++m)
                 if (m < rn) {
                   rp[rowbase + rid[m]] = vp[m];
                   ru[rowbase + rid[m]] = vu[m];
                   rw[rowbase + rid[m]] = vw[m];
                 }
-              for (int q = rb + lane - 1 + 62; q < re; q += 31) {  // more than 62 receivers in the tile
+              for (int q = rb + lane - 1 + 31 * RC; q < re; q += 31) {  // more than 31 RC receivers in the tile
                 const int cell = g.trcv_cell[q];
                 const int64_t o = rowbase + g.trcv_id[q], c = so + L.off(i0 + (cell >> 16), j0 + (cell & 0xffff));
                 rp[o] = a.o0[c];
@@ -512,12 +513,15 @@ __global__ void __launch_bounds__(VTHREADS, VAMINB)
     } else if (a.it >= 1 && a.rec_p != nullptr) {
       // dL/d p-records of step it-1 enter lambda_p after step it-1 (acoustic_kernels.py:167-169),
       // added to the item's stored lambda_p. A lane keeps its receiver cells cb + lane - 1 + 31 m
-      // (m < 2) with their receiver for the unit; cells with several receivers, and a tile's
-      // cells past the 62nd, walk the tables per item.
+      // (m < RC) with their receiver for the unit and issues every load of an item before its
+      // arithmetic, so that an item costs the relay one round trip (the relay paces the
+      // receiver tiles' blocks: work added here lengthens the launch). Cells with several
+      // receivers, and tiles of more than 31 RC receiver cells, walk the tables per item.
       const Layout L = g.L;
-      int64_t coff[2] = {0, 0};
-      int rid[2] = {0, 0}, cn = 0, cb = 0, ce = 0, i0 = 0, j0 = 0;
+      int64_t coff[RC] = {};
+      int rid[RC] = {}, cn = 0, cb = 0, ce = 0, i0 = 0, j0 = 0;
       bool walk = false;
+      const T gmul = ac::fused_scale(g);
       relay(g, a, h, u_beg, u_end, lane, [&](int tile) { return adj_relay_tile(g, a, tile); },
             [&](int tile) {
               cb = g.tile_cell_beg[tile];
@@ -525,9 +529,9 @@ __global__ void __launch_bounds__(VTHREADS, VAMINB)
               i0 = g.zbeg + (tile / g.tiles_x) * TZ;
               j0 = (tile % g.tiles_x) * TX;
               cn = 0;
-              walk = ce - cb > 62;
+              walk = ce - cb > 31 * RC;
 #pragma unroll
-              for (int m = 0; m < 2; ++m) {
+              for (int m = 0; m < RC; ++m) {
                 const int q = cb + lane - 1 + 31 * m;
                 if (q < ce) {
                   const int cell = g.tcell_cell[q], m0 = g.tcell_rbeg[q];
@@ -541,18 +545,19 @@ __global__ void __launch_bounds__(VTHREADS, VAMINB)
             [&](int tile, int sh) {
               const int64_t so = (int64_t)sh * L.plane;
               if (!walk) {
-                T v[2], o[2];
+                ac::RecPIn<T> in[RC];
+                T o[RC];
 #pragma unroll
-                for (int m = 0; m < 2; ++m)
+                for (int m = 0; m < RC; ++m)
                   if (m < cn) {
-                    v[m] = ac::grad_rec_p(g, a.rec_p, sh, a.it - 1, rid[m]);
+                    in[m] = ac::grad_rec_p_load(g, a.rec_p, sh, a.it - 1, rid[m]);
                     o[m] = a.o0[so + coff[m]];
                   }
 #pragma unroll
-                for (int m = 0; m < 2; ++m)
+                for (int m = 0; m < RC; ++m)
                   if (m < cn) {
                     T ap = T(0);
-                    ap += v[m];
+                    ap += ac::grad_rec_p_value(g, in[m], a.it - 1, gmul);
                     a.o0[so + coff[m]] = o[m] + ap;
                   }
               } else {
@@ -560,7 +565,7 @@ __global__ void __launch_bounds__(VTHREADS, VAMINB)
                   const int cell = g.tcell_cell[q];
                   T ap = T(0);
                   for (int mm = g.tcell_rbeg[q]; mm < g.tcell_rbeg[q + 1]; ++mm)
-                    ap += ac::grad_rec_p(g, a.rec_p, sh, a.it - 1, g.cell_rcv[mm]);
+                    ap += ac::grad_rec_p(g, a.rec_p, sh, a.it - 1, g.cell_rcv[mm], gmul);
                   T* o = a.o0 + so + L.off(i0 + (cell >> 16), j0 + (cell & 0xffff));
                   *o = *o + ap;
                 }
@@ -810,7 +815,7 @@ __global__ void __launch_bounds__(VTHREADS, VAMINB)
             T ap = T(0), au = T(0), aw = T(0);
             for (int mm = g.tcell_rbeg[q]; mm < g.tcell_rbeg[q + 1]; ++mm) {
               const int64_t o = rowbase + g.cell_rcv[mm];
-              if (a.rec_p) ap += ac::grad_rec_p(g, a.rec_p, sh, a.it - 1, g.cell_rcv[mm]);
+              if (a.rec_p) ap += ac::grad_rec_p(g, a.rec_p, sh, a.it - 1, g.cell_rcv[mm], ac::fused_scale(g));
               if (a.rec_u) au += a.rec_u[o];
               if (a.rec_w) aw += a.rec_w[o];
             }

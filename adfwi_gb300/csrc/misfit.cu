@@ -4,14 +4,11 @@
 //   ADFWI/fwi/misfit/L2.py:26-29        L = sum_{s,r} sqrt(sum_t (obs - syn)^2 dt)
 //   ADFWI/fwi/acoustic_fwi.py:149-150   both traces divided by their max |value| first
 // The reference evaluates it with PyTorch operations (a dozen (ns, nt, nr) round trips, FP32
-// sums) and differentiates it with autograd. Here three kernels read the records a few times
-// each and write the adjoint source once; every sum over time and over traces is FP64 in a
-// fixed order, so the loss and the adjoint source are deterministic.
-//
-// The per-trace statistics, factors and adjoint-source sample are in l2.cuh (shared with the
-// acoustic adjoint step, which forms the pressure records' adjoint source on the fly); here
-// three kernels read the records a few times each and write the adjoint source once, and one
-// block sums the per-trace norms in a fixed order.
+// sums) and differentiates it with autograd. Here three bandwidth-bound passes (l2.cuh: peaks,
+// factors, sources) read the records three times and write the adjoint source once, and one
+// block sums the per-trace norms; every sum over time and over traces is FP64 in a fixed order,
+// so the loss and the adjoint source are deterministic. The kernels are the ones the acoustic
+// plan's loss uses, so both give the same bits.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -26,30 +23,10 @@ namespace mf {
 
 using namespace l2;
 
-template <typename T>
-__global__ void __launch_bounds__(kThreads) adjoint(int ns, int nt, int nr, double dt, double silent_rel,
-                                                    int normalise_obs, const T* __restrict__ syn,
-                                                    const T* __restrict__ obs, const TraceStats<T>* __restrict__ st,
-                                                    const PeakWord<T>* __restrict__ gsyn,
-                                                    const PeakWord<T>* __restrict__ gobs, T* __restrict__ adj,
-                                                    double* __restrict__ norms) {
-  const int r = blockIdx.x * blockDim.x + threadIdx.x, s = blockIdx.y;
-  if (r >= nr) return;
-  const int64_t tr = (int64_t)s * nr + r;
-  const T* ps = syn + (int64_t)s * nt * nr + r;
-  const T* po = obs + (int64_t)s * nt * nr + r;
-  double n;
-  const TraceFactors<T> f = trace_factors(st[tr], (double)peak_value(gsyn + s), (double)peak_value(gobs + s), ps, po,
-                                          nt, nr, dt, silent_rel, normalise_obs, &n);
-  norms[tr] = n;
-  T* pa = adj + (int64_t)s * nt * nr + r;
-  for (int t = 0; t < nt; ++t) pa[(int64_t)t * nr] = source(f, ps[(int64_t)t * nr], po[(int64_t)t * nr], t, normalise_obs);
-}
-
 int64_t align256(int64_t x) { return (x + 255) / 256 * 256; }
 
 struct MCarve {
-  int64_t stats, gsyn, gobs, norms, total;
+  int64_t stats, gsyn, gobs, norms, fac, total;
 };
 
 MCarve mcarve(int dtype, int64_t ns, int64_t nr) {
@@ -65,6 +42,9 @@ MCarve mcarve(int dtype, int64_t ns, int64_t nr) {
   o += align256(ns * pw);
   c.norms = o;
   o += align256(ns * nr * 8);
+  c.fac = o;
+  o += align256(ns * nr *
+                (dtype == ADFWI_F64 ? (int64_t)sizeof(TraceFactors<double>) : (int64_t)sizeof(TraceFactors<float>)));
   c.total = o;
   return c;
 }
@@ -77,14 +57,16 @@ int run(int32_t ns, int32_t nt, int32_t nr, double dt, double silent_rel, int32_
   auto* gsyn = reinterpret_cast<PeakWord<T>*>(ws + c.gsyn);
   auto* gobs = reinterpret_cast<PeakWord<T>*>(ws + c.gobs);
   auto* norms = reinterpret_cast<double*>(ws + c.norms);
+  auto* fac = reinterpret_cast<TraceFactors<T>*>(ws + c.fac);
   ADFWI_CUDA_TRY(cudaMemsetAsync(ws + c.gsyn, 0, c.norms - c.gsyn, st));  // peaks start at +0
-  const dim3 grid((unsigned)((nr + kThreads - 1) / kThreads), (unsigned)ns);
-  ADFWI_LAUNCH(kAux, st, (peaks<T><<<grid, kThreads, 0, st>>>(ns, nt, nr, static_cast<const T*>(syn),
-                                                                static_cast<const T*>(obs), stats, gsyn, gobs)));
-  ADFWI_LAUNCH(kAux, st, (adjoint<T><<<grid, kThreads, 0, st>>>(ns, nt, nr, dt, silent_rel, flags & 1,
-                                                                  static_cast<const T*>(syn),
-                                                                  static_cast<const T*>(obs), stats, gsyn, gobs,
-                                                                  static_cast<T*>(adj), norms)));
+  const T* sy = static_cast<const T*>(syn);
+  const T* ob = static_cast<const T*>(obs);
+  const int nob = flags & 1;
+  ADFWI_LAUNCH(kAux, st, (peaks<T><<<grid(ns, nr), block(), 0, st>>>(ns, nt, nr, sy, ob, stats, gsyn, gobs)));
+  ADFWI_LAUNCH(kAux, st, (factors<T><<<grid(ns, nr), block(), 0, st>>>(ns, nt, nr, dt, silent_rel, nob, sy, ob, stats,
+                                                                         gsyn, gobs, fac, norms)));
+  ADFWI_LAUNCH(kAux, st, (sources<T><<<grid(ns, nr), block(), 0, st>>>(ns, nt, nr, nob, sy, ob, fac, nullptr,
+                                                                         static_cast<T*>(adj))));
   ADFWI_LAUNCH(kAux, st, (sum_norms<<<1, kThreads, 0, st>>>((int64_t)ns * nr, norms, loss)));
   ADFWI_CUDA_TRY(cudaGetLastError());
   return kOk;

@@ -173,15 +173,17 @@ class AcousticPropagator(_PropagatorBase):
 
 
     def forward_l2(self, obs, model=None, shot_index=None, checkpoint_segments: int = 1, silent_rel=0.0,
-                   normalise_obs=False):
+                   normalise_obs=False, adjoint_source="array"):
         """The normalised L2 misfit of the selected shots' pressure records against ``obs``
-        (ns, nt, nr), fused with the solve: returns (loss, record dict). ``loss`` (FP64) is
+        (ns, nt, nr) with the solve: returns (loss, record dict). ``loss`` (FP64) is
         differentiable with respect to the model parameters; its backward runs the hand-written
-        adjoint with the misfit's adjoint source formed inside the adjoint step (the reference
-        computes the records, the misfit of ADFWI/fwi/misfit/L2.py:26-29 on peak-normalised traces
-        (ADFWI/fwi/acoustic_fwi.py:149-150) and its autograd gradient as three separate passes).
+        adjoint driven by the misfit's adjoint source (the reference computes the records, the
+        misfit of ADFWI/fwi/misfit/L2.py:26-29 on peak-normalised traces
+        (ADFWI/fwi/acoustic_fwi.py:149-150) and its autograd gradient as separate PyTorch passes).
         ``normalise_obs`` divides obs by its trace peaks too; ``silent_rel`` > 0 treats traces
-        whose peak is at most that share of their gather's peak as zero (0 = the reference)."""
+        whose peak is at most that share of their gather's peak as zero (0 = the reference).
+        ``adjoint_source``: "array" (one (ns, nt, nr) source array, the faster form) or "inject"
+        (formed inside the adjoint step, no array); the same bits either way."""
         from .acoustic import AcousticL2Solve
         model = self.model if model is None else model
         model.forward()
@@ -191,7 +193,8 @@ class AcousticPropagator(_PropagatorBase):
             alpha1, alpha2 = alpha1.to(self.dtype), alpha2.to(self.dtype)
         obs = torch.as_tensor(obs, device=self._dev)
         loss, rp, ru, rw, fp, fu, fw = AcousticL2Solve.apply(alpha1, alpha2, self.damp, self._wavelet_rows(idx), obs,
-                                                             plan, float(silent_rel), bool(normalise_obs))
+                                                             plan, float(silent_rel), bool(normalise_obs),
+                                                             adjoint_source)
         return loss, {"p": rp, "u": ru, "w": rw, "forward_wavefield_p": fp, "forward_wavefield_u": fu,
                       "forward_wavefield_w": fw}
 

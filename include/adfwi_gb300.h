@@ -116,21 +116,27 @@ int adfwi_acoustic_backward(const adfwi_acoustic_plan* plan, const void* alpha1,
                             const void* grad_rec_w, void* grad_alpha1, void* grad_alpha2,
                             void* workspace, int64_t workspace_bytes, void* stream);
 
-/* The normalised L2 misfit fused into the adjoint: replaces the reference's misfit evaluation
+/* The normalised L2 misfit on a plan's records: replaces the reference's misfit evaluation
  * ADFWI/fwi/misfit/L2.py:26-29 on the traces normalised at ADFWI/fwi/acoustic_fwi.py:149-150
- * and the hand-off of its autograd gradient to the propagator's backward (the (ns, nt, nr)
- * adjoint source is never written: the adjoint step forms each dL/d p-record sample from the
- * records and the observed data as it injects it).
+ * and the hand-off of its autograd gradient to the propagator's backward.
  * adfwi_acoustic_l2_loss, after a with_gradient forward on the workspace: syn = the forward's
  * p records, obs (ns, nt, nr); writes each model's loss (nmodels device doubles; the misfit of
  * adfwi_l2_misfit, same flags and silent_rel, dt of the plan) and keeps the per-trace factors in
- * the workspace. adfwi_acoustic_backward_l2 then runs the adjoint with that source times
- * *grad_scale (one device double; exactly the unscaled source when it is 1), giving dL/d alpha1
- * and dL/d alpha2 like adfwi_acoustic_backward; the source values are bit-identical to
- * adfwi_l2_misfit's adj. */
+ * the workspace. Then either
+ *   adfwi_acoustic_l2_sources writes the adjoint source times *grad_scale (one device double;
+ *   exactly the unscaled source when it is 1) into adj (ns, nt, nr), for
+ *   adfwi_acoustic_backward's grad_rec_p; or
+ *   adfwi_acoustic_backward_l2 runs the adjoint with that source formed inside the adjoint step
+ *   as it is injected (no (ns, nt, nr) array; slower per step on GB300, where the extra work
+ *   lands on the lanes that inject the receivers),
+ * giving dL/d alpha1 and dL/d alpha2 like adfwi_acoustic_backward. The source values of both are
+ * bit-identical to adfwi_l2_misfit's adj. */
 int adfwi_acoustic_l2_loss(const adfwi_acoustic_plan* plan, const void* syn, const void* obs,
                            double silent_rel, int32_t flags, double* loss, void* workspace,
                            int64_t workspace_bytes, void* stream);
+int adfwi_acoustic_l2_sources(const adfwi_acoustic_plan* plan, const void* syn, const void* obs,
+                              int32_t flags, const double* grad_scale, void* adj, void* workspace,
+                              int64_t workspace_bytes, void* stream);
 int adfwi_acoustic_backward_l2(const adfwi_acoustic_plan* plan, const void* wavelet, const void* syn,
                                const void* obs, int32_t flags, const double* grad_scale,
                                void* grad_alpha1, void* grad_alpha2, void* workspace,

@@ -124,15 +124,16 @@ def c2_slice():
                 survey=survey)
 
 
-@pytest.mark.parametrize("snapshot_every", [0, 50])
-def test_c2_full_grid_fused_l2_gradient_matches_oracle(c2_slice, snapshot_every):
-    """The same misfit through AcousticPropagator.forward_l2 (the misfit fused into the adjoint:
-    obs normalised by the kernel with the same silent rule)."""
+@pytest.mark.parametrize("snapshot_every,adjoint_source", [(0, "array"), (50, "array"), (50, "inject")])
+def test_c2_full_grid_fused_l2_gradient_matches_oracle(c2_slice, snapshot_every, adjoint_source):
+    """The same misfit through AcousticPropagator.forward_l2 (the CUDA misfit on the plan's
+    records, obs normalised by the kernel with the same silent rule; its adjoint source as an
+    array or formed inside the adjoint step)."""
     model, survey = c2_slice["model"], c2_slice["survey"]
     prop = A.AcousticPropagator(model, survey, device="cuda:0", snapshot_every=snapshot_every)
     model.vp.grad = None
     loss, rec = prop.forward_l2(c2_slice["obs"].cuda(), shot_index=c2_slice["idx"], silent_rel=1e-3,
-                                normalise_obs=True)
+                                normalise_obs=True, adjoint_source=adjoint_source)
     loss.backward()
     assert rel(rec["p"], c2_slice["rec"]) <= 1e-5
     assert abs(float(loss) - c2_slice["loss"]) <= 1e-5 * abs(c2_slice["loss"])

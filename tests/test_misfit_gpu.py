@@ -52,6 +52,42 @@ def test_fused_misfit_is_the_autograd_gradient():
     assert float((s2.grad - 2.0 * s.grad).norm() / (2.0 * s.grad).norm()) <= 1e-12
 
 
+def test_misfit_peaks_keep_the_first_arg_max_across_time_phases():
+    """Equal peaks at several samples (their time phases in either order, a negative one first):
+    the max's share of the adjoint source goes to the earliest, as a scan in time order gives.
+    Expected values: the formula restated with numpy in FP64 (argmax: first occurrence)."""
+    import numpy as np
+    g = torch.Generator().manual_seed(11)
+    ns, nt, nr, dt = 2, 300, 40, 1e-3
+    syn = torch.randn(ns, nt, nr, generator=g, dtype=torch.float64) * 0.1
+    obs = torch.randn(ns, nt, nr, generator=g, dtype=torch.float64)
+    syn[0, 20, 3] = 2.0; syn[0, 7, 3] = 2.0        # first at t=7 (phase 7), tie at t=20 (phase 4)
+    syn[0, 35, 4] = -3.0; syn[0, 19, 4] = 3.0      # first at t=19, positive; tie at t=35, negative
+    syn[1, 50, 5] = -1.5; syn[1, 66, 5] = -1.5; syn[1, 290, 5] = 1.5  # same phase: first t=50
+    syn[1, 0, 6] = 4.0; syn[1, 299, 6] = -4.0      # ends of the trace
+    loss, adj = l2_misfit_and_adjoint(syn.cuda(), obs.cuda(), dt, normalise_obs=True)
+    y, o = syn.numpy(), obs.numpy()
+    exp = np.zeros_like(y)
+    tot = 0.0
+    for s in range(ns):
+        for r in range(nr):
+            v = y[s, :, r]
+            k = int(np.argmax(np.abs(v)))
+            m = abs(v[k])
+            on = o[s, :, r] / np.abs(o[s, :, r]).max()
+            rsd = on - v / m
+            n = np.sqrt(np.sum(rsd * rsd) * dt)
+            tot += n
+            e = -rsd * dt / (n * m)
+            e[k] += dt * np.sum(rsd * v) / (n * m * m) * np.sign(v[k])
+            exp[s, :, r] = e
+    assert abs(float(loss) - tot) <= 1e-12 * tot
+    a = adj.cpu().numpy()
+    assert np.abs(a - exp).max() <= 1e-12 * np.abs(exp).max()
+    for s, r, t in ((0, 3, 7), (0, 4, 19), (1, 5, 50), (1, 6, 0)):
+        assert abs(a[s, t, r] - exp[s, t, r]) <= 1e-12 * abs(exp[s, t, r])
+
+
 def test_fused_misfit_is_deterministic():
     syn, obs = _records(torch.float32, seed=5, ns=4, nt=500, nr=300)
     a = l2_misfit_and_adjoint(syn, obs, 1e-3)
@@ -91,6 +127,11 @@ def test_misfit_fused_into_the_adjoint_equals_the_two_pass_gradient(dtype, silen
     assert torch.equal(rp, rpf)
     assert float(loss0) == float(loss1[0])
     assert torch.equal(g1, f1) and torch.equal(g2, f2)
+    # the plan's array form of the source: the same bits as adfwi_l2_misfit's
+    src = plan.l2_sources(rpf, obs, wsf, one, normalise_obs)
+    assert torch.equal(src, adj)
+    src2 = plan.l2_sources(rpf, obs, wsf, 2.0 * one, normalise_obs)
+    assert torch.equal(src2, adj * 2.0)
     # the scale of the source scales the gradient
     rpf, _, _, _, _, _, wsf = plan.run_forward(a1, a2, damp, wav, True)
     plan.l2_loss(rpf, obs, wsf, silent_rel, normalise_obs)

@@ -356,7 +356,7 @@ class _Batch(object):
         rec = self.ns * self.nt * self.nr * 4
         grid = self.nm * self.nzp * self.nxp * 4
         model = self.nm * self.nz * self.nx * 4
-        self.nbytes = (_aligned(self.ws_bytes) + 3 * _aligned(rec) + (_aligned(rec) if self.grad else 0)
+        self.nbytes = (_aligned(self.ws_bytes) + 3 * _aligned(rec) + (2 * _aligned(rec) if self.grad else 0)
                        + 3 * _aligned(grid) + 5 * _aligned(model) + _aligned(self.ns * self.nt * 4) + 2 * _ALIGN)
         self.cells = [n * self.nzp * self.nxp * self.nt for n in self.ns_r]
         self.off = self.n = None
@@ -382,6 +382,7 @@ class _Batch(object):
         self.one.fill_(1.0)
         if self.grad:
             self.obs = cv.take(shp, torch.float32)
+            self.adj = cv.take(shp, torch.float32)  # the misfit's adjoint source
         _, w = _wavelet(self.nt, self.dt, self.f0)
         self.wav.copy_(torch.from_numpy(np.ascontiguousarray(np.tile(w, (self.ns, 1)), dtype=np.float32)))
         self.bound = True
@@ -413,11 +414,11 @@ class _Batch(object):
                               fw=self.fw, stream=h)
         if not self.grad:
             return
-        # each request's misfit over its own traces; the adjoint forms their sources as it
-        # injects them (no (ns, nt, nr) source array)
+        # each request's misfit over its own traces, its adjoint source in one pass, the adjoint
         self.out_loss = self.plan.l2_loss(self.recs[0], self.obs, self.ws, self.silent_rel, True, stream=h)
-        ga1, _ = self.plan.run_backward_l2(self.a1, self.wav, self.recs[0], self.obs, self.ws, self.one, True,
-                                           stream=h)
+        self.plan.l2_sources(self.recs[0], self.obs, self.ws, self.one, True, adj=self.adj, stream=h)
+        ga1, _ = self.plan.run_backward(self.a1, self.a2, self.damp, self.wav, (self.adj, None, None), self.ws,
+                                        stream=h)
         # alpha1 = ((den c) c) dt / dx; alpha2 and rho do not depend on vp
         g_t2 = ga1 * (self.dt / self.dx)
         self.out_grad = [fold_replicate_pad(g_t2[m] * t1[m] + g_t2[m] * c[m] * den[m], nb) for m in range(self.nm)]
@@ -468,6 +469,10 @@ class _Entry(object):
     def __init__(self, t, req, fut, bucket, shots, snapshot_every):
         self.t, self.req, self.fut, self.bucket, self.shots, self.snapshot_every = t, req, fut, bucket, shots, \
             snapshot_every
+
+
+def _member_order(e):
+    return (-e.shots, _i64(e.req.src_z), _i64(e.req.src_x))
 
 
 def form_batch(queue, i, max_shots, max_requests):
@@ -654,7 +659,10 @@ class SolveServer(object):
             idx = form_batch(q, i, self.max_batch_shots, self.max_batch_requests)
             admitted, dropped = None, False
             while idx and admitted is None:  # shed the newest members until the batch's range fits
-                members = [q[j] for j in idx]
+                # members in a canonical order (most shots first, then geometry), so that the
+                # same set of request shapes makes the same batch composition, whatever their
+                # arrival order, and reuses its graph
+                members = sorted((q[j] for j in idx), key=_member_order)
                 reqs = [e.req for e in members]
                 key = _batch_signature(members[0].bucket, reqs)
                 batch = self._take_idle(key)

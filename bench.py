@@ -5,8 +5,8 @@ Workload (one "step"): one full-waveform-inversion gradient evaluation on the 20
 layered/faulted iso-acoustic model (dx = 20 m, PML 50 -> 300 x 700 padded cells), 30 surface
 shots, 600 receivers, nt = 3000, dt = 1.5 ms, 8 Hz Ricker, FP32: forward solve on the smoothed
 starting model, per-trace normalisation and the L2 misfit against data observed on the true
-model (the misfit fused into the adjoint's receiver injection), then the hand-written
-checkpointed adjoint back to dL/dvp. Inputs are seeded synthetic
+model (the CUDA misfit passes on the plan's records and its adjoint source), then the
+hand-written checkpointed adjoint back to dL/dvp. Inputs are seeded synthetic
 stand-ins with those shapes and distributions (no public dataset).
 
 Metric: Gcell-updates/s = shots * nzp * nxp * nt / time per gradient step.
@@ -187,7 +187,7 @@ def gpu_arm(args, world, rank, local):
         model.vp.data.copy_(vp0)
         model.vp.grad = None
         # forward solve + normalised L2 misfit (obs normalised once at setup, as acoustic_fwi.py
-        # does), then the adjoint with the misfit's adjoint source formed inside it
+        # does), its adjoint source in one pass, then the adjoint
         loss, _ = prop.forward_l2(obs_dev)
         loss.backward()
         return loss

@@ -23,7 +23,7 @@ class AcousticDesc(ctypes.Structure):
         ("ns", c_int32), ("nt", c_int32), ("nr", c_int32), ("dtype", c_int32),
         ("checkpoint_segments", c_int32), ("snapshot_every", c_int32),
         ("snapshot_precision", c_int32), ("shots_per_block", c_int32),
-        ("dt", ctypes.c_double), ("memory_budget", c_int64),
+        ("dt", ctypes.c_double), ("memory_budget", c_int64), ("ring_depth", c_int32), ("reserved", c_int32),
     ]
 
 

@@ -44,7 +44,7 @@ class AcousticPlan(object):
 
     def __init__(self, *, nz, nx, nabc, free_surface, src_z, src_x, rcv_z, rcv_x, nt, dt, dtype,
                  checkpoint_segments=1, snapshot_every=0, snapshot_precision="native",
-                 shots_per_block=0, memory_budget=0, shot_model=None):
+                 shots_per_block=0, memory_budget=0, shot_model=None, ring_depth=0):
         """``shot_model`` (ns ints, non-decreasing) makes a batched plan: several velocity models of
         this grid shape solved in the same launches, shot s on model shot_model[s]; its
         coefficient inputs and its illumination / gradient outputs then carry a leading model
@@ -64,6 +64,7 @@ class AcousticPlan(object):
         d.shots_per_block = int(shots_per_block or 0)
         d.dt = float(dt)
         d.memory_budget = int(memory_budget or 0)
+        d.ring_depth = int(ring_depth)
         self.desc = d
         h = ctypes.c_void_p()
         geo = (ctypes.byref(d), self.src_z.ctypes.data_as(ctypes.c_void_p),

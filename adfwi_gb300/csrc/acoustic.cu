@@ -267,6 +267,7 @@ struct adfwi_acoustic_plan {
   int K, nseg;           // snapshot interval and number of segments (gradient mode)
   int last_chunk_start;  // first step of the reference's last checkpoint chunk
   int elem;              // bytes per element
+  bool deep = false;     // deep-ring variants of the step kernels (FP32 only)
   int nm;                // models of a batched plan (1 otherwise)
   std::vector<int> model_shot_beg;  // nm+1 offsets: the shots of each model
   std::vector<int> model_grp_beg;   // nm+1 offsets: the shot groups of each model
@@ -407,13 +408,31 @@ int setup_common(const adfwi_acoustic_plan* p, unsigned char* ws, const Carve& c
   return kOk;
 }
 
+// Stages of the TMA ring of each variant (deep: the FP32 variants compiled for VDEEP blocks per
+// SM; FP64 has one variant).
 template <typename T>
-int vec_adj_stages() {
-  return sizeof(T) == 8 ? 2 : (ac2::VAMINB >= 3 ? 2 : 3);
+int vec_adj_stages(bool deep) {
+  return sizeof(T) == 8 ? 2 : ((deep ? ac2::VDEEP : ac2::VAMINB) >= 3 ? 2 : 3);
 }
 template <typename T>
-int vec_stages() {
-  return sizeof(T) == 8 ? 2 : (ac2::VMINB >= 3 ? 3 : 4);
+int vec_stages(bool deep) {
+  return sizeof(T) == 8 ? 2 : ((deep ? ac2::VDEEP : ac2::VMINB) >= 3 ? 3 : 4);
+}
+template <typename T>
+using StepKernel = void (*)(ac2::Maps, ac::Geo<T>, ac2::StepArgs<T>);
+template <typename T>
+StepKernel<T> fwd_kernel(bool deep) {
+  if constexpr (sizeof(T) == 4) {
+    if (deep) return ac2::fwd_step_vec<T, ac2::VDEEP>;
+  }
+  return ac2::fwd_step_vec<T, ac2::VMINB>;
+}
+template <typename T>
+StepKernel<T> adj_kernel(bool deep) {
+  if constexpr (sizeof(T) == 4) {
+    if (deep) return ac2::adj_step_vec<T, ac2::VDEEP>;
+  }
+  return ac2::adj_step_vec<T, ac2::VAMINB>;
 }
 
 // Launch of a persistent step kernel with programmatic stream serialisation (the kernel
@@ -460,7 +479,7 @@ int launch_fwd(const adfwi_acoustic_plan* p, const ac::Geo<T>& g, int it, int ac
   if (rc) return rc;
   ac2::StepArgs<T> a = step_args<T>(p, it, cf, flag);
   a.accum_u = accum_u;
-  a.stages = vec_stages<T>();
+  a.stages = vec_stages<T>(p->deep);
   a.wav = wav;
   a.o0 = p1;
   a.o1 = u1;
@@ -472,7 +491,8 @@ int launch_fwd(const adfwi_acoustic_plan* p, const ac::Geo<T>& g, int it, int ac
   a.acc0 = ilp;
   a.acc1 = ilu;
   const int smem = ac2::VecFwdLayout<T>::bytes(a.stages);
-  ADFWI_LAUNCH(kAcFwdStep, st, ADFWI_CUDA_TRY(launch_pdl(ac2::fwd_step_vec<T>, p->t2.fwd_blocks, smem, st, maps, g, a)));
+  ADFWI_LAUNCH(kAcFwdStep, st,
+               ADFWI_CUDA_TRY(launch_pdl(fwd_kernel<T>(p->deep), p->t2.fwd_blocks, smem, st, maps, g, a)));
   return kOk;
 }
 
@@ -489,7 +509,7 @@ int launch_adj(const adfwi_acoustic_plan* p, const ac::Geo<T>& g, int it, const 
   if (!rc) rc = make_plane_map(&maps.e, dh, sizeof(T), p->L, ns, ac2::BOXX, ac2::EZ);
   if (rc) return rc;
   ac2::StepArgs<T> a = step_args<T>(p, it, cf, flag);
-  a.stages = vec_adj_stages<T>();
+  a.stages = vec_adj_stages<T>(p->deep);
   a.o0 = lp1;
   a.o1 = lu1;
   a.o2 = lw1;
@@ -499,7 +519,8 @@ int launch_adj(const adfwi_acoustic_plan* p, const ac::Geo<T>& g, int it, const 
   a.acc0 = g1;
   a.acc1 = g2;
   const int smem = ac2::VecAdjLayout<T>::bytes(a.stages);
-  ADFWI_LAUNCH(kAcAdjStep, st, ADFWI_CUDA_TRY(launch_pdl(ac2::adj_step_vec<T>, p->t2.blocks, smem, st, maps, g, a)));
+  ADFWI_LAUNCH(kAcAdjStep, st,
+               ADFWI_CUDA_TRY(launch_pdl(adj_kernel<T>(p->deep), p->t2.blocks, smem, st, maps, g, a)));
   return kOk;
 }
 
@@ -517,10 +538,12 @@ int set_smem_limits() {
   std::lock_guard<std::mutex> lk(g_smem_mu);
   if ((int)g_smem_done.size() <= dev) g_smem_done.resize(dev + 1, 0);
   if (!(g_smem_done[dev] & bit)) {
-    ADFWI_CUDA_TRY(cudaFuncSetAttribute(ac2::fwd_step_vec<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        ac2::VecFwdLayout<T>::bytes(vec_stages<T>())));
-    ADFWI_CUDA_TRY(cudaFuncSetAttribute(ac2::adj_step_vec<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        ac2::VecAdjLayout<T>::bytes(vec_adj_stages<T>())));
+    for (int deep = 0; deep < (sizeof(T) == 4 ? 2 : 1); ++deep) {
+      ADFWI_CUDA_TRY(cudaFuncSetAttribute(fwd_kernel<T>(deep), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          ac2::VecFwdLayout<T>::bytes(vec_stages<T>(deep))));
+      ADFWI_CUDA_TRY(cudaFuncSetAttribute(adj_kernel<T>(deep), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          ac2::VecAdjLayout<T>::bytes(vec_adj_stages<T>(deep))));
+    }
     g_smem_done[dev] |= bit;
   }
   return kOk;
@@ -770,15 +793,25 @@ int resident_blocks(K kernel, int threads, int smem, int fallback) {
 }
 
 template <typename T>
-int resident_adj_blocks() {
-  return resident_blocks(ac2::adj_step_vec<T>, ac2::VTHREADS, ac2::VecAdjLayout<T>::bytes(vec_adj_stages<T>()),
-                         sizeof(T) == 8 ? 1 : ac2::VAMINB);
+int resident_adj_blocks(bool deep) {
+  return resident_blocks(adj_kernel<T>(deep), ac2::VTHREADS, ac2::VecAdjLayout<T>::bytes(vec_adj_stages<T>(deep)),
+                         sizeof(T) == 8 ? 1 : (deep ? ac2::VDEEP : ac2::VAMINB));
 }
 template <typename T>
-int resident_fwd_blocks() {
-  return resident_blocks(ac2::fwd_step_vec<T>, ac2::VTHREADS, ac2::VecFwdLayout<T>::bytes(vec_stages<T>()),
-                         sizeof(T) == 8 ? 1 : ac2::VMINB);
+int resident_fwd_blocks(bool deep) {
+  return resident_blocks(fwd_kernel<T>(deep), ac2::VTHREADS, ac2::VecFwdLayout<T>::bytes(vec_stages<T>(deep)),
+                         sizeof(T) == 8 ? 1 : (deep ? ac2::VDEEP : ac2::VMINB));
 }
+
+// Padded grids at least this wide run the deep-ring variants (one more stage, 2 blocks per SM).
+// An empirical rule from per-launch times of both rings (FP32, full history; forward / adjoint
+// in us, shallow -> deep): 600 x 1600 padded with 4 / 8 / 16 shots 44.1 -> 41.6 / 77.2 -> 69.1,
+// 86.0 -> 73.5 / 130.8 -> 118.0, 161.8 -> 165.8 / 227.6 -> 217.1; every narrower grid measured
+// (300 x 700 with 10 / 30 / 60 shots, 400 x 1000 with 8 / 16 / 30, 200 x 400 with 16 / 64,
+// up to 144 MB of fields per time level) ran 4-42 % slower with the deep ring. The wide grid's
+// kernels read 27 B per cell-update from DRAM against 13.5 B on the 300 x 700 grid (L2 hit
+// rate 19 % against 30 %), so they wait longer per stage and profit from the extra stage.
+constexpr int kDeepRingCols = 1400;
 
 // Shots per unit for the persistent TMA kernels: balance the units over the resident blocks
 // (the block with the most units sets the time) against the per-unit costs (the coefficient
@@ -996,6 +1029,7 @@ int plan_create_impl(const adfwi_acoustic_desc* desc, const int32_t* src_z, cons
   ADFWI_CHECK_ARG(d.dtype == ADFWI_F32 || d.dtype == ADFWI_F64, "dtype must be ADFWI_F32 or ADFWI_F64");
   ADFWI_CHECK_ARG(d.snapshot_precision >= 0 && d.snapshot_precision <= 3, "bad snapshot_precision");
   ADFWI_CHECK_ARG(d.checkpoint_segments >= 1, "checkpoint_segments must be >= 1");
+  ADFWI_CHECK_ARG(d.ring_depth >= 0 && d.ring_depth <= 2, "ring_depth must be 0, 1 or 2");
   ADFWI_CHECK_ARG(src_z && src_x && (d.nr == 0 || (rcv_z && rcv_x)), "null geometry array");
   adfwi_acoustic_plan* p = new (std::nothrow) adfwi_acoustic_plan();
   if (!p) {
@@ -1042,8 +1076,13 @@ int plan_create_impl(const adfwi_acoustic_desc* desc, const int32_t* src_z, cons
   // 16 x 64 tiles: units of G shots spread over the resident blocks of the pipelined steps.
   {
     const int ntiles = ((p->nxp + ac2::TX - 1) / ac2::TX) * ((p->nzp - p->zbeg + ac2::TZ - 1) / ac2::TZ);
-    const int blocks = p->elem == 8 ? resident_adj_blocks<double>() : resident_adj_blocks<float>();
-    const int fblocks = p->elem == 8 ? resident_fwd_blocks<double>() : resident_fwd_blocks<float>();
+    // shots per group from the shallow variants' widths whatever the ring, so that the ring
+    // changes launch widths and stages only, never the results
+    const int blocks = p->elem == 8 ? resident_adj_blocks<double>(false) : resident_adj_blocks<float>(false);
+    const int fblocks = p->elem == 8 ? resident_fwd_blocks<double>(false) : resident_fwd_blocks<float>(false);
+    p->deep = p->elem == 4 && (d.ring_depth == 2 || (d.ring_depth == 0 && p->nxp >= kDeepRingCols));
+    const int run_blocks = p->deep ? resident_adj_blocks<float>(true) : blocks;
+    const int run_fblocks = p->deep ? resident_fwd_blocks<float>(true) : fblocks;
     // shots per group of each model: as a plan of that model alone would choose them, so a
     // model's partial sums (and so its results) do not depend on the other models of a batch
     std::vector<int> Gm(p->nm);
@@ -1052,8 +1091,8 @@ int plan_create_impl(const adfwi_acoustic_desc* desc, const int32_t* src_z, cons
       Gm[m] = d.shots_per_block > 0 ? d.shots_per_block : pick_unit_shots(alone, ntiles, fblocks, blocks);
     }
     build_tiling(p, &p->t2, ac2::TZ, ac2::TX, Gm, rcv_z, rcv_x);
-    p->t2.blocks = std::max(1, std::min(blocks, p->t2.ntiles * p->t2.ngroups));
-    p->t2.fwd_blocks = std::max(1, std::min(fblocks, p->t2.ntiles * p->t2.ngroups));
+    p->t2.blocks = std::max(1, std::min(run_blocks, p->t2.ntiles * p->t2.ngroups));
+    p->t2.fwd_blocks = std::max(1, std::min(run_fblocks, p->t2.ntiles * p->t2.ngroups));
   }
   if (t.empty()) t.push_back(0);
 

@@ -35,7 +35,8 @@ constexpr int VTHREADS = VG + 32;            // the consumer group + the produce
 #ifndef ADFWI_VEC_MINB
 #define ADFWI_VEC_MINB 3
 #endif
-constexpr int VMINB = ADFWI_VEC_MINB;        // resident blocks per SM the kernel is compiled for
+constexpr int VMINB = ADFWI_VEC_MINB;        // resident blocks per SM of the shallow-ring forward
+constexpr int VDEEP = 2;                     // resident blocks per SM of the deep-ring variants
 constexpr int CGE = BOXX / 4;                // four-column groups across the box (18)
 constexpr int ERP = (EZ + 1) / 2;            // row pairs of the p halo (10)
 constexpr int EXT_TASKS = ERP * CGE;         // halo tasks (180)
@@ -140,8 +141,10 @@ __device__ __forceinline__ void relay(const ac::Geo<T>& g, const StepArgs<T>& a,
   }
 }
 
-template <typename T>
-__global__ void __launch_bounds__(VTHREADS, VMINB)
+// MB: resident blocks per SM the variant is compiled for (VMINB: shallow ring; VDEEP: fewer
+// blocks with more registers and one stage more, for grids whose fields do not stay in L2).
+template <typename T, int MB>
+__global__ void __launch_bounds__(VTHREADS, MB)
     fwd_step_vec(const __grid_constant__ Maps maps, ac::Geo<T> g, StepArgs<T> a) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   unsigned char* smem = aligned_smem128(smem_raw);
@@ -475,8 +478,8 @@ __device__ __forceinline__ bool adj_relay_tile(const ac::Geo<T>& g, const StepAr
          !adj_smem_tile(g, a, tile);
 }
 
-template <typename T>
-__global__ void __launch_bounds__(VTHREADS, VAMINB)
+template <typename T, int MB>
+__global__ void __launch_bounds__(VTHREADS, MB)
     adj_step_vec(const __grid_constant__ Maps maps, ac::Geo<T> g, StepArgs<T> a) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   unsigned char* smem = aligned_smem128(smem_raw);

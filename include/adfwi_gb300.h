@@ -60,6 +60,10 @@ typedef struct adfwi_acoustic_desc {
   int32_t shots_per_block;    /* shots handled by one thread block; 0 = automatic            */
   double dt;                  /* time step (s)                                               */
   int64_t memory_budget;      /* byte cap for the gradient workspace; 0 = no cap             */
+  int32_t ring_depth;         /* TMA ring of the step kernels: 0 = automatic, 1 = shallow    */
+                              /* (3 blocks / SM), 2 = deep (2 blocks / SM, one stage more);  */
+                              /* results do not depend on it                                 */
+  int32_t reserved;           /* 0                                                           */
 } adfwi_acoustic_desc;
 
 typedef struct adfwi_acoustic_plan adfwi_acoustic_plan; /* opaque */

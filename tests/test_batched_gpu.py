@@ -59,3 +59,34 @@ def test_batched_solve_equals_single_model_solves(dtype, free_surface, snapshot_
         assert torch.equal(ga2[m], g2), (m, rel(ga2[m], g2))
         s0 = s1
 
+
+
+@pytest.mark.parametrize("free_surface", [False, True])
+@pytest.mark.parametrize("snapshot_every", [0, 23])
+def test_ring_depth_changes_no_result(free_surface, snapshot_every):
+    """The deep-ring variants of the step kernels (2 blocks per SM, one stage more) launch with
+    other widths and stages but the same units and arithmetic: records, forward-wavefield maps
+    and gradients are bit-identical to the shallow ring's, also on a batched plan."""
+    cases = [_model_inputs(seed, ns, torch.float32, free_surface) for seed, ns in ((6, 3), (7, 2))]
+    p0 = cases[0][0]
+    src_z = np.concatenate([c[0].src_loc[:, 1] for c in cases])
+    src_x = np.concatenate([c[0].src_loc[:, 0] for c in cases])
+    shot_model = np.concatenate([np.full(c[0].src_n, m) for m, c in enumerate(cases)])
+    kw = dict(nz=p0.nz, nx=p0.nx, nabc=p0.nabc, free_surface=free_surface, rcv_z=p0.rcv_loc[:, 1],
+              rcv_x=p0.rcv_loc[:, 0], nt=p0.nt, dt=p0.dt, dtype=torch.float32, snapshot_every=snapshot_every,
+              src_z=src_z, src_x=src_x, shot_model=shot_model)
+    stack = lambda k: torch.stack([c[k] for c in cases]).contiguous()  # noqa: E731
+    a1, a2, damp = stack(1), stack(2), stack(3)
+    wav = torch.cat([c[4] for c in cases]).contiguous()
+    w = None
+    res = []
+    for depth in (1, 2):
+        plan = AcousticPlan(ring_depth=depth, **kw)
+        out = plan.run_forward(a1, a2, damp, wav, True)
+        if w is None:
+            w = torch.randn(out[0].shape, generator=torch.Generator().manual_seed(4)).cuda()
+        ga1, ga2 = plan.run_backward(a1, a2, damp, wav, (w, None, None), out[6])
+        assert plan.status(out[6], True) == 0
+        res.append([t.clone() for t in out[:6]] + [ga1, ga2])
+    for q, (x, y) in enumerate(zip(*res)):
+        assert torch.equal(x, y), (q, rel(x, y))

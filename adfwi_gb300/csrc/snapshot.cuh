@@ -22,37 +22,46 @@ namespace adfwi {
 
 constexpr int kSnapThreads = 512;
 
+// Each plane is split into chunks of kSnapChunk elements, one block per (chunk, plane): the
+// max-abs pass combines the chunks' maxima by atomicMax on the bit patterns of the non-negative
+// floats (exact and order-independent: the scale is the plane's max |x| whatever the split),
+// then the (de)quantising passes run over the same grid.
+constexpr int kSnapChunk = 8192;
+
+inline dim3 snap_grid(int64_t nplanes, int64_t plane) {
+  return dim3((unsigned)((plane + kSnapChunk - 1) / kSnapChunk), (unsigned)nplanes);
+}
+
 template <typename T>
-__device__ __forceinline__ float block_maxabs(const T* __restrict__ x, int64_t n) {
+__global__ void __launch_bounds__(kSnapThreads) snap_maxabs(const T* __restrict__ src, int64_t plane,
+                                                            unsigned* __restrict__ scale_bits) {
   __shared__ float red[kSnapThreads / 32];
+  const int64_t pi = blockIdx.y, b0 = (int64_t)blockIdx.x * kSnapChunk;
+  const int64_t b1 = b0 + kSnapChunk < plane ? b0 + kSnapChunk : plane;
+  const T* x = src + pi * plane;
   float m = 0.f;
-  for (int64_t e = threadIdx.x; e < n; e += blockDim.x) m = fmaxf(m, fabsf((float)x[e]));
+  for (int64_t e = b0 + threadIdx.x; e < b1; e += blockDim.x) m = fmaxf(m, fabsf((float)x[e]));
   for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
   __syncthreads();
   if (threadIdx.x < 32) {
     m = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.f;
     for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-    if (threadIdx.x == 0) red[0] = m;
+    if (threadIdx.x == 0) atomicMax(scale_bits + pi, __float_as_uint(m));
   }
-  __syncthreads();
-  float r = red[0];
-  __syncthreads();
-  return r;
 }
 
-// One block per plane (blockIdx.x selects the plane; its threads stride the elements).
 template <typename T, bool kHalf>
 __global__ void __launch_bounds__(kSnapThreads) snap_quantize(const T* __restrict__ src, int64_t plane,
                                                               unsigned short* __restrict__ dst,
-                                                              float* __restrict__ scales) {
-  const int64_t pi = blockIdx.x;
+                                                              const float* __restrict__ scales) {
+  const int64_t pi = blockIdx.y, b0 = (int64_t)blockIdx.x * kSnapChunk;
+  const int64_t b1 = b0 + kSnapChunk < plane ? b0 + kSnapChunk : plane;
   const T* x = src + pi * plane;
-  const float m = block_maxabs(x, plane);
-  if (threadIdx.x == 0) scales[pi] = m;
+  const float m = scales[pi];
   const float inv = m > 0.f ? (kHalf ? 32768.f : 1.f) / m : 0.f;
   unsigned short* q = dst + pi * plane;
-  for (int64_t e = threadIdx.x; e < plane; e += blockDim.x) {
+  for (int64_t e = b0 + threadIdx.x; e < b1; e += blockDim.x) {
     float v = (float)x[e] * inv;
     if (kHalf) {
       __half h = __float2half_rn(v);
@@ -68,12 +77,13 @@ template <typename T, bool kHalf>
 __global__ void __launch_bounds__(kSnapThreads) snap_dequantize(const unsigned short* __restrict__ src,
                                                                 const float* __restrict__ scales, int64_t plane,
                                                                 T* __restrict__ dst) {
-  const int64_t pi = blockIdx.x;
+  const int64_t pi = blockIdx.y, b0 = (int64_t)blockIdx.x * kSnapChunk;
+  const int64_t b1 = b0 + kSnapChunk < plane ? b0 + kSnapChunk : plane;
   const float m = scales[pi];
   const float s = kHalf ? m / 32768.f : m;
   const unsigned short* q = src + pi * plane;
   T* y = dst + pi * plane;
-  for (int64_t e = threadIdx.x; e < plane; e += blockDim.x) {
+  for (int64_t e = b0 + threadIdx.x; e < b1; e += blockDim.x) {
     unsigned short bits = q[e];
     float v;
     if (kHalf) {
@@ -96,32 +106,31 @@ __device__ __forceinline__ unsigned fp24_round(float v) {
 }
 
 template <typename T>
-__global__ void snap_q24(const T* __restrict__ src, int64_t nplanes, int64_t plane, unsigned char* __restrict__ dst) {
-  const int64_t n = nplanes * plane;
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t pi = e / plane, k = e - pi * plane;
-    const unsigned r = fp24_round((float)src[e]);
-    unsigned char* base = dst + pi * 3 * plane;
+__global__ void __launch_bounds__(kSnapThreads) snap_q24(const T* __restrict__ src, int64_t plane,
+                                                         unsigned char* __restrict__ dst) {
+  const int64_t pi = blockIdx.y, b0 = (int64_t)blockIdx.x * kSnapChunk;
+  const int64_t b1 = b0 + kSnapChunk < plane ? b0 + kSnapChunk : plane;
+  const T* x = src + pi * plane;
+  unsigned char* base = dst + pi * 3 * plane;
+  for (int64_t k = b0 + threadIdx.x; k < b1; k += blockDim.x) {
+    const unsigned r = fp24_round((float)x[k]);
     reinterpret_cast<unsigned short*>(base)[k] = (unsigned short)(r >> 16);
     base[2 * plane + k] = (unsigned char)((r >> 8) & 0xffu);
   }
 }
 
 template <typename T>
-__global__ void snap_dq24(const unsigned char* __restrict__ src, int64_t nplanes, int64_t plane, T* __restrict__ dst) {
-  const int64_t n = nplanes * plane;
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t pi = e / plane, k = e - pi * plane;
-    const unsigned char* base = src + pi * 3 * plane;
+__global__ void __launch_bounds__(kSnapThreads) snap_dq24(const unsigned char* __restrict__ src, int64_t plane,
+                                                          T* __restrict__ dst) {
+  const int64_t pi = blockIdx.y, b0 = (int64_t)blockIdx.x * kSnapChunk;
+  const int64_t b1 = b0 + kSnapChunk < plane ? b0 + kSnapChunk : plane;
+  const unsigned char* base = src + pi * 3 * plane;
+  T* y = dst + pi * plane;
+  for (int64_t k = b0 + threadIdx.x; k < b1; k += blockDim.x) {
     const unsigned r = ((unsigned)reinterpret_cast<const unsigned short*>(base)[k] << 16) |
                        ((unsigned)base[2 * plane + k] << 8);
-    dst[e] = (T)__uint_as_float(r);
+    y[k] = (T)__uint_as_float(r);
   }
-}
-
-inline unsigned snap_blocks(int64_t n) {
-  const int64_t b = (n + 255) / 256;
-  return (unsigned)(b < 152 * 32 ? (b < 1 ? 1 : b) : 152 * 32);
 }
 
 // Bytes per snapshot value of a precision (scales aside).
@@ -138,18 +147,25 @@ int snapshot_store(int prec, const T* src, int64_t nplanes, int64_t plane, unsig
                                    cudaMemcpyDeviceToDevice, st));
     return kOk;
   }
+  if (nplanes > 65535) {
+    set_error("snapshot of %lld planes: at most 65535 per store", (long long)nplanes);
+    return kBadArgument;
+  }
   if (prec == ADFWI_SNAP_FP24) {
-    ADFWI_LAUNCH(kAux, st, (snap_q24<T><<<snap_blocks(nplanes * plane), 256, 0, st>>>(src, nplanes, plane,
-                                                                                    snap + first * 3 * plane)));
+    ADFWI_LAUNCH(kAux, st, (snap_q24<T><<<snap_grid(nplanes, plane), kSnapThreads, 0, st>>>(
+                               src, plane, snap + first * 3 * plane)));
     ADFWI_CUDA_TRY(cudaGetLastError());
     return kOk;
   }
   unsigned short* q = reinterpret_cast<unsigned short*>(snap) + first * plane;
   float* sc = reinterpret_cast<float*>(scales) + first;
+  const dim3 grid = snap_grid(nplanes, plane);
+  ADFWI_CUDA_TRY(cudaMemsetAsync(sc, 0, nplanes * sizeof(float), st));  // maxima start at +0
+  ADFWI_LAUNCH(kAux, st, (snap_maxabs<T><<<grid, kSnapThreads, 0, st>>>(src, plane, reinterpret_cast<unsigned*>(sc))));
   if (prec == ADFWI_SNAP_FP16)
-    ADFWI_LAUNCH(kAux, st, (snap_quantize<T, true><<<(unsigned)nplanes, kSnapThreads, 0, st>>>(src, plane, q, sc)));
+    ADFWI_LAUNCH(kAux, st, (snap_quantize<T, true><<<grid, kSnapThreads, 0, st>>>(src, plane, q, sc)));
   else
-    ADFWI_LAUNCH(kAux, st, (snap_quantize<T, false><<<(unsigned)nplanes, kSnapThreads, 0, st>>>(src, plane, q, sc)));
+    ADFWI_LAUNCH(kAux, st, (snap_quantize<T, false><<<grid, kSnapThreads, 0, st>>>(src, plane, q, sc)));
   ADFWI_CUDA_TRY(cudaGetLastError());
   return kOk;
 }
@@ -162,18 +178,23 @@ int snapshot_load(int prec, T* dst, int64_t nplanes, int64_t plane, const unsign
                                    cudaMemcpyDeviceToDevice, st));
     return kOk;
   }
+  if (nplanes > 65535) {
+    set_error("snapshot of %lld planes: at most 65535 per load", (long long)nplanes);
+    return kBadArgument;
+  }
   if (prec == ADFWI_SNAP_FP24) {
-    ADFWI_LAUNCH(kAux, st, (snap_dq24<T><<<snap_blocks(nplanes * plane), 256, 0, st>>>(snap + first * 3 * plane,
-                                                                                     nplanes, plane, dst)));
+    ADFWI_LAUNCH(kAux, st, (snap_dq24<T><<<snap_grid(nplanes, plane), kSnapThreads, 0, st>>>(
+                               snap + first * 3 * plane, plane, dst)));
     ADFWI_CUDA_TRY(cudaGetLastError());
     return kOk;
   }
   const unsigned short* q = reinterpret_cast<const unsigned short*>(snap) + first * plane;
   const float* sc = reinterpret_cast<const float*>(scales) + first;
+  const dim3 grid = snap_grid(nplanes, plane);
   if (prec == ADFWI_SNAP_FP16)
-    ADFWI_LAUNCH(kAux, st, (snap_dequantize<T, true><<<(unsigned)nplanes, kSnapThreads, 0, st>>>(q, sc, plane, dst)));
+    ADFWI_LAUNCH(kAux, st, (snap_dequantize<T, true><<<grid, kSnapThreads, 0, st>>>(q, sc, plane, dst)));
   else
-    ADFWI_LAUNCH(kAux, st, (snap_dequantize<T, false><<<(unsigned)nplanes, kSnapThreads, 0, st>>>(q, sc, plane, dst)));
+    ADFWI_LAUNCH(kAux, st, (snap_dequantize<T, false><<<grid, kSnapThreads, 0, st>>>(q, sc, plane, dst)));
   ADFWI_CUDA_TRY(cudaGetLastError());
   return kOk;
 }

@@ -33,9 +33,50 @@ def _is_survey(s):
     return hasattr(s, "source") and hasattr(s, "receiver")
 
 
+def fold_replicate(g, top, bottom, left, right):
+    """Adjoint of edge-replicate padding by (top, bottom, left, right) cells: the padded strips
+    fold into the edge rows / columns and the corner blocks into the corner cells, with
+    fixed-order reductions (the same sums on every run)."""
+    nz, nx = g.shape[0] - top - bottom, g.shape[1] - left - right
+    r0, r1, c0, c1 = top, top + nz, left, left + nx
+    out = g[r0:r1, c0:c1].clone()
+    if top:
+        out[0, :] += g[:r0, c0:c1].sum(0)
+    if bottom:
+        out[-1, :] += g[r1:, c0:c1].sum(0)
+    if left:
+        out[:, 0] += g[r0:r1, :c0].sum(1)
+    if right:
+        out[:, -1] += g[r0:r1, c1:].sum(1)
+    if top and left:
+        out[0, 0] += g[:r0, :c0].sum()
+    if top and right:
+        out[0, -1] += g[:r0, c1:].sum()
+    if bottom and left:
+        out[-1, 0] += g[r1:, :c0].sum()
+    if bottom and right:
+        out[-1, -1] += g[r1:, c1:].sum()
+    return out
+
+
+class _PadReplicate(torch.autograd.Function):
+    """Edge-replicate padding with the fold above as its backward (PyTorch's replicate-pad
+    backward accumulates with atomics on CUDA, so its FP32 sums vary from run to run)."""
+
+    @staticmethod
+    def forward(ctx, v, top, bottom, left, right):
+        ctx.pads = (top, bottom, left, right)
+        return torch.nn.functional.pad(v[None, None], (left, right, top, bottom), mode="replicate")[0, 0]
+
+    @staticmethod
+    def backward(ctx, g):
+        return fold_replicate(g, *ctx.pads), None, None, None, None
+
+
 def _pad_replicate(v, top, bottom, left, right):
-    """Edge-replicate padding (acoustic_kernels.py:16-37, elastic_kernels.py:175-216)."""
-    return torch.nn.functional.pad(v[None, None], (left, right, top, bottom), mode="replicate")[0, 0]
+    """Edge-replicate padding (acoustic_kernels.py:16-37, elastic_kernels.py:175-216),
+    differentiable with a deterministic backward."""
+    return _PadReplicate.apply(v, top, bottom, left, right)
 
 
 class _PropagatorBase(torch.nn.Module):

@@ -156,18 +156,8 @@ def l2_misfit_grad(syn, obs_n, dt, silent_rel=0.0):
 def fold_replicate_pad(g, n):
     """Adjoint of edge-replicate padding by n cells (acoustic_kernels.py:16-37): the padded
     strips fold into the edge rows / columns and the corner blocks into the corner cells."""
-    if n == 0:
-        return g.clone()
-    out = g[n:-n, n:-n].clone()
-    out[0, :] += g[:n, n:-n].sum(0)
-    out[-1, :] += g[-n:, n:-n].sum(0)
-    out[:, 0] += g[n:-n, :n].sum(1)
-    out[:, -1] += g[n:-n, -n:].sum(1)
-    out[0, 0] += g[:n, :n].sum()
-    out[0, -1] += g[:n, -n:].sum()
-    out[-1, 0] += g[-n:, :n].sum()
-    out[-1, -1] += g[-n:, -n:].sum()
-    return out
+    from .propagator import fold_replicate
+    return fold_replicate(g, n, n, n, n)
 
 
 def _pad(v, n):

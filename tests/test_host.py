@@ -178,3 +178,22 @@ def test_batched_plan_geometry_on_the_host(native_lib):
         AcousticPlan(src_z=[1, 1, 1], src_x=[3, 9, 15], shot_model=[1, 0, 0], **kw)
     with pytest.raises(RuntimeError, match="has no shot"):
         AcousticPlan(src_z=[1, 1], src_x=[3, 9], shot_model=[0, 2], **kw)
+
+
+@pytest.mark.parametrize("pads", [(3, 2, 4, 1), (0, 5, 2, 2), (2, 0, 0, 3), (0, 0, 0, 0), (1, 1, 1, 1)])
+def test_replicate_pad_backward_is_the_fold(pads):
+    """The propagators' edge-replicate padding (acoustic_kernels.py:16-37) differentiates by
+    the explicit fold, equal to autograd through torch's replicate pad."""
+    import torch
+    from adfwi_gb300.propagator import _pad_replicate, fold_replicate
+    top, bottom, left, right = pads
+    g = torch.Generator().manual_seed(1)
+    v = torch.randn(7, 9, generator=g, dtype=torch.float64, requires_grad=True)
+    w = torch.randn(7 + top + bottom, 9 + left + right, generator=g, dtype=torch.float64)
+    ref = torch.nn.functional.pad(v[None, None], (left, right, top, bottom), mode="replicate")[0, 0]
+    (ga,) = torch.autograd.grad((ref * w).sum(), v)
+    out = _pad_replicate(v, top, bottom, left, right)
+    assert torch.equal(out, ref)
+    (gb,) = torch.autograd.grad((out * w).sum(), v)
+    assert torch.allclose(gb, ga, rtol=0, atol=1e-13)
+    assert torch.allclose(fold_replicate(w, *pads), ga, rtol=0, atol=1e-13)

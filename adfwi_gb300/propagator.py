@@ -12,7 +12,8 @@ Options beyond the reference's (all keyword-only, with reference-compatible defa
 ``snapshot_precision`` ("native", "bf16", "fp16", "fp24"), ``snapshot_every`` (steps between
 checkpoint snapshots, 0 = chosen from ``memory_budget``), ``memory_budget`` (bytes for the
 gradient workspace; default half of the free device memory when the plan is built),
-``shots_per_block`` (0 = automatic).
+``shots_per_block`` (0 = automatic); for the acoustic propagator ``ring_depth`` (TMA ring of
+the step kernels: 0 = automatic, 1 = shallow, 2 = deep; results do not depend on it).
 """
 from typing import Dict, Optional
 
@@ -155,9 +156,11 @@ class AcousticPropagator(_PropagatorBase):
 
     def __init__(self, model, survey, device: Optional[str] = "cpu", cpu_num: Optional[int] = 1,
                  gpu_num: Optional[int] = 1, dtype: torch.dtype = torch.float32, *,
-                 snapshot_precision="native", snapshot_every=0, memory_budget=None, shots_per_block=0):
+                 snapshot_precision="native", snapshot_every=0, memory_budget=None, shots_per_block=0,
+                 ring_depth=0):
         super().__init__(model, survey, device, cpu_num, gpu_num, dtype, snapshot_precision, snapshot_every,
                          memory_budget, shots_per_block)
+        self.ring_depth = int(ring_depth)
 
     def boundary_condition(self, vmax=None):
         """Damping frame of acoustic_propagator.py:102-118 (always built without a free surface)."""
@@ -182,7 +185,8 @@ class AcousticPropagator(_PropagatorBase):
                              rcv_z=self.rcv_loc[:, 1], rcv_x=self.rcv_loc[:, 0], nt=self.nt, dt=self.dt,
                              dtype=self.dtype, checkpoint_segments=checkpoint_segments,
                              snapshot_every=self.snapshot_every, snapshot_precision=self.snapshot_precision,
-                             shots_per_block=self.shots_per_block, memory_budget=self._budget())
+                             shots_per_block=self.shots_per_block, memory_budget=self._budget(),
+                             ring_depth=self.ring_depth)
             self._plans[key] = p
         return idx, p
 

@@ -410,7 +410,7 @@ def checkpointed_leg(args, dev):
         model = A.AcousticModel(0, 0, nx, nz, dx, dx, vp=vp.astype(npdt), rho=(np.power(vp, 0.25) * 310).astype(npdt),
                                 vp_grad=True, nabc=50, device=str(dev), dtype=dtype)
         prop = A.AcousticPropagator(model, sv, device=str(dev), dtype=dtype, snapshot_precision=prec,
-                                    snapshot_every=50)
+                                    snapshot_every=50, ring_depth=args.ring_depth)
         w = wts.to(dtype)
 
         def grad():
@@ -451,7 +451,9 @@ def checkpointed_leg(args, dev):
                                   "scope": "whole checkpointed gradient (forward, recompute, adjoint, snapshots)"}}
     return {"workload": "checkpointed gradient, 500x1500 model (600x1600 padded), nt=%d, snapshots every 50 steps, "
                         "%d of the 64 surface shots (every %dth), 1500 receivers" % (nt, len(idx), 64 // args.ckpt_shots),
-            "shots": len(idx), "nt": nt, "snapshot_every": 50, "results": res}
+            "shots": len(idx), "nt": nt, "snapshot_every": 50,
+            "ring": {0: "automatic (deep: padded grid >= 1400 cells wide)", 1: "shallow", 2: "deep"}[args.ring_depth],
+            "results": res}
 
 
 def plain_gpu_leg(args, dev):
@@ -753,6 +755,9 @@ def main():
                     help="skip the forward-only, checkpointed, FP64-error and plain-GPU legs")
     ap.add_argument("--ckpt-nt", type=int, default=6000, help="time steps of the checkpointed 500x1500 leg")
     ap.add_argument("--ckpt-shots", type=int, default=8, help="shots (of 64) of the checkpointed 500x1500 leg")
+    ap.add_argument("--ckpt-only", action="store_true", help="run only the checkpointed 500x1500 leg")
+    ap.add_argument("--ring-depth", type=int, default=0, choices=[0, 1, 2],
+                    help="TMA ring of the checkpointed leg's step kernels (0 = automatic, 1 shallow, 2 deep)")
     ap.add_argument("--precision", action="store_true",
                     help="run only the snapshot-precision study (BF16 / FP16 / FP32 checkpoints vs FP64)")
     ap.add_argument("--precision-nt", type=int, default=6000)
@@ -770,6 +775,11 @@ def main():
         if rank == 0:
             torch.cuda.set_device(local)
             print(json.dumps(elastic_arm(args, torch.device("cuda", local))), flush=True)
+        return
+    if args.ckpt_only:
+        if rank == 0:
+            torch.cuda.set_device(local)
+            print(json.dumps(checkpointed_leg(args, torch.device("cuda", local))), flush=True)
         return
     line = gpu_arm(args, world, rank, local)
     if world == 1 and not args.no_extra_legs:

@@ -813,3 +813,64 @@ def observed_data(server, stream):
     for (_, _, req), f in zip(stream, futs):
         req.obs = f.result().records
     return stream
+
+
+# ------------------------------------------------------------------------------------------
+# closed-loop FWI clients
+# ------------------------------------------------------------------------------------------
+FWI_CLIENTS = (((200, 600), 8, 2000), ((100, 300), 4, 1000), ((300, 900), 6, 2000), ((100, 300), 12, 2000))
+
+
+def fwi_clients(seed=0, shapes=FWI_CLIENTS, dt=1e-3, f0=10.0, nabc=50):
+    """One gradient request per client shape ((nz, nx), shots, nt): a smoothed random layered
+    starting model, its true model, evenly spaced surface shots and a receiver at every column.
+    Returns [(true_vp, request)]; ``observed_data`` fills the observed records."""
+    from .synthetic import smooth
+    rng = np.random.default_rng(seed)
+    out = []
+    for k, ((nz, nx), ns, nt) in enumerate(shapes):
+        true_vp = random_layered_vp(rng, nz, nx)
+        dx = 12.5 if nz >= 300 else 10.0
+        sx = np.linspace(0, nx - 1, ns + 2)[1:-1].round().astype(int) if ns > 1 else np.array([nx // 2])
+        req = SolveRequest(vp=smooth(true_vp, 10.0).astype(np.float32), dx=dx, nt=nt, dt=dt, f0=f0,
+                           src_z=np.full(len(sx), 2), src_x=sx, rcv_z=np.full(nx, 2), rcv_x=np.arange(nx),
+                           nabc=nabc, rid=k, meta={"shape": (nz, nx), "shots": ns, "nt": nt})
+        out.append((0.0, true_vp, req))
+    return out
+
+
+def run_fwi_clients(server, clients, iterations, step=20.0):
+    """Closed-loop FWI: every client submits a gradient solve, takes a normalised
+    steepest-descent step of ``step`` m/s (vp -= step * grad / max|grad|, kept in
+    [1000, 6000] m/s) and submits the next iteration, ``iterations`` times; the clients run
+    concurrently, one thread each. A client's requests keep their shape, so its solves reuse
+    the same batch and, from its third iteration on, replay that batch's CUDA graph. Returns
+    each client's [(loss, vp)] per iteration."""
+    import copy
+    results = [None] * len(clients)
+    errors = []
+
+    def client(k):
+        try:
+            req = copy.copy(clients[k][2])
+            hist = []
+            for _ in range(iterations):
+                res = server.submit(req).result()
+                g = res.grad
+                gm = float(np.abs(g).max())
+                vp = req.vp - (step * g / gm if gm > 0 else 0.0)
+                hist.append((res.loss, req.vp))
+                req = copy.copy(req)
+                req.vp = np.clip(vp, 1000.0, 6000.0).astype(np.float32)
+            results[k] = hist
+        except Exception as e:  # reported to the caller after every client has stopped
+            errors.append(e)
+
+    threads = [threading.Thread(target=client, args=(k,), name="fwi-client-%d" % k) for k in range(len(clients))]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    if errors:
+        raise errors[0]
+    return results

@@ -534,6 +534,8 @@ def serving_arm(args, dev):
     same = all(a.loss == b.loss and np.array_equal(a.grad, b.grad)
                for name in results for a, b in zip(results[name], ref))
     top = out["served"]["served@%g" % max(rates)]
+    if args.fwi_iterations > 0:
+        out["fwi_clients"] = fwi_clients_leg(args, dev, budget)
     out.update({"requests": args.serve_requests, "hbm_budget_gb": budget / 2 ** 30,
                 "arena_gb": round(srv.book.capacity / 2 ** 30, 2), "per_request_budget_gb": round(per_req / 2 ** 30, 2),
                 "snapshot_precision": "fp24", "bit_identical_alone_vs_mix": bool(same),
@@ -541,6 +543,37 @@ def serving_arm(args, dev):
                 "speedup_vs_one_at_a_time": round(top["throughput_gcell_per_s"]
                                                   / out["one_at_a_time"]["throughput_gcell_per_s"], 3),
                 "sample": "first %d requests of the seeded 2000-request stream" % args.serve_requests})
+    return out
+
+
+def fwi_clients_leg(args, dev, budget):
+    """Closed-loop FWI clients on the server (``serving.run_fwi_clients``): four clients with
+    fixed shapes (200x600 8 shots nt 2000, 100x300 4 shots nt 1000, 300x900 6 shots nt 2000,
+    100x300 12 shots nt 2000), each iterating gradient -> model update -> next gradient, served
+    with and without CUDA graphs. Every client's requests keep one shape, so its batches repeat
+    and, with graphs, replay from the third iteration on; the two runs give the same bits."""
+    from adfwi_gb300 import serving as S
+    clients = S.fwi_clients(seed=1)
+    with S.SolveServer(device=dev, hbm_budget=budget, slots=args.serve_slots, snapshot_precision="fp24") as srv:
+        S.observed_data(srv, clients)
+    out, hists = {}, {}
+    for graphs in (True, False):
+        with S.SolveServer(device=dev, hbm_budget=budget, slots=args.serve_slots, snapshot_precision="fp24",
+                           graphs=graphs) as srv:
+            srv.reset_stats()
+            t0 = time.perf_counter()
+            hists[graphs] = S.run_fwi_clients(srv, clients, args.fwi_iterations)
+            wall = time.perf_counter() - t0
+            st = srv.stats()
+        out["graphs" if graphs else "eager"] = {
+            "throughput_gcell_per_s": round(st["gcell_per_s"], 3), "wall_s": round(wall, 3),
+            "p50_s": round(st["p50_s"], 4), "p99_s": round(st["p99_s"], 4), "requests": st["requests"],
+            "graph_replays": st["graph_replays"], "batches": st["batches"]}
+    same = all(a[0] == b[0] and np.array_equal(a[1], b[1])
+               for ha, hb in zip(hists[True], hists[False]) for a, b in zip(ha, hb))
+    out.update({"clients": len(clients), "iterations": args.fwi_iterations, "bit_identical_graphs_vs_eager": bool(same),
+                "loss_first_last": [[round(h[0][0], 6), round(h[-1][0], 6)] for h in hists[True]],
+                "speedup_graphs_vs_eager": round(out["eager"]["wall_s"] / out["graphs"]["wall_s"], 3)})
     return out
 
 
@@ -746,6 +779,8 @@ def main():
     ap.add_argument("--serve-rates", default="10,500",
                     help="Poisson arrival rates of the served stream (1/s), comma separated")
     ap.add_argument("--serve-slots", type=int, default=4, help="concurrent solves of the server")
+    ap.add_argument("--fwi-iterations", type=int, default=8,
+                    help="iterations of the closed-loop FWI clients on the server (0 skips them)")
     ap.add_argument("--no-elastic", action="store_true", help="skip the VTI-elastic gradient measurement")
     ap.add_argument("--elastic-only", action="store_true", help="run only the VTI-elastic gradient measurement")
     ap.add_argument("--elastic-nt", type=int, default=2000,

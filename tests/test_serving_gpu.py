@@ -208,3 +208,30 @@ def test_failing_and_withdrawn_requests_leave_the_others_unchanged(native_lib):
     assert withdrawn.cancelled() and st["cancelled"] == 1 and st["requests"] == 3
     for a, b in zip((alone[0], alone[2]), got):
         assert a.loss == b.loss and np.array_equal(a.grad, b.grad)
+
+
+def test_iterating_clients_replay_graphs_and_match_eager_solves(native_lib):
+    """Closed-loop FWI clients (gradient -> model update -> next gradient): each client's
+    batches repeat, so with graphs they replay from the third iteration on, and every loss and
+    model of every iteration is bit-identical to an eager server's."""
+    clients = []
+    for seed, (nz, nx, ns, nt) in ((31, (40, 64, 3, 300)), (32, (36, 56, 2, 260))):
+        req, vp_true = _request(seed, nz, nx, ns, nt)
+        clients.append((0.0, vp_true, req))
+    hist = {}
+    for graphs in (True, False):
+        with S.SolveServer(hbm_budget=2 << 30, slots=2, snapshot_precision="native", graphs=graphs) as srv:
+            if not hist:
+                S.observed_data(srv, clients)
+            srv.reset_stats()
+            hist[graphs] = S.run_fwi_clients(srv, clients, 4, step=10.0)
+            st = srv.stats()
+        if graphs:
+            assert st["graph_replays"] >= 2 * len(clients), st
+        else:
+            assert st["graph_replays"] == 0
+    for ha, hb in zip(hist[True], hist[False]):
+        assert len(ha) == 4
+        for (la, va), (lb, vb) in zip(ha, hb):
+            assert la == lb and np.array_equal(va, vb)
+        assert ha[-1][0] < ha[0][0]  # the misfit decreases along the iterations

@@ -587,6 +587,12 @@ class SolveServer(object):
             for batch in list(self._idle.values()):
                 self.book.free(batch.off, batch.n)
             self._idle.clear()
+            if wait:
+                # the workers have stopped and every batch is done: drop the cached batches
+                # (their buffers and graphs) and the arena, so that the device memory is free for
+                # whatever comes next even while this object is still referenced
+                self._planned.clear()
+                self.arena = None
 
     def __enter__(self):
         return self

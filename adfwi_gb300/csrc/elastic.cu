@@ -275,17 +275,31 @@ __device__ __forceinline__ bool vel_fs_row(const Geo<T>& g, int i, int j) {
   return g.fsurf && j >= g.jlo && j <= g.jhi && (i == g.h - 2 || i == g.h - 3);
 }
 
+// Cells that keep split fields: inside the update region, where a PML factor differs from 1,
+// and in the rows the free-surface kernels rebuild from split parts (h-3 .. h) plus one. Every
+// other cell of the update region advances its totals directly: there the split update is
+// x' = x + a, z' = z + b, total = x' + z' (the factors are exactly 1), so the unsplit
+// t' = (t + a) + b differs only by one rounding of the sum and moves half the bytes.
+template <typename T>
+__device__ __forceinline__ bool keeps_split(const Geo<T>& g, int i, T bcx, T bcz) {
+  return bcx != T(0) || bcz != T(0) || (g.fsurf && i <= g.h + 1);
+}
+
+// tprev: stress totals at the start of the step (tt itself when the totals advance in place);
+// tt: where the new totals go.
 template <typename T, int NN>
 __global__ void stress_pml_tot(Geo<T> g, int it, const T* __restrict__ cf, const T* __restrict__ v,
-                               T* __restrict__ ts, T* __restrict__ tt, const T* __restrict__ wav) {
+                               T* __restrict__ ts, T* tt, const T* tprev, const T* __restrict__ wav) {
   griddep_wait();  // launched with programmatic serialisation in the PML time loops
   griddep_launch_dependents();
   EL_CELL_SHOTS
   const bool inside = in_I(g, i, j);
+  bool split = true;
   T pxn = T(0), pzn = T(0), pxi = T(0), pzi = T(0);
   T c11 = T(0), c13 = T(0), c15 = T(0), c33 = T(0), c35 = T(0), c55 = T(0);
   if (inside) {
     const T bcx = cf[BCX * PL + occ], bcz = cf[BCZ * PL + occ];
+    split = keeps_split(g, i, bcx, bcz);
     const T pxd = radd(T(1), rmul(g.hdt, bcx)), pzd = radd(T(1), rmul(g.hdt, bcz));
     pxn = rsub(T(1), rmul(g.hdt, bcx));
     pzn = rsub(T(1), rmul(g.hdt, bcz));
@@ -303,6 +317,30 @@ __global__ void stress_pml_tot(Geo<T> g, int it, const T* __restrict__ cf, const
     const int s = s_lo + q;
     if (s >= g.ns) break;
     const int64_t o = (int64_t)s * PL + occ;
+    if (!split) {
+      const T* vx = v;
+      const T* vz = v + NSP;
+      const T dxbm_vx = dxb<NN>(g, vx, o), dxbm_vz = dxb<NN>(g, vz, o);
+      const T dzbm_vx = dzb<NN>(g, vx, o), dzbm_vz = dzb<NN>(g, vz, o);
+      const T dxfm_vx = dxf<NN>(g, vx, o), dzfm_vx = dzf<NN>(g, vx, o);
+      const T dxfm_vz = dxf<NN>(g, vz, o), dzfm_vz = dzf<NN>(g, vz, o);
+      T xx = radd(radd(tprev[TXX * NSP + o], rmul(g.dt_dx, radd(rmul(c11, dxbm_vx), rmul(c15, dxbm_vz)))),
+                  rmul(g.dt_dz, radd(rmul(c15, dzbm_vx), rmul(c13, dzbm_vz))));
+      T zz = radd(radd(tprev[TZZ * NSP + o], rmul(g.dt_dx, radd(rmul(c13, dxbm_vx), rmul(c35, dxbm_vz)))),
+                  rmul(g.dt_dz, radd(rmul(c35, dzbm_vx), rmul(c33, dzbm_vz))));
+      T xz = radd(radd(tprev[TXZ * NSP + o], rmul(g.dt_dx, radd(rmul(c15, dxfm_vx), rmul(c55, dxfm_vz)))),
+                  rmul(g.dt_dz, radd(rmul(c55, dzfm_vx), rmul(c35, dzfm_vz))));
+      if (i == g.src_z[s] && j == g.src_x[s]) {  // -MT/2 w on both split parts: twice on the total
+        const T w = wav[(int64_t)s * g.nt + it];
+        xx = radd(xx, rmul(T(2), rmul(g.src_m[3 * s + 0], w)));
+        zz = radd(zz, rmul(T(2), rmul(g.src_m[3 * s + 1], w)));
+        xz = radd(xz, rmul(T(2), rmul(g.src_m[3 * s + 2], w)));
+      }
+      tt[TXX * NSP + o] = xx;
+      tt[TZZ * NSP + o] = zz;
+      tt[TXZ * NSP + o] = xz;
+      continue;
+    }
     T sp[6];
 #pragma unroll
     for (int k = 0; k < 6; ++k) sp[k] = ts[k * NSP + o];
@@ -362,16 +400,19 @@ __global__ void stress_fs_rows_pml(Geo<T> g, const T* __restrict__ ts, T* __rest
   tt[TXZ * NSP + o] = xz;
 }
 
+// vprev: velocity totals at the start of the step (v itself when they advance in place).
 template <typename T, int NN>
 __global__ void vel_pml_tot(Geo<T> g, const T* __restrict__ cf, const T* __restrict__ tt, T* __restrict__ vs,
-                            T* __restrict__ v) {
+                            T* v, const T* vprev) {
   griddep_wait();  // launched with programmatic serialisation in the PML time loops
   griddep_launch_dependents();
   EL_CELL_SHOTS
   const bool inside = in_I(g, i, j);
+  bool split = true;
   T pxd = T(1), pxn = T(0), pzd = T(1), pzn = T(0), dbx = T(0), dbz = T(0);
   if (inside) {
     const T bcx = cf[BCX * PL + occ], bcz = cf[BCZ * PL + occ];
+    split = keeps_split(g, i, bcx, bcz);
     pxd = radd(T(1), rmul(g.hdt, bcx));
     pxn = rsub(T(1), rmul(g.hdt, bcx));
     pzd = radd(T(1), rmul(g.hdt, bcz));
@@ -384,6 +425,17 @@ __global__ void vel_pml_tot(Geo<T> g, const T* __restrict__ cf, const T* __restr
     const int s = s_lo + q;
     if (s >= g.ns) break;
     const int64_t o = (int64_t)s * PL + occ;
+    if (!split) {
+      const T dxfm_txx = dxf<NN>(g, tt + TXX * NSP, o);
+      const T dzbm_txz = dzb<NN>(g, tt + TXZ * NSP, o);
+      const T dxbm_txz = dxb<NN>(g, tt + TXZ * NSP, o);
+      const T dzfm_tzz = dzf<NN>(g, tt + TZZ * NSP, o);
+      const T vx = radd(radd(vprev[VX * NSP + o], rdiv(rmul(dbx, dxfm_txx), g.dx)), rdiv(rmul(dbx, dzbm_txz), g.dz));
+      const T vz = radd(radd(vprev[VZ * NSP + o], rdiv(rmul(dbz, dxbm_txz), g.dx)), rdiv(rmul(dbz, dzfm_tzz), g.dz));
+      v[VX * NSP + o] = vx;
+      v[VZ * NSP + o] = vz;
+      continue;
+    }
     T sv[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) sv[k] = vs[k * NSP + o];
@@ -1272,7 +1324,8 @@ using namespace adfwi;
 struct adfwi_elastic_plan {
   adfwi_elastic_desc d;
   int nzp, nxp, NN, h, top;
-  int nstate;           // state fields per shot: PML 6 split stresses + 4 split velocities + 2 v totals, ABL 3 + 2
+  int nstate;           // state fields per shot: PML 6 split stresses + 4 split velocities + 2 v totals + 3 stress
+                        // totals, ABL 3 + 2
   int K, nseg;
   int elem;
   Layout L;
@@ -1437,7 +1490,7 @@ int esetup(const adfwi_elastic_plan* p, unsigned char* ws, const ECarve& c, cons
 // totals go; tt: where the stress totals go (PML). ABL keeps v in vin (= vout) in place.
 template <typename T, int NN>
 void estep(const adfwi_elastic_plan* p, const el::Geo<T>& g, int it, const T* cf, const T* wav, T* st, T* tt,
-           const T* vin, T* vout, cudaStream_t s) {
+           const T* tprev, const T* vin, T* vout, cudaStream_t s) {
   const dim3 gc = cells_grid(p, p->d.ns), b(el::kTileThreads);
   const int64_t NSP = (int64_t)p->d.ns * p->L.plane;
   if (p->d.pml) {
@@ -1445,12 +1498,13 @@ void estep(const adfwi_elastic_plan* p, const el::Geo<T>& g, int it, const T* cf
     T* vs = st + 6 * NSP;
     const dim3 gcs = cells_grid(p, (p->d.ns + el::kCellShots - 1) / el::kCellShots);
     // programmatically serialised launches: each kernel waits for the previous one's data
-    ADFWI_LAUNCH(kElFwdStep, s, (void)launch_pdl_kernel(el::stress_pml_tot<T, NN>, gcs, b, 0, s, g, it, cf, vin, ts, tt, wav));
+    ADFWI_LAUNCH(kElFwdStep, s,
+                 (void)launch_pdl_kernel(el::stress_pml_tot<T, NN>, gcs, b, 0, s, g, it, cf, vin, ts, tt, tprev, wav));
     if (p->d.free_surface) {
       const dim3 gfs((unsigned)((p->nxp + 127) / 128), p->d.ns, 3);
       ADFWI_LAUNCH(kElFwdStep, s, (void)launch_pdl_kernel(el::stress_fs_rows_pml<T>, gfs, dim3(128), 0, s, g, ts, tt));
     }
-    ADFWI_LAUNCH(kElFwdStep, s, (void)launch_pdl_kernel(el::vel_pml_tot<T, NN>, gcs, b, 0, s, g, cf, tt, vs, vout));
+    ADFWI_LAUNCH(kElFwdStep, s, (void)launch_pdl_kernel(el::vel_pml_tot<T, NN>, gcs, b, 0, s, g, cf, tt, vs, vout, vin));
     if (p->d.free_surface) {
       const dim3 gfs((unsigned)((p->nxp + 127) / 128), p->d.ns, 2);
       ADFWI_LAUNCH(kElFwdStep, s, (void)launch_pdl_kernel(el::vel_fs_rows_pml<T>, gfs, dim3(128), 0, s, g, vs, vout));
@@ -1469,17 +1523,25 @@ void estep(const adfwi_elastic_plan* p, const el::Geo<T>& g, int it, const T* cf
 }
 
 // Snapshot helpers: the state of a step start is (PML) 10 split fields in st + 2 velocity
-// totals, or (ABL) 3 stresses in tt + 2 velocities.
+// totals + 3 stress totals (the cells without split fields keep their state in the totals), or
+// (ABL) 3 stresses in tt + 2 velocities (nc = 0).
 template <typename T>
 int esnap(const adfwi_elastic_plan* p, bool store, unsigned char* ws, const ECarve& c, T* a, int64_t na, T* b,
-          int64_t nb, int seg, cudaStream_t s) {
+          int64_t nb, T* cc, int64_t nc, int seg, cudaStream_t s) {
   const int64_t pl = p->L.plane;
-  const int64_t first = (int64_t)seg * (na + nb);
-  int rc = store ? snapshot_store<T>(p->d.snapshot_precision, a, na, pl, ws + c.snap, ws + c.snap_scale, first, s)
-                 : snapshot_load<T>(p->d.snapshot_precision, a, na, pl, ws + c.snap, ws + c.snap_scale, first, s);
-  if (rc) return rc;
-  return store ? snapshot_store<T>(p->d.snapshot_precision, b, nb, pl, ws + c.snap, ws + c.snap_scale, first + na, s)
-               : snapshot_load<T>(p->d.snapshot_precision, b, nb, pl, ws + c.snap, ws + c.snap_scale, first + na, s);
+  const int64_t first = (int64_t)seg * (na + nb + nc);
+  T* parts[3] = {a, b, cc};
+  const int64_t n[3] = {na, nb, nc};
+  int64_t at = first;
+  for (int q = 0; q < 3; ++q) {
+    if (n[q] == 0) continue;
+    const int rc =
+        store ? snapshot_store<T>(p->d.snapshot_precision, parts[q], n[q], pl, ws + c.snap, ws + c.snap_scale, at, s)
+              : snapshot_load<T>(p->d.snapshot_precision, parts[q], n[q], pl, ws + c.snap, ws + c.snap_scale, at, s);
+    if (rc) return rc;
+    at += n[q];
+  }
+  return kOk;
 }
 
 template <typename T, int NN>
@@ -1515,14 +1577,15 @@ int eforward(const adfwi_elastic_plan* p, const void* const* coef, const int32_t
   for (int it = 0; it < nt; ++it) {
     if (grad && !full && it % K == 0) {
       if (p->d.pml)
-        rc = esnap<T>(p, true, ws, c, stt, 10 * p->d.ns, v0, 2 * p->d.ns, it / K, s);
+        rc = esnap<T>(p, true, ws, c, stt, 10 * p->d.ns, v0, 2 * p->d.ns, tt0, 3 * p->d.ns, it / K, s);
       else
-        rc = esnap<T>(p, true, ws, c, tt0, 3 * p->d.ns, v0, 2 * p->d.ns, it / K, s);
+        rc = esnap<T>(p, true, ws, c, tt0, 3 * p->d.ns, v0, 2 * p->d.ns, nullptr, 0, it / K, s);
       if (rc) return rc;
     }
     T* vin = v0;
     T* vout = v0;
     T* tt = tt0;
+    const T* tprev = tt0;  // stress totals at the start of the step
     if (full) {
       // the histories double as the state: Hv[it] = v at the start of step it, Ht[it] = T after it
       vin = it == 0 ? v0 : hv + (int64_t)it * 2 * NSP;
@@ -1530,8 +1593,9 @@ int eforward(const adfwi_elastic_plan* p, const void* const* coef, const int32_t
       if (it == 0) ADFWI_CUDA_TRY(cudaMemsetAsync(hv, 0, 2 * NSP * sizeof(T), s));
       if (it == 0) vin = hv;
       tt = p->d.pml ? ht + (int64_t)it * 3 * NSP : tt0;
+      if (p->d.pml && it > 0) tprev = ht + (int64_t)(it - 1) * 3 * NSP;
     }
-    estep<T, NN>(p, g, it, cf, wav, stt, tt, vin, vout, s);
+    estep<T, NN>(p, g, it, cf, wav, stt, tt, tprev, vin, vout, s);
     if (full && !p->d.pml) {
       // ABL: stresses evolve in tt0; keep a copy of this step's stresses for the adjoint
       ADFWI_CUDA_TRY(cudaMemcpyAsync(ht + (int64_t)it * 3 * NSP, tt0, 3 * NSP * sizeof(T), cudaMemcpyDeviceToDevice, s));
@@ -1613,16 +1677,17 @@ int ebackward(const adfwi_elastic_plan* p, const void* wavelet, const void* grec
     const int t1 = full ? nt : std::min(nt, t0 + K);
     if (!full) {
       // restore the state at t0 (v totals straight into Hv[0]) and recompute the segment
-      int rc = p->d.pml ? esnap<T>(p, false, ws, c, stt, 10 * ns, hv, 2 * ns, seg, s)
-                        : esnap<T>(p, false, ws, c, tt0, 3 * ns, hv, 2 * ns, seg, s);
+      int rc = p->d.pml ? esnap<T>(p, false, ws, c, stt, 10 * ns, hv, 2 * ns, tt0, 3 * ns, seg, s)
+                        : esnap<T>(p, false, ws, c, tt0, 3 * ns, hv, 2 * ns, nullptr, 0, seg, s);
       if (rc) return rc;
       for (int it = t0; it < t1; ++it) {
         const int k = it - t0;
         T* vin = hv + (int64_t)k * 2 * NSP;
         T* vout = k + 1 < K && it + 1 < t1 ? hv + (int64_t)(k + 1) * 2 * NSP : v0;
         T* tt = p->d.pml ? ht + (int64_t)k * 3 * NSP : tt0;
+        const T* tprev = p->d.pml && k > 0 ? ht + (int64_t)(k - 1) * 3 * NSP : tt0;
         if (!p->d.pml && vout != vin) ADFWI_CUDA_TRY(cudaMemcpyAsync(vout, vin, 2 * NSP * sizeof(T), cudaMemcpyDeviceToDevice, s));
-        estep<T, NN>(p, g, it, cf, wav, stt, tt, p->d.pml ? vin : vout, vout, s);
+        estep<T, NN>(p, g, it, cf, wav, stt, tt, tprev, p->d.pml ? vin : vout, vout, s);
         if (!p->d.pml) ADFWI_CUDA_TRY(cudaMemcpyAsync(ht + (int64_t)k * 3 * NSP, tt0, 3 * NSP * sizeof(T), cudaMemcpyDeviceToDevice, s));
       }
     }
@@ -1701,7 +1766,7 @@ int adfwi_elastic_plan_create(const adfwi_elastic_desc* desc, const int32_t* src
   p->nzp = d.nz + (d.free_surface ? d.nabc + fs_off : 2 * d.nabc + fs_off);
   p->top = d.free_surface ? fs_off : fs_off + d.nabc;
   p->elem = d.dtype == ADFWI_F64 ? 8 : 4;
-  p->nstate = d.pml ? 12 : 5;
+  p->nstate = d.pml ? 15 : 5;
   p->L = make_layout(p->nzp, p->nxp, 16, 64, p->elem);
   std::vector<int32_t>& t = p->tab;
   p->o_srcz = t.size();

@@ -14,6 +14,12 @@ checkpoint snapshots, 0 = chosen from ``memory_budget``), ``memory_budget`` (byt
 gradient workspace; default half of the free device memory when the plan is built),
 ``shots_per_block`` (0 = automatic); for the acoustic propagator ``ring_depth`` (TMA ring of
 the step kernels: 0 = automatic, 1 = shallow, 2 = deep; results do not depend on it).
+
+``device="cpu"`` (the reference's default) keeps the reference's placement: the model's
+parameters and the returned records stay on the CPU, and the solve itself runs on the current
+CUDA device (the parameters' padded coefficients are copied there and the records back, both
+differentiably, so gradients reach the CPU parameters). There is no CPU solver: without a CUDA
+device the constructor raises.
 """
 from typing import Dict, Optional
 
@@ -89,7 +95,14 @@ class _PropagatorBase(torch.nn.Module):
         if not _is_survey(survey):
             raise ValueError("survey is not an instance of Survey")
         dev = torch.device(device)
-        if dev.type != "cuda":
+        # device="cpu": CPU placement of the model and the records, the solve on the GPU
+        self._host_io = dev.type == "cpu"
+        if self._host_io:
+            if not torch.cuda.is_available():
+                raise RuntimeError("adfwi_gb300 propagators solve on a CUDA device and none is available "
+                                   "(device=%r; there is no CPU implementation)" % (device,))
+            dev = torch.device("cuda", torch.cuda.current_device())
+        elif dev.type != "cuda":
             raise RuntimeError("adfwi_gb300 propagators run on a CUDA device (got device=%r); "
                                "there is no CPU implementation" % (device,))
         if dev.index is None:
@@ -144,6 +157,14 @@ class _PropagatorBase(torch.nn.Module):
             return int(self.memory_budget)
         free, _ = torch.cuda.mem_get_info(self._dev)
         return int(0.5 * free)
+
+    def _to_solver(self, *ts):
+        """Tensors onto the solve's device (differentiable copies when they are elsewhere)."""
+        return [t if t is None or t.device == self._dev else t.to(self._dev) for t in ts]
+
+    def _to_caller(self, rec):
+        """The record dict on the caller's device (the CPU for device="cpu")."""
+        return {k: v.cpu() for k, v in rec.items()} if self._host_io else rec
 
     def _wavelet_rows(self, idx):
         if len(idx) == self.src_n and np.array_equal(idx, np.arange(self.src_n)):
@@ -211,10 +232,11 @@ class AcousticPropagator(_PropagatorBase):
         alpha1, alpha2 = self.coefficients(model)
         if alpha1.dtype != self.dtype:
             alpha1, alpha2 = alpha1.to(self.dtype), alpha2.to(self.dtype)
+        alpha1, alpha2 = self._to_solver(alpha1, alpha2)
         wav = self._wavelet_rows(idx)
         rp, ru, rw, fp, fu, fw = AcousticSolve.apply(alpha1, alpha2, self.damp, wav, plan)
-        return {"p": rp, "u": ru, "w": rw, "forward_wavefield_p": fp, "forward_wavefield_u": fu,
-                "forward_wavefield_w": fw}
+        return self._to_caller({"p": rp, "u": ru, "w": rw, "forward_wavefield_p": fp, "forward_wavefield_u": fu,
+                                "forward_wavefield_w": fw})
 
 
     def forward_l2(self, obs, model=None, shot_index=None, checkpoint_segments: int = 1, silent_rel=0.0,
@@ -236,12 +258,14 @@ class AcousticPropagator(_PropagatorBase):
         alpha1, alpha2 = self.coefficients(model)
         if alpha1.dtype != self.dtype:
             alpha1, alpha2 = alpha1.to(self.dtype), alpha2.to(self.dtype)
+        alpha1, alpha2 = self._to_solver(alpha1, alpha2)
         obs = torch.as_tensor(obs, device=self._dev)
         loss, rp, ru, rw, fp, fu, fw = AcousticL2Solve.apply(alpha1, alpha2, self.damp, self._wavelet_rows(idx), obs,
                                                              plan, float(silent_rel), bool(normalise_obs),
                                                              adjoint_source)
-        return loss, {"p": rp, "u": ru, "w": rw, "forward_wavefield_p": fp, "forward_wavefield_u": fu,
-                      "forward_wavefield_w": fw}
+        rec = self._to_caller({"p": rp, "u": ru, "w": rw, "forward_wavefield_p": fp, "forward_wavefield_u": fu,
+                               "forward_wavefield_w": fw})
+        return (loss.cpu() if self._host_io else loss), rec
 
 
 class ElasticPropagator(_PropagatorBase):
@@ -312,9 +336,10 @@ class ElasticPropagator(_PropagatorBase):
         model.forward()
         idx, plan = self.plan(shot_index, fd_order, checkpoint_segments)
         coefs, abc = self.padded_coefficients(model, fd_order)
+        coefs = self._to_solver(*coefs)
         wav = self._wavelet_rows(idx)
         outs = ElasticSolve.apply(*coefs, abc[0], abc[1], wav, plan)
         rec = {k: outs[q] for q, k in enumerate(COMPONENTS)}
         for q, k in enumerate(COMPONENTS):
             rec["forward_wavefield_" + k] = outs[5 + q]
-        return rec
+        return self._to_caller(rec)

@@ -116,3 +116,28 @@ def test_drop_in_gradients_are_bitwise_repeatable():
         egrads.append([getattr(model, par).grad.clone() for par in ("vp", "vs", "rho", "eps", "delta")])
     for a, b in zip(*egrads):
         assert torch.equal(a, b)
+
+
+def test_cpu_device_keeps_cpu_placement_and_solves_on_the_gpu():
+    """device="cpu" (the reference's default): CPU model parameters and CPU records, the solve on
+    the GPU, gradients on the CPU parameters equal to those of the same solve on cuda:0."""
+    from _cases import elastic_problem
+    out = {}
+    for dev in ("cuda:0", "cpu"):
+        model, survey, prop = acoustic_problem(A, seed=21, ns=2, nt=160, device=dev)
+        assert model.vp.device.type == torch.device(dev).type
+        rec = prop.forward()
+        assert rec["p"].device.type == torch.device(dev).type
+        w = torch.randn(rec["p"].shape, generator=torch.Generator().manual_seed(5)).to(rec["p"].device)
+        (rec["p"] * w).sum().backward()
+        out[dev] = (rec["p"].detach().cpu(), model.vp.grad.detach().cpu())
+    assert rel(out["cpu"][0], out["cuda:0"][0]) <= 1e-6 and rel(out["cpu"][1], out["cuda:0"][1]) <= 1e-5
+    eout = {}
+    for dev in ("cuda:0", "cpu"):
+        model, survey, prop = elastic_problem(A, seed=4, ns=2, nt=100, device=dev)
+        rec = prop.forward(fd_order=4)
+        assert rec["vx"].device.type == torch.device(dev).type
+        w = torch.randn(rec["vx"].shape, generator=torch.Generator().manual_seed(6)).to(rec["vx"].device)
+        (rec["vx"] * w).sum().backward()
+        eout[dev] = (rec["vx"].detach().cpu(), model.vp.grad.detach().cpu())
+    assert rel(eout["cpu"][0], eout["cuda:0"][0]) <= 1e-5 and rel(eout["cpu"][1], eout["cuda:0"][1]) <= 1e-4

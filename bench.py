@@ -474,6 +474,9 @@ def headline_checkpointed_leg(args, dev):
     out, grads = {}, {}
     for name, K, prec in (("full_history", 0, "native"), ("fp32_every_50", 50, "native"), ("fp24_every_50", 50, "fp24")):
         free, _ = torch.cuda.mem_get_info(dev)
+        # built on the starting model: the damping frame takes max(vp) at construction, as the
+        # reference's propagator does, so every run here gets the same frame
+        model.vp.data.copy_(vp0)
         prop = A.AcousticPropagator(model, survey, device=str(dev), snapshot_every=K, snapshot_precision=prec,
                                     memory_budget=int(args.memory_fraction * free))
 

@@ -141,3 +141,20 @@ def test_cpu_device_keeps_cpu_placement_and_solves_on_the_gpu():
         (rec["vx"] * w).sum().backward()
         eout[dev] = (rec["vx"].detach().cpu(), model.vp.grad.detach().cpu())
     assert rel(eout["cpu"][0], eout["cuda:0"][0]) <= 1e-5 and rel(eout["cpu"][1], eout["cuda:0"][1]) <= 1e-4
+
+
+def test_checkpointed_gradient_is_bit_identical_to_the_full_history():
+    """With native snapshots the recomputed segments replay the forward states exactly, so the
+    gradient of K < nt equals the full-history gradient bit for bit (loss through forward_l2)."""
+    res = {}
+    for K in (0, 40, 75):
+        model, survey, prop = acoustic_problem(A, seed=17, ns=6, nt=300, snapshot_every=K, memory_budget=4 << 30)
+        obs = torch.randn((prop.src_n, prop.nt, prop.rcv_n), generator=torch.Generator().manual_seed(8)).cuda()
+        model.vp.grad = None
+        loss, rec = prop.forward_l2(obs, silent_rel=1e-3, normalise_obs=True)
+        loss.backward()
+        assert prop.plan()[1].snapshot_every == (300 if K == 0 else K)
+        res[K] = (float(loss), rec["p"].detach().clone(), model.vp.grad.detach().clone())
+    for K in (40, 75):
+        assert res[K][0] == res[0][0]
+        assert torch.equal(res[K][1], res[0][1]) and torch.equal(res[K][2], res[0][2])

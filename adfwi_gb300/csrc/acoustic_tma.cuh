@@ -2,9 +2,12 @@
 // themselves are in acoustic_vec.cuh).
 //
 // Work of one launch = all (tile, shot) items of one time step. A persistent block owns a
-// contiguous range of "units" (one 16 x 64 tile x one group of at most G shots; tile-major), so
-// every accumulator a unit produces (illumination, coefficient gradients) belongs to one block
-// and is flushed once, deterministically, into the group's partial plane. The shots of a group
+// contiguous range of "units" (one 16 x 64 tile x one group of at most G shots; group-major:
+// unit u is tile u mod ntiles of group u / ntiles, so a block walks neighbouring tiles of one
+// group and reads their shared halo columns from L2 -- 2 % faster than tile-major on the
+// 600 x 1600 grid, the same elsewhere), so every accumulator a unit produces (illumination,
+// coefficient gradients) belongs to one block and is flushed once, deterministically, into the
+// group's partial plane. The shots of a group
 // share one velocity model: a batched plan solves several models of one grid shape in the same
 // launches, each with its own coefficient block and its own groups.
 //
@@ -90,7 +93,7 @@ __device__ __forceinline__ void produce(const Maps& maps, const ac::Geo<T>& g, c
   const int S = a.stages;
   int k = 0;
   for (int un = u_beg; un < u_end && !aborted(h); ++un) {
-    const int tile = un / a.ngroups, grp = un - tile * a.ngroups;
+    const int grp = un / a.ntiles, tile = un - grp * a.ntiles;
     const int i0 = g.zbeg + (tile / g.tiles_x) * TZ, j0 = (tile % g.tiles_x) * TX;
     const int x = j0 - 4 + GX;
     const int s_beg = g.grp_beg[grp], s_end = g.grp_beg[grp + 1];

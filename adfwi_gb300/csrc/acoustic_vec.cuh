@@ -121,7 +121,7 @@ __device__ __forceinline__ void relay(const ac::Geo<T>& g, const StepArgs<T>& a,
   unsigned par = 0;  // parity of each stage's next `stored` phase
   int k = 0;
   for (int un = u_beg; un < u_end && !aborted(h); ++un) {
-    const int tile = un / a.ngroups, grp = un - tile * a.ngroups;
+    const int grp = un / a.ntiles, tile = un - grp * a.ntiles;
     const int s_beg = g.grp_beg[grp], s_end = g.grp_beg[grp + 1];
     if (!relayed(tile)) {
       k += s_end - s_beg;
@@ -255,7 +255,7 @@ __global__ void __launch_bounds__(VTHREADS, MB)
   int prev_tile = -1, prev_model = -1, sel = 0, k = 0;
 
   for (int un = u_beg; un < u_end; ++un) {
-    const int tile = un / a.ngroups, sgrp = un - tile * a.ngroups;
+    const int sgrp = un / a.ntiles, tile = un - sgrp * a.ntiles;
     const int s_beg = g.grp_beg[sgrp], s_end = g.grp_beg[sgrp + 1];
     const int model = g.grp_model[sgrp];
     const int i0 = g.zbeg + (tile / g.tiles_x) * TZ, j0 = (tile % g.tiles_x) * TX;
@@ -600,7 +600,7 @@ __global__ void __launch_bounds__(VTHREADS, MB)
   int prev_tile = -1, k = 0;
 
   for (int un = u_beg; un < u_end; ++un) {
-    const int tile = un / a.ngroups, sgrp = un - tile * a.ngroups;
+    const int sgrp = un / a.ntiles, tile = un - sgrp * a.ntiles;
     const int i0 = g.zbeg + (tile / g.tiles_x) * TZ, j0 = (tile % g.tiles_x) * TX;
     const int s_beg = g.grp_beg[sgrp], s_end = g.grp_beg[sgrp + 1];
     const T* cf = a.cf + (int64_t)g.grp_model[sgrp] * a.cf_stride;

@@ -13,6 +13,10 @@ import torch
 
 from . import _native as N
 
+# snapshot_every value of boundary saving: the forward keeps the absorbing frame of every step
+# and the adjoint rebuilds the interior states backwards (no snapshots, no recomputation)
+BOUNDARY_SAVING = -1
+
 _SNAP = {"native": N.SNAP_NATIVE, "f32": N.SNAP_NATIVE, "fp32": N.SNAP_NATIVE, "float32": N.SNAP_NATIVE,
          "bf16": N.SNAP_BF16, "bfloat16": N.SNAP_BF16, "fp16": N.SNAP_FP16, "float16": N.SNAP_FP16,
          "fp24": N.SNAP_FP24, "f24": N.SNAP_FP24}
@@ -116,6 +120,21 @@ class AcousticPlan(object):
 
     def grid_shape(self):
         return (self.nz + 2 * self.nabc, self.nx + 2 * self.nabc)
+
+    def check_boundary_saving(self, damp):
+        """Boundary saving inverts the update where the damping vanishes: check that ``damp``
+        (nzp, nxp) or (nmodels, nzp, nxp) is zero on the plan's rebuilt interior and the one
+        cell beyond it that the u / w damping averages in (raises ValueError otherwise)."""
+        nzp, nxp = self.grid_shape()
+        fs = self.nabc if bool(self.desc.free_surface) else 1
+        i_lo, i_hi = max(self.nabc, fs + 1), min(self.nabc + self.nz - 2, nzp - 4)
+        j_lo, j_hi = max(self.nabc, 2), min(self.nabc + self.nx - 2, nxp - 4)
+        if i_hi < i_lo or j_hi < j_lo:
+            return
+        inner = damp[..., i_lo:i_hi + 2, j_lo:j_hi + 2]
+        if bool((inner != 0).any()):
+            raise ValueError("boundary saving needs a damping frame that vanishes inside the model "
+                             "(rows %d-%d, columns %d-%d of the padded grid)" % (i_lo, i_hi + 1, j_lo, j_hi + 1))
 
     def _model_shape(self, shape):
         """Shape of a per-model array: with a leading model axis for a batched plan."""
@@ -234,6 +253,8 @@ class AcousticSolve(torch.autograd.Function):
         damp = damp.contiguous()
         wavelet = wavelet.contiguous()
         need_grad = bool(ctx.needs_input_grad[0] or ctx.needs_input_grad[1])
+        if need_grad and plan.snapshot_every == BOUNDARY_SAVING:
+            plan.check_boundary_saving(damp)
         # records the loss does not use reach backward as None (no zero-filled adjoint sources
         # to allocate and inject)
         ctx.set_materialize_grads(False)
@@ -284,6 +305,8 @@ class AcousticL2Solve(torch.autograd.Function):
             raise ValueError("AcousticL2Solve takes a single-model plan")
         alpha1, alpha2, damp, wavelet = (t.contiguous() for t in (alpha1, alpha2, damp, wavelet))
         obs = obs.to(dtype=plan.dtype).contiguous()
+        if plan.snapshot_every == BOUNDARY_SAVING:
+            plan.check_boundary_saving(damp)
         rp, ru, rw, fp, fu, fw, ws = plan.run_forward(alpha1, alpha2, damp, wavelet, True)
         loss = plan.l2_loss(rp, obs, ws, silent_rel, normalise_obs)[0]
         ctx.plan, ctx.ws, ctx.norm, ctx.source = plan, ws, normalise_obs, adjoint_source

@@ -243,6 +243,7 @@ __global__ void mask_coefficients(Geo<T> g, T* cf) {
 
 #include "acoustic_tma.cuh"
 #include "acoustic_vec.cuh"
+#include "bsave.cuh"
 
 // ----------------------------------------------------------------------------------------
 // Plan, workspace and drivers.
@@ -268,6 +269,9 @@ struct adfwi_acoustic_plan {
   int last_chunk_start;  // first step of the reference's last checkpoint chunk
   int elem;              // bytes per element
   bool deep = false;     // deep-ring variants of the step kernels (FP32 only)
+  bool bsave = false;    // gradient by boundary saving (snapshot_every = ADFWI_SNAP_EVERY_BOUNDARY)
+  int nframe = 0;        // frame cells of a plane (boundary saving)
+  int64_t o_fidx = 0, o_foff = 0;  // tab offsets: frame index of every cell (-1: interior), frame offsets
   int nm;                // models of a batched plan (1 otherwise)
   std::vector<int> model_shot_beg;  // nm+1 offsets: the shots of each model
   std::vector<int> model_grp_beg;   // nm+1 offsets: the shot groups of each model
@@ -281,12 +285,16 @@ namespace {
 
 struct Carve {
   int64_t coef, fa, fb, ilp, ilu, tab, flag;  // forward
-  int64_t snap, snap_scale, hp, hd, la, lb, g1, g2;  // gradient extras
+  int64_t snap, snap_scale, bsv, hp, hd, la, lb, g1, g2;  // gradient extras
   int64_t mst, mpk, mnorm, mfac;                     // fused misfit: trace stats, gather peaks, norms, factors
   int64_t total;
 };
 
 int64_t align256(int64_t x) { return (x + 255) / 256 * 256; }
+
+// A gradient plan in boundary-saving mode (with a single step there is nothing to rebuild: the
+// history of that step is kept).
+bool boundary_saving(const adfwi_acoustic_plan* p) { return p->bsave && p->d.nt > 1; }
 
 Carve carve(const adfwi_acoustic_plan* p, bool grad, int K) {
   Carve c{};
@@ -303,10 +311,13 @@ Carve carve(const adfwi_acoustic_plan* p, bool grad, int K) {
   c.flag = take(256);
   if (grad) {
     const int nseg = (p->d.nt + K - 1) / K;
-    const bool full = K >= p->d.nt;
+    const bool bs = boundary_saving(p);
+    const bool full = !bs && K >= p->d.nt;
     const int64_t snap_elem = snapshot_value_bytes(p->d.snapshot_precision, p->elem);
-    c.snap = take(full ? 0 : (int64_t)nseg * 3 * ns * p->L.plane * snap_elem);
-    c.snap_scale = take(full ? 0 : (int64_t)nseg * 3 * ns * 4);
+    c.snap = take(full || bs ? 0 : (int64_t)nseg * 3 * ns * p->L.plane * snap_elem);
+    c.snap_scale = take(full || bs ? 0 : (int64_t)nseg * 3 * ns * 4);
+    // boundary saving: the frame's p, u, w after each step (slot it: the state before step it)
+    c.bsv = take(bs ? (int64_t)p->d.nt * 3 * ns * p->nframe * p->elem : 0);
     c.hp = take((int64_t)K * ns * pl);
     c.hd = take((int64_t)K * ns * pl);
     c.la = take(3 * ns * pl);
@@ -327,6 +338,7 @@ Carve carve(const adfwi_acoustic_plan* p, bool grad, int K) {
 int choose_K(const adfwi_acoustic_plan* p) {
   const int nt = p->d.nt;
   const int64_t budget = p->d.memory_budget;
+  if (p->bsave) return 1;  // one slot of divergence history, rebuilt step by step
   if (p->d.snapshot_every > 0) return std::min(p->d.snapshot_every, nt);
   if (budget <= 0) return std::min(nt, std::max(1, (int)std::ceil(std::sqrt(1.5 * nt))));
   // The whole history fits: the forward pass keeps it and no step is recomputed.
@@ -573,7 +585,8 @@ int forward_impl(const adfwi_acoustic_plan* p, const void* alpha1, const void* a
   T* ilu = reinterpret_cast<T*>(ws + c.ilu);
   int* flag = reinterpret_cast<int*>(ws + c.flag);
   const T* wav = static_cast<const T*>(wavelet);
-  const bool full = grad && K >= p->d.nt;
+  const bool bs = grad && boundary_saving(p);
+  const bool full = grad && !bs && K >= p->d.nt;
   T* hp = grad ? reinterpret_cast<T*>(ws + c.hp) : nullptr;
   T* hd = grad ? reinterpret_cast<T*>(ws + c.hd) : nullptr;
   if (full) {
@@ -583,8 +596,9 @@ int forward_impl(const adfwi_acoustic_plan* p, const void* alpha1, const void* a
   }
   T* cur = fa;
   T* nxt = fb;
+  const int64_t bslot = (int64_t)3 * ns * p->nframe;  // elements of one boundary-saving slot
   for (int it = 0; it < p->d.nt; ++it) {
-    if (grad && !full && it % K == 0) {
+    if (grad && !full && !bs && it % K == 0) {
       rc = snapshot_store<T>(p->d.snapshot_precision, cur, 3 * ns, pl, ws + c.snap, ws + c.snap_scale,
                              (int64_t)(it / K) * 3 * ns, st);
       if (rc) return rc;
@@ -602,6 +616,13 @@ int forward_impl(const adfwi_acoustic_plan* p, const void* alpha1, const void* a
                        p1, nxt + ns * pl, nxt + 2 * ns * pl, d1, static_cast<T*>(rec_p), static_cast<T*>(rec_u),
                        static_cast<T*>(rec_w), ilp, ilu, flag, st);
     if (rc) return rc;
+    if (bs && it + 1 < p->d.nt) {
+      const dim3 gs((unsigned)((p->nframe + 255) / 256), (unsigned)ns);
+      const int* foff = reinterpret_cast<const int*>(ws + c.tab) + p->o_foff;
+      ADFWI_LAUNCH(kAux, st, (ac::bs_save<T><<<gs, 256, 0, st>>>(p->L, (int)ns, p->nframe, foff, nxt,
+                                                                  reinterpret_cast<T*>(ws + c.bsv) +
+                                                                      (it + 1) * bslot)));
+    }
     std::swap(cur, nxt);
   }
   ADFWI_CUDA_TRY(cudaGetLastError());
@@ -683,7 +704,33 @@ int backward_impl(const adfwi_acoustic_plan* p, const void* wavelet, const void*
   }
   T* lcur = la;
   T* lnxt = lb;
-  const int nseg = full ? 1 : (nt + K - 1) / K;
+  if (boundary_saving(p)) {
+    // The forward left its last state in fa (nt even) or fb; rebuild the states backwards, the
+    // pressure ping-ponging between the two buffers' p planes, u and w in place.
+    T* sbuf = nt % 2 == 0 ? fa : fb;
+    T* pcur = sbuf;
+    T* poth = sbuf == fa ? fb : fa;
+    T* u = sbuf + ns * pl;
+    T* w = sbuf + 2 * ns * pl;
+    const int* fidx = reinterpret_cast<const int*>(ws + c.tab) + p->o_fidx;
+    const T* bsv = reinterpret_cast<const T*>(ws + c.bsv);
+    const int64_t bslot = (int64_t)3 * ns * p->nframe;
+    const int64_t n = (int64_t)p->nzp * p->nxp;
+    const dim3 gr((unsigned)((n + 255) / 256), (unsigned)ns);
+    for (int it = nt - 1; it >= 0; --it) {
+      const T* slot = it > 0 ? bsv + it * bslot : nullptr;
+      ADFWI_LAUNCH(kAux, st, (ac::bs_reverse_uw<T><<<gr, 256, 0, st>>>(g2, fidx, cf, pcur, u, w, slot, p->nframe)));
+      ADFWI_LAUNCH(kAux, st, (ac::bs_reverse_p<T><<<gr, 256, 0, st>>>(g2, it, fidx, cf, pcur, u, w, poth, hd, slot,
+                                                                       p->nframe, wav)));
+      rc = launch_adj<T>(p, g2, it, cf, lcur, lcur + ns * pl, lcur + 2 * ns * pl, lnxt, lnxt + ns * pl,
+                         lnxt + 2 * ns * pl, pcur, hd, gp, gu, gw, g1p, g2p, flag, st);
+      if (rc) return rc;
+      std::swap(lcur, lnxt);
+      std::swap(pcur, poth);
+    }
+    ADFWI_CUDA_TRY(cudaGetLastError());
+  }
+  const int nseg = boundary_saving(p) ? 0 : (full ? 1 : (nt + K - 1) / K);
   for (int seg = nseg - 1; seg >= 0; --seg) {
     const int t0 = full ? 0 : seg * K;
     const int t1 = full ? nt : std::min(nt, t0 + K);
@@ -1030,6 +1077,8 @@ int plan_create_impl(const adfwi_acoustic_desc* desc, const int32_t* src_z, cons
   ADFWI_CHECK_ARG(d.snapshot_precision >= 0 && d.snapshot_precision <= 3, "bad snapshot_precision");
   ADFWI_CHECK_ARG(d.checkpoint_segments >= 1, "checkpoint_segments must be >= 1");
   ADFWI_CHECK_ARG(d.ring_depth >= 0 && d.ring_depth <= 2, "ring_depth must be 0, 1 or 2");
+  ADFWI_CHECK_ARG(d.snapshot_every >= ADFWI_SNAP_EVERY_BOUNDARY,
+                  "snapshot_every must be >= 0, or ADFWI_SNAP_EVERY_BOUNDARY for boundary saving");
   ADFWI_CHECK_ARG(src_z && src_x && (d.nr == 0 || (rcv_z && rcv_x)), "null geometry array");
   adfwi_acoustic_plan* p = new (std::nothrow) adfwi_acoustic_plan();
   if (!p) {
@@ -1045,6 +1094,28 @@ int plan_create_impl(const adfwi_acoustic_desc* desc, const int32_t* src_z, cons
   p->zbeg = d.free_surface ? p->fs - 1 : 0;
   p->elem = d.dtype == ADFWI_F64 ? 8 : 4;
   p->L = make_layout(p->nzp, p->nxp, ac2::TZ, ac2::TX, p->elem);
+  p->bsave = d.snapshot_every == ADFWI_SNAP_EVERY_BOUNDARY;
+  if (p->bsave) {
+    // The interior whose update inverts exactly: the model window, inside every update region,
+    // away from the free-surface rows, and one cell short of the frame on the right and at the
+    // bottom (the u / w damping averages a cell with its right / lower neighbour). Everything
+    // else is the frame that the forward keeps step by step.
+    const int i_lo = std::max(d.nabc, p->fs + 1), i_hi = std::min(d.nabc + d.nz - 2, p->nzp - 4);
+    const int j_lo = std::max(d.nabc, 2), j_hi = std::min(d.nabc + d.nx - 2, p->nxp - 4);
+    std::vector<int32_t>& tb = p->tab;
+    p->o_fidx = tb.size();
+    tb.resize(tb.size() + (size_t)p->nzp * p->nxp, -1);
+    std::vector<int32_t> off;
+    for (int i = 0; i < p->nzp; ++i)
+      for (int j = 0; j < p->nxp; ++j)
+        if (!(i >= i_lo && i <= i_hi && j >= j_lo && j <= j_hi)) {
+          tb[p->o_fidx + (size_t)i * p->nxp + j] = (int32_t)off.size();
+          off.push_back((int32_t)p->L.off(i, j));
+        }
+    p->nframe = (int)off.size();
+    p->o_foff = tb.size();
+    tb.insert(tb.end(), off.begin(), off.end());
+  }
   // torch.chunk(wavelet, checkpoint_segments): chunks of ceil(nt / segments) steps.
   const int chunk = (d.nt + d.checkpoint_segments - 1) / d.checkpoint_segments;
   const int nchunks = (d.nt + chunk - 1) / chunk;
@@ -1151,7 +1222,7 @@ int adfwi_acoustic_workspace_bytes(const adfwi_acoustic_plan* p, int32_t with_gr
 
 int adfwi_acoustic_snapshot_every(const adfwi_acoustic_plan* p, int32_t* steps) {
   ADFWI_CHECK_ARG(p && steps, "null plan or output pointer");
-  *steps = p->K;
+  *steps = p->bsave ? ADFWI_SNAP_EVERY_BOUNDARY : p->K;
   return kOk;
 }
 

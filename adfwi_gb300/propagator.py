@@ -10,7 +10,9 @@ through the time loop.
 
 Options beyond the reference's (all keyword-only, with reference-compatible defaults):
 ``snapshot_precision`` ("native", "bf16", "fp16", "fp24"), ``snapshot_every`` (steps between
-checkpoint snapshots, 0 = chosen from ``memory_budget``), ``memory_budget`` (bytes for the
+checkpoint snapshots, 0 = chosen from ``memory_budget``; for the acoustic propagator -1 =
+boundary saving: the forward keeps the absorbing frame of every step and the adjoint rebuilds
+the interior states backwards), ``memory_budget`` (bytes for the
 gradient workspace; default half of the free device memory when the plan is built),
 ``shots_per_block`` (0 = automatic); for the acoustic propagator ``ring_depth`` (TMA ring of
 the step kernels: 0 = automatic, 1 = shallow, 2 = deep; results do not depend on it).

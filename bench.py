@@ -458,10 +458,10 @@ def checkpointed_leg(args, dev):
 
 def headline_checkpointed_leg(args, dev):
     """The headline gradient (200 x 600, 30 shots, nt = 3000, normalised L2 through forward_l2)
-    with snapshots every 50 steps and the segments recomputed in the adjoint, as a
-    memory-bounded run of the configuration would do, against the full-history gradient of the
-    headline (which the 280 GB of HBM allows): time and gradient difference, FP32 and FP24
-    snapshots."""
+    in the memory-bounded forms -- snapshots every 50 steps with the segments recomputed in the
+    adjoint (FP32 and FP24 snapshots), and boundary saving (the absorbing frame of every step
+    kept, the interior rebuilt backwards) -- against the full-history gradient of the headline
+    (which the 280 GB of HBM allows): time, workspace and gradient difference."""
     import adfwi_gb300 as A
     from adfwi_gb300.synthetic import acoustic_gradient_case
     model, survey, vp_true, vp_init = acoustic_gradient_case(seed=0, device=str(dev), nt=args.nt)
@@ -472,7 +472,9 @@ def headline_checkpointed_leg(args, dev):
         obs = (obs / torch.max(torch.abs(obs), dim=1, keepdim=True).values).contiguous()
     vp0 = torch.as_tensor(vp_init, device=dev)
     out, grads = {}, {}
-    for name, K, prec in (("full_history", 0, "native"), ("fp32_every_50", 50, "native"), ("fp24_every_50", 50, "fp24")):
+    runs = (("full_history", 0, "native"), ("fp32_every_50", 50, "native"), ("fp24_every_50", 50, "fp24"),
+            ("boundary_saving", -1, "native"))
+    for name, K, prec in runs:
         free, _ = torch.cuda.mem_get_info(dev)
         # built on the starting model: the damping frame takes max(vp) at construction, as the
         # reference's propagator does, so every run here gets the same frame
@@ -488,12 +490,14 @@ def headline_checkpointed_leg(args, dev):
 
         ms = _device_time(step, dev, 1, 2)
         grads[name] = model.vp.grad.detach().double().clone()
+        plan = prop.plan()[1]
         out[name] = {"value": round(cells / (ms * 1e-3) / 1e9, 3), "unit": UNIT, "ms_per_gradient": round(ms, 1),
-                     "snapshot_every": prop.plan()[1].snapshot_every}
+                     "snapshot_every": plan.snapshot_every,
+                     "workspace_gb": round(plan.workspace_bytes(True) / 2 ** 30, 2)}
         del prop
         torch.cuda.empty_cache()
     g0 = grads["full_history"]
-    for name in ("fp32_every_50", "fp24_every_50"):
+    for name in ("fp32_every_50", "fp24_every_50", "boundary_saving"):
         out[name]["grad_vp_rel_l2_vs_full_history"] = float((grads[name] - g0).norm() / g0.norm())
         out[name]["bit_identical_to_full_history"] = bool(torch.equal(grads[name], g0))
     return out

@@ -34,6 +34,14 @@ extern "C" {
 #define ADFWI_SNAP_FP16 2   /* float16 with one max-abs scale per snapshot, shot and field */
 #define ADFWI_SNAP_FP24 3   /* float32 rounded to a 15-bit mantissa, 3 bytes per value, no scale */
 
+/* adfwi_acoustic_desc.snapshot_every: boundary saving instead of snapshots. The forward keeps
+ * p, u, w of the absorbing frame (every cell outside the damping-free interior of the model)
+ * after every step; the adjoint rebuilds the interior states backwards by inverting the update
+ * and restores the frame. Replaces the reference's planned boundary-saving time step
+ * (ADFWI/propagator/acoustic_kernels_bs.py:40-54, 202-313); the damping must vanish in the
+ * model's interior (true of the reference's PML, Gerjan and sin^2 frames). */
+#define ADFWI_SNAP_EVERY_BOUNDARY (-1)
+
 /* Status codes. */
 #define ADFWI_OK 0
 #define ADFWI_ERR_ARGUMENT (-1)
@@ -55,7 +63,8 @@ typedef struct adfwi_acoustic_desc {
   int32_t nr;                 /* receivers, shared by all shots                              */
   int32_t dtype;              /* ADFWI_F32 / ADFWI_F64                                       */
   int32_t checkpoint_segments;/* reference chunk count; only shapes forward_wavefield_u/w    */
-  int32_t snapshot_every;     /* steps between snapshots for the gradient; 0 = automatic     */
+  int32_t snapshot_every;     /* steps between snapshots for the gradient; 0 = automatic;    */
+                              /* ADFWI_SNAP_EVERY_BOUNDARY = boundary saving                 */
   int32_t snapshot_precision; /* ADFWI_SNAP_*                                                */
   int32_t shots_per_block;    /* shots handled by one thread block; 0 = automatic            */
   double dt;                  /* time step (s)                                               */

@@ -1079,6 +1079,8 @@ int plan_create_impl(const adfwi_acoustic_desc* desc, const int32_t* src_z, cons
   ADFWI_CHECK_ARG(d.ring_depth >= 0 && d.ring_depth <= 2, "ring_depth must be 0, 1 or 2");
   ADFWI_CHECK_ARG(d.snapshot_every >= ADFWI_SNAP_EVERY_BOUNDARY,
                   "snapshot_every must be >= 0, or ADFWI_SNAP_EVERY_BOUNDARY for boundary saving");
+  ADFWI_CHECK_ARG(d.snapshot_every != ADFWI_SNAP_EVERY_BOUNDARY || nmodels == 1,
+                  "boundary saving takes a single-model plan");
   ADFWI_CHECK_ARG(src_z && src_x && (d.nr == 0 || (rcv_z && rcv_x)), "null geometry array");
   adfwi_acoustic_plan* p = new (std::nothrow) adfwi_acoustic_plan();
   if (!p) {

@@ -39,7 +39,8 @@ extern "C" {
  * after every step; the adjoint rebuilds the interior states backwards by inverting the update
  * and restores the frame. Replaces the reference's planned boundary-saving time step
  * (ADFWI/propagator/acoustic_kernels_bs.py:40-54, 202-313); the damping must vanish in the
- * model's interior (true of the reference's PML, Gerjan and sin^2 frames). */
+ * model's interior (true of the reference's PML, Gerjan and sin^2 frames). Single-model plans
+ * only. */
 #define ADFWI_SNAP_EVERY_BOUNDARY (-1)
 
 /* Status codes. */

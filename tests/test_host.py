@@ -197,3 +197,20 @@ def test_replicate_pad_backward_is_the_fold(pads):
     (gb,) = torch.autograd.grad((out * w).sum(), v)
     assert torch.allclose(gb, ga, rtol=0, atol=1e-13)
     assert torch.allclose(fold_replicate(w, *pads), ga, rtol=0, atol=1e-13)
+
+
+def test_boundary_saving_plan_on_the_host(native_lib):
+    """Boundary saving builds its frame tables on the host, reports snapshot_every = -1, sizes a
+    gradient workspace between the snapshot and the full-history ones, and refuses batched plans."""
+    from adfwi_gb300.acoustic import AcousticPlan, BOUNDARY_SAVING
+    kw = dict(nz=30, nx=40, nabc=10, free_surface=False, src_z=[2, 2], src_x=[8, 30], rcv_z=[2] * 40,
+              rcv_x=list(range(40)), nt=120, dt=1e-3, dtype=torch.float32)
+    bs = AcousticPlan(snapshot_every=BOUNDARY_SAVING, **kw)
+    assert bs.snapshot_every == BOUNDARY_SAVING
+    full = AcousticPlan(snapshot_every=120, **kw)
+    ck = AcousticPlan(snapshot_every=20, **kw)
+    assert ck.workspace_bytes(True) < bs.workspace_bytes(True) < full.workspace_bytes(True)
+    # forward only, the plans differ by the frame tables (an index per cell and the frame list)
+    assert 0 <= bs.workspace_bytes(False) - full.workspace_bytes(False) <= 4 * 2 * 50 * 60 + 512
+    with pytest.raises(RuntimeError, match="single-model"):
+        AcousticPlan(snapshot_every=BOUNDARY_SAVING, shot_model=[0, 1], **kw)

@@ -272,6 +272,7 @@ struct adfwi_acoustic_plan {
   bool bsave = false;    // gradient by boundary saving (snapshot_every = ADFWI_SNAP_EVERY_BOUNDARY)
   int nframe = 0;        // frame cells of a plane (boundary saving)
   int64_t o_fidx = 0, o_foff = 0;  // tab offsets: frame index of every cell (-1: interior), frame offsets
+  ac::BsBox bbox{0, -1, 0, -1};     // the interior the reverse pass rebuilds
   int nm;                // models of a batched plan (1 otherwise)
   std::vector<int> model_shot_beg;  // nm+1 offsets: the shots of each model
   std::vector<int> model_grp_beg;   // nm+1 offsets: the shot groups of each model
@@ -715,13 +716,13 @@ int backward_impl(const adfwi_acoustic_plan* p, const void* wavelet, const void*
     const int* fidx = reinterpret_cast<const int*>(ws + c.tab) + p->o_fidx;
     const T* bsv = reinterpret_cast<const T*>(ws + c.bsv);
     const int64_t bslot = (int64_t)3 * ns * p->nframe;
-    const int64_t n = (int64_t)p->nzp * p->nxp;
-    const dim3 gr((unsigned)((n + 255) / 256), (unsigned)ns);
+    const dim3 gb(32, 8), gr((unsigned)((p->nxp + 31) / 32), (unsigned)((p->nzp + 7) / 8), (unsigned)ns);
     for (int it = nt - 1; it >= 0; --it) {
       const T* slot = it > 0 ? bsv + it * bslot : nullptr;
-      ADFWI_LAUNCH(kAux, st, (ac::bs_reverse_uw<T><<<gr, 256, 0, st>>>(g2, fidx, cf, pcur, u, w, slot, p->nframe)));
-      ADFWI_LAUNCH(kAux, st, (ac::bs_reverse_p<T><<<gr, 256, 0, st>>>(g2, it, fidx, cf, pcur, u, w, poth, hd, slot,
-                                                                       p->nframe, wav)));
+      ADFWI_LAUNCH(kAux, st, (ac::bs_reverse_uw<T><<<gr, gb, 0, st>>>(g2, p->bbox, fidx, cf, pcur, u, w, slot,
+                                                                      p->nframe)));
+      ADFWI_LAUNCH(kAux, st, (ac::bs_reverse_p<T><<<gr, gb, 0, st>>>(g2, p->bbox, it, fidx, cf, pcur, u, w, poth, hd,
+                                                                     slot, p->nframe, wav)));
       rc = launch_adj<T>(p, g2, it, cf, lcur, lcur + ns * pl, lcur + 2 * ns * pl, lnxt, lnxt + ns * pl,
                          lnxt + 2 * ns * pl, pcur, hd, gp, gu, gw, g1p, g2p, flag, st);
       if (rc) return rc;
@@ -1104,6 +1105,7 @@ int plan_create_impl(const adfwi_acoustic_desc* desc, const int32_t* src_z, cons
     // else is the frame that the forward keeps step by step.
     const int i_lo = std::max(d.nabc, p->fs + 1), i_hi = std::min(d.nabc + d.nz - 2, p->nzp - 4);
     const int j_lo = std::max(d.nabc, 2), j_hi = std::min(d.nabc + d.nx - 2, p->nxp - 4);
+    p->bbox = ac::BsBox{i_lo, i_hi, j_lo, j_hi};
     std::vector<int32_t>& tb = p->tab;
     p->o_fidx = tb.size();
     tb.resize(tb.size() + (size_t)p->nzp * p->nxp, -1);

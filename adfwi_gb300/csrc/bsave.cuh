@@ -16,13 +16,20 @@
 // absorbing frame (not a strip of stencil width), so the PML cells' states, which the
 // gradient of the padded coefficients needs, are the forward's own.
 //
-// Saved slot layout: [field p, u, w][shot][frame cell], frame cells listed by plane offset.
+// Saved slot layout: [field p, u, w][shot][frame cell], frame cells listed by plane offset. The
+// reverse kernels run over 32 x 8 cell tiles of one shot (grid x: columns, y: rows, z: shots);
+// the interior is the box [ilo, ihi] x [jlo, jhi], and only frame cells read their index.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
 
 namespace adfwi {
 namespace ac {
+
+struct BsBox {
+  int ilo, ihi, jlo, jhi;
+  __device__ __forceinline__ bool interior(int i, int j) const { return i >= ilo && i <= ihi && j >= jlo && j <= jhi; }
+};
 
 template <typename T>
 __global__ void bs_save(Layout L, int ns, int nframe, const int* __restrict__ frame_off, const T* __restrict__ st,
@@ -38,18 +45,16 @@ __global__ void bs_save(Layout L, int ns, int nframe, const int* __restrict__ fr
 // u, w before step it, from p', u', w' after it (u, w in place); frame cells from the slot kept
 // after step it-1 (zero before the first step: slot == nullptr).
 template <typename T>
-__global__ void bs_reverse_uw(Geo<T> g, const int* __restrict__ fidx, const T* __restrict__ cf,
+__global__ void bs_reverse_uw(Geo<T> g, BsBox box, const int* __restrict__ fidx, const T* __restrict__ cf,
                               const T* __restrict__ pn, T* __restrict__ u, T* __restrict__ w,
                               const T* __restrict__ slot, int nframe) {
-  const int64_t n = (int64_t)g.L.nzp * g.L.nxp;
-  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  const int s = blockIdx.y;
-  if (e >= n) return;
-  const int i = (int)(e / g.L.nxp), j = (int)(e - (int64_t)i * g.L.nxp);
+  const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y * blockDim.y + threadIdx.y;
+  const int s = blockIdx.z;
+  if (i >= g.L.nzp || j >= g.L.nxp) return;
   const int64_t PL = g.L.plane, P = g.L.pitch;
   const int64_t oc = g.L.off(i, j), o = (int64_t)s * PL + oc;
-  const int k = fidx[e];
-  if (k >= 0) {
+  if (!box.interior(i, j)) {
+    const int k = fidx[(int64_t)i * g.L.nxp + j];
     u[o] = slot ? slot[((int64_t)1 * g.ns + s) * nframe + k] : T(0);
     w[o] = slot ? slot[((int64_t)2 * g.ns + s) * nframe + k] : T(0);
     return;
@@ -63,15 +68,13 @@ __global__ void bs_reverse_uw(Geo<T> g, const int* __restrict__ fidx, const T* _
 // p before step it into pp, and the divergence of (u, w) that step it used into dh (the
 // forward's operation order, zero outside the p update region, as the forward keeps it).
 template <typename T>
-__global__ void bs_reverse_p(Geo<T> g, int it, const int* __restrict__ fidx, const T* __restrict__ cf,
+__global__ void bs_reverse_p(Geo<T> g, BsBox box, int it, const int* __restrict__ fidx, const T* __restrict__ cf,
                              const T* __restrict__ pn, const T* __restrict__ u, const T* __restrict__ w,
                              T* __restrict__ pp, T* __restrict__ dh, const T* __restrict__ slot, int nframe,
                              const T* __restrict__ wav) {
-  const int64_t n = (int64_t)g.L.nzp * g.L.nxp;
-  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  const int s = blockIdx.y;
-  if (e >= n) return;
-  const int i = (int)(e / g.L.nxp), j = (int)(e - (int64_t)i * g.L.nxp);
+  const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y * blockDim.y + threadIdx.y;
+  const int s = blockIdx.z;
+  if (i >= g.L.nzp || j >= g.L.nxp) return;
   const int64_t PL = g.L.plane, P = g.L.pitch;
   const int64_t oc = g.L.off(i, j), o = (int64_t)s * PL + oc;
   T dv = T(0);
@@ -81,8 +84,8 @@ __global__ void bs_reverse_p(Geo<T> g, int it, const int* __restrict__ fidx, con
     dv = radd(rmul(g.c1, t1), rmul(g.c2, t2));
   }
   dh[o] = dv;
-  const int k = fidx[e];
-  if (k >= 0) {
+  if (!box.interior(i, j)) {
+    const int k = fidx[(int64_t)i * g.L.nxp + j];
     pp[o] = slot ? slot[(int64_t)s * nframe + k] : T(0);
     return;
   }

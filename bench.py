@@ -804,8 +804,22 @@ def reference_arm(args):
             "data": "synthetic (seeded layered/faulted model, Ricker sources)",
             "config": {"workload": WORKLOAD, "sample": sample},
             "cpu_baseline": {"value": round(value, 5), "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": sample},
+                             "sample": sample, "port_vs_reference_cpu": port_vs_reference()},
             "e2e": {"value": round(value, 5), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def port_vs_reference():
+    """The committed timing of the reference's own CPU propagator against this port on the same
+    slice and threads (tests/golden/cpu_timing_ref_vs_port.json; the reference itself cannot run
+    where the benchmark does), or None."""
+    path = os.path.join(ROOT, "tests", "golden", "cpu_timing_ref_vs_port.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return {"port_over_reference_speed": d["port_over_reference_speed"], "threads": d["threads"],
+                "machine": d["machine"], "sample": d["sample"]}
+    except Exception:
+        return None
 
 
 def main():

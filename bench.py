@@ -906,7 +906,7 @@ def main():
             t_all += t
             reps += 1
         line["cpu_baseline"] = {"value": round(done / t_all / 1e9, 5), "unit": UNIT, "cores": threads,
-                                "kind": "port",
+                                "kind": "port", "port_vs_reference_cpu": port_vs_reference(),
                                 "sample": "%d x (1 shot x %d steps) of the 300x700 padded gradient workload, CPU "
                                           "oracle forward + autograd backward, %.1f s" % (reps, args.cpu_sample_steps,
                                                                                           t_all)}

@@ -40,7 +40,8 @@ extern "C" {
  * and restores the frame. Replaces the reference's planned boundary-saving time step
  * (ADFWI/propagator/acoustic_kernels_bs.py:40-54, 202-313); the damping must vanish in the
  * model's interior (true of the reference's PML, Gerjan and sin^2 frames). Single-model plans
- * only. */
+ * only. The backward rebuilds the states in the workspace it was given, consuming the forward's
+ * last state: run the forward again before another backward. */
 #define ADFWI_SNAP_EVERY_BOUNDARY (-1)
 
 /* Status codes. */

@@ -759,29 +759,120 @@ __global__ void adj_tq(Geo<T> g, const T* __restrict__ cf, const T* __restrict__
   q4[3 * NSP + o] = d;
 }
 
-// (B3a) lt = transposes of the velocity update's stress differences (the dL/d stress records
-// of the step are added after it, by adj_inject); bx, bz gradients.
-// Staged planes per shot: 0 q_vxx (x), 1 q_vxz (z), 2 q_vzx (x), 3 q_vzz (z), 4 txx (x),
-// 5 txz (x, z), 6 tzz (z) of the forward history, 7-10 lambda of the split velocities.
-constexpr int kAdjTPlanes = 11;
+// (B4 + B3a) per shot group: the split velocities' lambda after the step (the velocity
+// free-surface adjoint, then S * lambda + lambda of the totals; read from lvs_in, written to
+// lvs_out, so that no block reads a halo cell another block has already advanced), lt = the
+// transposes of the velocity update's stress differences (the dL/d stress records of the step
+// are added after it, by adj_inject), and the bx, bz gradients. The update's adjoint sources q
+// (lambda of the split velocities times dt b / (d pml_d), zero outside I) are formed in shared
+// memory where the transposes read them. Per block the tile's factors are formed once with the
+// halo (S and dt b / (d pml_d); x factors on compact x planes, z factors on compact z planes).
+// Per shot, the lambda of the four split velocities (x parts on compact x planes, z parts on
+// compact z planes), the lambda of the velocity totals and txx, txz, tzz of the forward history
+// (full planes) are staged into one of two buffers -- the next shot's copies are in flight while
+// a shot is evaluated. Each thread then advances the lambda of its own cell (kept in registers
+// for the gradients, stored for the next step) and of at most one halo cell, and turns the
+// staged lambda into q in place; the transposes and gradients follow. 43.9 KB of shared memory
+// in single precision.
+constexpr int kAdjTShot = 2 * kXPlane + 2 * kZPlane + 5 * kSPlane;     // one shot's staged planes
+constexpr int kAdjTElems = 3 * kXPlane + 3 * kZPlane + 2 * kAdjTShot;  // factors; two shot buffers
+constexpr int kXHalo = kTileZ * 8, kZHalo = 6 * kTileX;  // halo cells of the compact x / z planes
+static_assert(kXHalo + kZHalo == kTileThreads, "one halo cell per thread");
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait_group() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
 template <typename T, int NN>
-__global__ void __launch_bounds__(kTileThreads)
-    adj_t_pml(Geo<T> g, const T* __restrict__ cf, const T* __restrict__ lvs, const T* __restrict__ q4,
-              T* __restrict__ lt, const T* __restrict__ tt_hist, T* __restrict__ gpart, int eg) {
+__global__ void __launch_bounds__(kTileThreads, sizeof(T) == 4 ? 5 : 2)
+    adj_t_pml(Geo<T> g, const T* __restrict__ cf, const T* __restrict__ lv, const T* __restrict__ lvs_in,
+              T* __restrict__ lvs_out, T* __restrict__ lt, const T* __restrict__ tt_hist, T* __restrict__ gpart,
+              int eg) {
   griddep_wait();  // launched with programmatic serialisation in the PML time loops
   griddep_launch_dependents();
   extern __shared__ __align__(16) unsigned char el_smem[];
-  T* sm = reinterpret_cast<T*>(el_smem);
+  T* sFx = reinterpret_cast<T*>(el_smem);  // S_x, dt bx / (dx pml_xd), dt bz / (dx pml_xd) (x planes)
+  T* sFz = sFx + 3 * kXPlane;              // S_z, dt bx / (dz pml_zd), dt bz / (dz pml_zd) (z planes)
+  T* sB = sFz + 3 * kZPlane;               // two shot buffers
+  // a shot buffer: lambda vx_x, vz_x (x planes; q_vxx, q_vzx once formed), lambda vx_z, vz_z (z
+  // planes; q_vxz, q_vzz), lambda of the totals vx, vz, txx, txz, tzz (full planes)
+  constexpr int oLz = 2 * kXPlane, oV = oLz + 2 * kZPlane, oT = oV + 2 * kSPlane;
   const int tiles_x = (g.L.nxp + kTileX - 1) / kTileX;
   const int i0 = ((int)blockIdx.x / tiles_x) * kTileZ, j0 = ((int)blockIdx.x % tiles_x) * kTileX;
   const int ty = (int)threadIdx.x / kTileX, tx = (int)threadIdx.x % kTileX;
   const int i = i0 + ty, j = j0 + tx;
   const bool valid = i < g.L.nzp && j < g.L.nxp, inside = valid && in_I(g, i, j);
   const int64_t PL = g.L.plane, NSP = (int64_t)g.ns * PL, oc = g.L.off(i, j);
-  const int sc = kSC + ty * kSW + tx;  // this cell in a staged plane
+  const int sc = kSC + ty * kSW + tx, cx = ty * kSW + tx + 4, cz = (ty + 3) * kTileX + tx;
+  // this thread's halo cell: x-plane columns j0-4 .. j0-1 and j0+32 .. j0+35, or z-plane rows
+  // i0-3 .. i0-1 and i0+8 .. i0+10
+  const bool hx = (int)threadIdx.x < kXHalo;
+  int hr, hc;  // the halo cell's row and column relative to (i0, j0)
+  if (hx) {
+    const int c8 = (int)threadIdx.x & 7;
+    hr = (int)threadIdx.x >> 3;
+    hc = c8 < 4 ? c8 - 4 : c8 + kTileX - 4;
+  } else {
+    const int t = (int)threadIdx.x - kXHalo, r6 = t / kTileX;
+    hr = r6 < 3 ? r6 - 3 : r6 + kTileZ - 3;
+    hc = t - r6 * kTileX;
+  }
+  const int hi = i0 + hr, hj = j0 + hc;
+  const bool hvalid = hi >= 0 && hi < g.L.nzp && hj >= 0 && hj < g.L.nxp;
+  const int hs = hx ? hr * kSW + hc + 4 : (hr + 3) * kTileX + hc;  // in its compact plane
+  const int hf = (hr + 3) * kSW + hc + 4;                            // in a full plane
   EL_SHOT_GROUP
   T* gbx = gbase + 6 * PL;
   T* gbz = gbase + 7 * PL;
+  const T* lvx = lv + VX * NSP;
+  const T* lvz = lv + VZ * NSP;
+  auto issue = [&](int s, T* B) {
+    const int64_t so = (int64_t)s * PL;
+    stage_x(B, lvs_in + VX_X * NSP + so, g.L, i0, j0);
+    stage_x(B + kXPlane, lvs_in + VZ_X * NSP + so, g.L, i0, j0);
+    stage_z(B + oLz, lvs_in + VX_Z * NSP + so, g.L, i0, j0);
+    stage_z(B + oLz + kZPlane, lvs_in + VZ_Z * NSP + so, g.L, i0, j0);
+    stage(B + oV, lvx + so, g.L, i0, j0, 3, 4);
+    stage(B + oV + kSPlane, lvz + so, g.L, i0, j0, 3, 4);
+    stage(B + oT, tt_hist + TXX * NSP + so, g.L, i0, j0, 0, 4);
+    stage(B + oT + kSPlane, tt_hist + TXZ * NSP + so, g.L, i0, j0, 3, 4);
+    stage(B + oT + 2 * kSPlane, tt_hist + TZZ * NSP + so, g.L, i0, j0, 3, 0);
+    cp_async_commit();
+  };
+  if (s_beg < s_end) issue(s_beg, sB);
+  // the factors, formed as the per-cell adjoint forms them (S = 1 and the source factors zero
+  // outside I), while the first shot's copies land
+  for (int t = threadIdx.x; t < kXPlane; t += kTileThreads) {
+    const int ii = i0 + t / kSW, jj = j0 - 4 + t % kSW;
+    T sx = T(1), fx = T(0), fz = T(0);
+    if (in_I(g, ii, jj)) {
+      const int64_t c0 = g.L.off(ii, jj);
+      const Pml<T> p = pml_at(g, cf, c0, PL);
+      const T ix = T(1) / p.xd, kx = g.dt_dx * ix;
+      sx = p.xn * ix;
+      fx = cf[BX * PL + c0] * kx;
+      fz = cf[BZ * PL + c0] * kx;
+    }
+    sFx[t] = sx;
+    sFx[kXPlane + t] = fx;
+    sFx[2 * kXPlane + t] = fz;
+  }
+  for (int t = threadIdx.x; t < kZPlane; t += kTileThreads) {
+    const int ii = i0 - 3 + t / kTileX, jj = j0 + t % kTileX;
+    T sz = T(1), fx = T(0), fz = T(0);
+    if (in_I(g, ii, jj)) {
+      const int64_t c0 = g.L.off(ii, jj);
+      const Pml<T> p = pml_at(g, cf, c0, PL);
+      const T iz = T(1) / p.zd, kz = g.dt_dz * iz;
+      sz = p.zn * iz;
+      fx = cf[BX * PL + c0] * kz;
+      fz = cf[BZ * PL + c0] * kz;
+    }
+    sFz[t] = sz;
+    sFz[kZPlane + t] = fx;
+    sFz[2 * kZPlane + t] = fz;
+  }
+  // (the barrier after the first shot's copies orders these writes before their reads)
   // d(v_x')/d(bx) = dt * D(T) / (d * pml_d), likewise for bz: the cell's factors dt / (d pml_d)
   T kx = T(0), kz = T(0), gx = T(0), gz = T(0);
   if (inside) {
@@ -789,35 +880,72 @@ __global__ void __launch_bounds__(kTileThreads)
     kx = g.dt / (g.dx * p.xd);
     kz = g.dt / (g.dz * p.zd);
   }
-  const StagedQ<T> q_vxx{sm, i0, j0}, q_vxz{sm + kSPlane, i0, j0};
-  const StagedQ<T> q_vzx{sm + 2 * kSPlane, i0, j0}, q_vzz{sm + 3 * kSPlane, i0, j0};
+  // rows whose totals' lambda the velocity free-surface adjoint combines across cells
+  const int fs_lo = g.fsurf ? g.h - 3 : 1 << 30, fs_hi = g.fsurf ? g.h : -1;
+  auto q_of = [](T v, T f) { return f != T(0) ? v * f : T(0); };
   for (int s = s_beg; s < s_end; ++s) {
+    T* B = sB + ((s - s_beg) & 1) * kAdjTShot;
+    if (s + 1 < s_end) {
+      issue(s + 1, sB + ((s + 1 - s_beg) & 1) * kAdjTShot);  // into the buffer the previous shot used
+      cp_async_wait_group<1>();
+    } else {
+      cp_async_wait_group<0>();
+    }
+    __syncthreads();
     const int64_t so = (int64_t)s * PL;
-    stage(sm, q4 + so, g.L, i0, j0, 0, 4);
-    stage(sm + kSPlane, q4 + NSP + so, g.L, i0, j0, 3, 0);
-    stage(sm + 2 * kSPlane, q4 + 2 * NSP + so, g.L, i0, j0, 0, 4);
-    stage(sm + 3 * kSPlane, q4 + 3 * NSP + so, g.L, i0, j0, 3, 0);
-    stage(sm + 4 * kSPlane, tt_hist + TXX * NSP + so, g.L, i0, j0, 0, 4);
-    stage(sm + 5 * kSPlane, tt_hist + TXZ * NSP + so, g.L, i0, j0, 3, 4);
-    stage(sm + 6 * kSPlane, tt_hist + TZZ * NSP + so, g.L, i0, j0, 3, 0);
-#pragma unroll
-    for (int k = 0; k < 4; ++k) stage(sm + (7 + k) * kSPlane, lvs + k * NSP + so, g.L, i0, j0, 0, 0);
-    cp_async_wait_all();
+    T* sLx = B;
+    T* sLz = B + oLz;
+    // own cell: lambda after the step (cells outside the grid keep their zero), stored; q
+    T vxx = sLx[cx], vzx = sLx[kXPlane + cx], vxz = sLz[cz], vzz = sLz[kZPlane + cz];
+    if (valid) {
+      const int64_t o = so + oc;
+      T ax = B[oV + sc], az = B[oV + kSPlane + sc];
+      if (i >= fs_lo && i <= fs_hi) vfs_adjoint(g, lvx, lvz, i, j, o, ax, az);
+      const T sx = sFx[cx], sz = sFz[cz];
+      vxx = sx * vxx + ax;
+      vzx = sx * vzx + az;
+      vxz = sz * vxz + ax;
+      vzz = sz * vzz + az;
+      lvs_out[VX_X * NSP + o] = vxx;
+      lvs_out[VZ_X * NSP + o] = vzx;
+      lvs_out[VX_Z * NSP + o] = vxz;
+      lvs_out[VZ_Z * NSP + o] = vzz;
+    }
+    sLx[cx] = q_of(vxx, sFx[kXPlane + cx]);
+    sLx[kXPlane + cx] = q_of(vzx, sFx[2 * kXPlane + cx]);
+    sLz[cz] = q_of(vxz, sFz[kZPlane + cz]);
+    sLz[kZPlane + cz] = q_of(vzz, sFz[2 * kZPlane + cz]);
+    // halo cell: lambda after the step (not stored: another block owns the cell); q
+    {
+      T* hl = hx ? sLx + hs : sLz + hs;
+      const int HP = hx ? kXPlane : kZPlane;
+      const T* hF = hx ? sFx + hs : sFz + hs;
+      T va = hl[0], vb = hl[HP];
+      if (hvalid) {
+        T ax = B[oV + hf], az = B[oV + kSPlane + hf];
+        if (hi >= fs_lo && hi <= fs_hi) vfs_adjoint(g, lvx, lvz, hi, hj, so + g.L.off(hi, hj), ax, az);
+        const T sh = hF[0];
+        va = sh * va + ax;
+        vb = sh * vb + az;
+      }
+      hl[0] = q_of(va, hF[HP]);
+      hl[HP] = q_of(vb, hF[2 * HP]);
+    }
     __syncthreads();
     if (valid) {
+      const StagedX<T> q_vxx{sLx, i0, j0}, q_vzx{sLx + kXPlane, i0, j0};
+      const StagedZ<T> q_vxz{sLz, i0, j0}, q_vzz{sLz + kZPlane, i0, j0};
+      const T* sT = B + oT;
       const int64_t o = so + oc;
       lt[TXX * NSP + o] = dxf_t<NN>(g, q_vxx, i, j);
       lt[TXZ * NSP + o] = dzb_t<NN>(g, q_vxz, i, j) + dxb_t<NN>(g, q_vzx, i, j);
       lt[TZZ * NSP + o] = dzf_t<NN>(g, q_vzz, i, j);
       if (inside) {
-        const T* lv = sm + 7 * kSPlane + sc;
-        gx += lv[VX_X * kSPlane] * dxf<NN>(g, sm + 4 * kSPlane, sc) * kx +
-              lv[VX_Z * kSPlane] * dzb<NN>(g, sm + 5 * kSPlane, sc, kSW) * kz;
-        gz += lv[VZ_X * kSPlane] * dxb<NN>(g, sm + 5 * kSPlane, sc) * kx +
-              lv[VZ_Z * kSPlane] * dzf<NN>(g, sm + 6 * kSPlane, sc, kSW) * kz;
+        gx += vxx * dxf<NN>(g, sT, sc) * kx + vxz * dzb<NN>(g, sT + kSPlane, sc, kSW) * kz;
+        gz += vzx * dxb<NN>(g, sT + kSPlane, sc) * kx + vzz * dzf<NN>(g, sT + 2 * kSPlane, sc, kSW) * kz;
       }
     }
-    __syncthreads();  // the next shot's copies overwrite the staged planes
+    __syncthreads();  // this buffer is refilled by the copies of the shot after next
   }
   if (inside) {
     gbx[oc] += gx;
@@ -925,48 +1053,6 @@ __global__ void adj_vq(Geo<T> g, const T* __restrict__ cf, const T* __restrict__
   for (int k = 0; k < 8; ++k) q8[k * NSP + o] = v[k];
 }
 
-// (B4 + B3q) fused per cell and shot: the split velocities' lambda after the step (adj_vfs_pml)
-// and, from those new values, the velocity update's adjoint sources (adj_tq, PML form).
-template <typename T>
-__global__ void adj_vfs_tq_pml(Geo<T> g, const T* __restrict__ cf, const T* __restrict__ lv, T* lvs,
-                               T* __restrict__ q4) {
-  griddep_wait();  // launched with programmatic serialisation in the PML time loops
-  griddep_launch_dependents();
-  EL_CELL_SHOTS
-  const bool inside = in_I(g, i, j);
-  T sx = T(1), sz = T(1), kbx_x = T(0), kbx_z = T(0), kbz_x = T(0), kbz_z = T(0);
-  if (inside) {
-    const Pml<T> p = pml_at(g, cf, occ, PL);
-    const T ix = T(1) / p.xd, iz = T(1) / p.zd;  // the adjoint needs no bit-exact rounding
-    sx = p.xn * ix;
-    sz = p.zn * iz;
-    const T bx = cf[BX * PL + occ], bz = cf[BZ * PL + occ];
-    const T kx = g.dt_dx * ix, kz = g.dt_dz * iz;
-    kbx_x = bx * kx;
-    kbx_z = bx * kz;
-    kbz_x = bz * kx;
-    kbz_z = bz * kz;
-  }
-#pragma unroll
-  for (int q = 0; q < kCellShots; ++q) {
-    const int s = s_lo + q;
-    if (s >= g.ns) break;
-    const int64_t o = (int64_t)s * PL + occ;
-    T ax, az;
-    vfs_adjoint(g, lv + VX * NSP, lv + VZ * NSP, i, j, o, ax, az);
-    const T vxx = sx * lvs[VX_X * NSP + o] + ax, vxz = sz * lvs[VX_Z * NSP + o] + ax;
-    const T vzx = sx * lvs[VZ_X * NSP + o] + az, vzz = sz * lvs[VZ_Z * NSP + o] + az;
-    lvs[VX_X * NSP + o] = vxx;
-    lvs[VX_Z * NSP + o] = vxz;
-    lvs[VZ_X * NSP + o] = vzx;
-    lvs[VZ_Z * NSP + o] = vzz;
-    q4[0 * NSP + o] = inside ? vxx * kbx_x : T(0);  // zero outside I
-    q4[1 * NSP + o] = inside ? vxz * kbx_z : T(0);
-    q4[2 * NSP + o] = inside ? vzx * kbz_x : T(0);
-    q4[3 * NSP + o] = inside ? vzz * kbz_z : T(0);
-  }
-}
-
 // (B1a) lambda of the velocity totals at the start of the step (overwrite) and the C gradients.
 // pml = 1: split-field update; pml = 0: absorbing-layer update (lts then holds txx, tzz, txz,
 // and lv is accumulated instead of overwritten because v' = v + ...).
@@ -1053,28 +1139,34 @@ __global__ void __launch_bounds__(kTileThreads)
 
 // (B1a, PML) lambda of the velocity totals at the start of the step (overwrite) and the C
 // gradients, with the stress update's adjoint sources formed in shared memory. Per block the
-// tile's cell coefficients C11 .. C55 and PML factors dt/dx / pml_xd, dt/dz / pml_zd (zero outside
-// I) are staged once with the full halo; per shot the lambda of the six split stresses and vx, vz
-// of the forward history are staged, the eight sources q (sx_b, sx_zb, sx_f, sx_zf, sz_b, sz_zb,
-// sz_f, sz_zf: coefficient-weighted lambda, zero outside I) formed where their differences read
-// them, and the transposes and gradients evaluated from them. C, the factors, vx and vz are full
-// staged planes; the x parts of lambda and the sources of x differences are compact x planes,
-// the z ones compact z planes (43.9 KB in single precision: 5 blocks per SM).
-constexpr int kAdjVPmlElems = 10 * kSPlane + 7 * kXPlane + 7 * kZPlane;  // C, factors, vx, vz; lambda, q
+// tile's cell coefficients C11 .. C55 (full planes, with the halo) are staged once and the PML
+// factors dt/dx / pml_xd (compact x plane) and dt/dz / pml_zd (compact z plane; zero outside I)
+// formed once. Per shot the lambda of the six split stresses (x parts on compact x planes, z
+// parts on compact z planes) and vx, vz of the forward history (full planes) are staged into
+// one of two buffers -- the next shot's copies are in flight while a shot is evaluated. Each
+// thread then forms the eight sources q (sx_b, sx_zb, sx_f, sx_zf, sz_b, sz_zb, sz_f, sz_zf:
+// coefficient-weighted lambda, zero outside I) of its own cell (whose weighted lambda it keeps
+// for the gradients) and of at most one halo cell, three of each four over the lambda they are
+// formed from; the transposes and gradients follow. 47.0 KB of shared memory in single
+// precision.
+constexpr int kAdjVShot = 3 * kXPlane + 3 * kZPlane + 2 * kSPlane;  // one shot's staged planes
+constexpr int kAdjVPmlElems = 6 * kSPlane + 2 * kXPlane + 2 * kZPlane + 2 * kAdjVShot;  // C, factors, q; buffers
 template <typename T, int NN>
-__global__ void __launch_bounds__(kTileThreads)
+__global__ void __launch_bounds__(kTileThreads, sizeof(T) == 4 ? 4 : 2)
     adj_v_pml(Geo<T> g, const T* __restrict__ cf, const T* __restrict__ lts, T* __restrict__ lv,
               const T* __restrict__ v_hist, T* __restrict__ gpart, int eg) {
   griddep_wait();  // launched with programmatic serialisation in the PML time loops
   griddep_launch_dependents();
   extern __shared__ __align__(16) unsigned char el_smem[];
   T* sC = reinterpret_cast<T*>(el_smem);  // 6 full planes
-  T* sK = sC + 6 * kSPlane;                // kx, kz (full)
-  T* sV = sC + 8 * kSPlane;                // vx, vz (full)
-  T* sLx = sC + 10 * kSPlane;              // lambda txx_x, tzz_x, txz_x (x planes)
-  T* sLz = sLx + 3 * kXPlane;              // lambda txx_z, tzz_z, txz_z (z planes)
-  T* sQx = sLz + 3 * kZPlane;              // q0, q2, q4, q6 (x planes)
-  T* sQz = sQx + 4 * kXPlane;              // q1, q3, q5, q7 (z planes)
+  T* sKx = sC + 6 * kSPlane;              // dt/dx / pml_xd (x plane)
+  T* sKz = sKx + kXPlane;                 // dt/dz / pml_zd (z plane)
+  T* sQx = sKz + kZPlane;                 // the fourth x source q6 (x plane)
+  T* sQz = sQx + kXPlane;                 // the fourth z source q7 (z plane)
+  T* sB = sQz + kZPlane;                  // two shot buffers
+  // a shot buffer: lambda txx_x, tzz_x, txz_x (x planes; then q0, q2, q4), lambda txx_z, tzz_z,
+  // txz_z (z planes; then q1, q3, q5), vx, vz (full planes)
+  constexpr int oLz = 3 * kXPlane, oV = oLz + 3 * kZPlane;
   const int tiles_x = (g.L.nxp + kTileX - 1) / kTileX;
   const int i0 = ((int)blockIdx.x / tiles_x) * kTileZ, j0 = ((int)blockIdx.x % tiles_x) * kTileX;
   const int ty = (int)threadIdx.x / kTileX, tx = (int)threadIdx.x % kTileX;
@@ -1082,95 +1174,140 @@ __global__ void __launch_bounds__(kTileThreads)
   const bool valid = i < g.L.nzp && j < g.L.nxp, inside = valid && in_I(g, i, j);
   const int64_t PL = g.L.plane, NSP = (int64_t)g.ns * PL, oc = g.L.off(i, j);
   const int sc = kSC + ty * kSW + tx, cx = ty * kSW + tx + 4, cz = (ty + 3) * kTileX + tx;
+  // this thread's halo cell: x-plane columns j0-4 .. j0-1 and j0+32 .. j0+35, or z-plane rows
+  // i0-3 .. i0-1 and i0+8 .. i0+10
+  const bool hx = (int)threadIdx.x < kXHalo;
+  int hr, hc;  // the halo cell's row and column relative to (i0, j0)
+  if (hx) {
+    const int c8 = (int)threadIdx.x & 7;
+    hr = (int)threadIdx.x >> 3;
+    hc = c8 < 4 ? c8 - 4 : c8 + kTileX - 4;
+  } else {
+    const int t = (int)threadIdx.x - kXHalo, r6 = t / kTileX;
+    hr = r6 < 3 ? r6 - 3 : r6 + kTileZ - 3;
+    hc = t - r6 * kTileX;
+  }
+  const int hs = hx ? hr * kSW + hc + 4 : (hr + 3) * kTileX + hc;  // in its compact plane
+  const int hf = (hr + 3) * kSW + hc + 4;                            // in a full plane
   EL_SHOT_GROUP
   T* gc = gbase;
 #pragma unroll
   for (int k = 0; k < 6; ++k) stage(sC + k * kSPlane, cf + (C11 + k) * PL, g.L, i0, j0, 3, 4);
-  stage(sK, cf + BCX * PL, g.L, i0, j0, 3, 4);
-  stage(sK + kSPlane, cf + BCZ * PL, g.L, i0, j0, 3, 4);
-  cp_async_wait_all();
-  __syncthreads();
-  for (int t = threadIdx.x; t < kSPlane; t += kTileThreads) {  // bcx, bcz -> the factors, in place
-    const int ii = i0 + t / kSW - 3, jj = j0 + t % kSW - 4;
-    T kx = T(0), kz = T(0);
-    if (in_I(g, ii, jj)) {
-      kx = g.dt_dx / (T(1) + g.hdt * sK[t]);
-      kz = g.dt_dz / (T(1) + g.hdt * sK[kSPlane + t]);
-    }
-    sK[t] = kx;
-    sK[kSPlane + t] = kz;
-  }
-  // (the barrier after the first shot's copies orders these writes before their reads)
-  T g11 = T(0), g13 = T(0), g15 = T(0), g33 = T(0), g35 = T(0), g55 = T(0);
-  for (int s = s_beg; s < s_end; ++s) {
+  cp_async_commit();
+  auto issue = [&](int s, T* B) {
     const int64_t so = (int64_t)s * PL;
     // the x parts of the split stresses feed the sources of x differences, the z parts those of
     // z differences
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-      stage_x(sLx + k * kXPlane, lts + (2 * k) * NSP + so, g.L, i0, j0);
-      stage_z(sLz + k * kZPlane, lts + (2 * k + 1) * NSP + so, g.L, i0, j0);
+      stage_x(B + k * kXPlane, lts + (2 * k) * NSP + so, g.L, i0, j0);
+      stage_z(B + oLz + k * kZPlane, lts + (2 * k + 1) * NSP + so, g.L, i0, j0);
     }
-    stage(sV, v_hist + VX * NSP + so, g.L, i0, j0, 3, 4);
-    stage(sV + kSPlane, v_hist + VZ * NSP + so, g.L, i0, j0, 3, 4);
-    cp_async_wait_all();
+    stage(B + oV, v_hist + VX * NSP + so, g.L, i0, j0, 3, 4);
+    stage(B + oV + kSPlane, v_hist + VZ * NSP + so, g.L, i0, j0, 3, 4);
+    cp_async_commit();
+  };
+  if (s_beg < s_end) issue(s_beg, sB);
+  for (int t = threadIdx.x; t < kXPlane; t += kTileThreads) {
+    const int ii = i0 + t / kSW, jj = j0 - 4 + t % kSW;
+    sKx[t] = in_I(g, ii, jj) ? g.dt_dx / (T(1) + g.hdt * cf[BCX * PL + g.L.off(ii, jj)]) : T(0);
+  }
+  for (int t = threadIdx.x; t < kZPlane; t += kTileThreads) {
+    const int ii = i0 - 3 + t / kTileX, jj = j0 + t % kTileX;
+    sKz[t] = in_I(g, ii, jj) ? g.dt_dz / (T(1) + g.hdt * cf[BCZ * PL + g.L.off(ii, jj)]) : T(0);
+  }
+  // (the barrier after the first shot's copies orders these writes before their reads)
+  T g11 = T(0), g13 = T(0), g15 = T(0), g33 = T(0), g35 = T(0), g55 = T(0);
+  for (int s = s_beg; s < s_end; ++s) {
+    T* B = sB + ((s - s_beg) & 1) * kAdjVShot;
+    if (s + 1 < s_end) {
+      issue(s + 1, sB + ((s + 1 - s_beg) & 1) * kAdjVShot);  // into the buffer the previous shot used
+      cp_async_wait_group<1>();
+    } else {
+      cp_async_wait_group<0>();
+    }
     __syncthreads();
-    for (int t = threadIdx.x; t < kXPlane; t += kTileThreads) {  // q0, q2, q4, q6
-      const int u = 3 * kSW + t;                                  // the same cell in a full plane
-      const T kx = sK[u];
+    T* sLx = B;
+    T* sLz = B + oLz;
+    // own cell: the stress update's sources at the cell (stress_q's PML form), then q
+    StressQ<T> r;
+    {
+      const T kx = sKx[cx], kz = sKz[cz];
+      r.a = sLx[cx] * kx;
+      r.c = sLx[kXPlane + cx] * kx;
+      r.e = sLx[2 * kXPlane + cx] * kx;
+      r.b = sLz[cz] * kz;
+      r.d = sLz[kZPlane + cz] * kz;
+      r.f = sLz[2 * kZPlane + cz] * kz;
+      const T c11 = sC[sc], c13 = sC[kSPlane + sc], c15 = sC[2 * kSPlane + sc];
+      const T c33 = sC[3 * kSPlane + sc], c35 = sC[4 * kSPlane + sc], c55 = sC[5 * kSPlane + sc];
       T a = T(0), b = T(0), c = T(0), d = T(0);
       if (kx != T(0)) {  // inside I (the factor is positive there)
-        const T ra = sLx[t] * kx, rc = sLx[kXPlane + t] * kx, re = sLx[2 * kXPlane + t] * kx;
-        const T c15 = sC[2 * kSPlane + u];
-        a = sC[u] * ra + sC[kSPlane + u] * rc;
-        b = c15 * re;
-        c = c15 * ra + sC[4 * kSPlane + u] * rc;
-        d = sC[5 * kSPlane + u] * re;
+        a = c11 * r.a + c13 * r.c;
+        b = c15 * r.e;
+        c = c15 * r.a + c35 * r.c;
+        d = c55 * r.e;
       }
-      sQx[t] = a;
-      sQx[kXPlane + t] = b;
-      sQx[2 * kXPlane + t] = c;
-      sQx[3 * kXPlane + t] = d;
+      sLx[cx] = a;
+      sLx[kXPlane + cx] = b;
+      sLx[2 * kXPlane + cx] = c;
+      sQx[cx] = d;
+      a = b = c = d = T(0);
+      if (kz != T(0)) {
+        a = c15 * r.b + c35 * r.d;
+        b = c55 * r.f;
+        c = c13 * r.b + c33 * r.d;
+        d = c35 * r.f;
+      }
+      sLz[cz] = a;
+      sLz[kZPlane + cz] = b;
+      sLz[2 * kZPlane + cz] = c;
+      sQz[cz] = d;
     }
-    for (int t = threadIdx.x; t < kZPlane; t += kTileThreads) {  // q1, q3, q5, q7
-      const int u = (t / kTileX) * kSW + 4 + t % kTileX;
-      const T kz = sK[kSPlane + u];
+    // halo cell: its sources
+    if (hx) {
+      const T kx = sKx[hs];
+      T a = T(0), b = T(0), c = T(0), d = T(0);
+      if (kx != T(0)) {
+        const T ra = sLx[hs] * kx, rc = sLx[kXPlane + hs] * kx, re = sLx[2 * kXPlane + hs] * kx;
+        const T c15 = sC[2 * kSPlane + hf];
+        a = sC[hf] * ra + sC[kSPlane + hf] * rc;
+        b = c15 * re;
+        c = c15 * ra + sC[4 * kSPlane + hf] * rc;
+        d = sC[5 * kSPlane + hf] * re;
+      }
+      sLx[hs] = a;
+      sLx[kXPlane + hs] = b;
+      sLx[2 * kXPlane + hs] = c;
+      sQx[hs] = d;
+    } else {
+      const T kz = sKz[hs];
       T a = T(0), b = T(0), c = T(0), d = T(0);
       if (kz != T(0)) {
-        const T rb = sLz[t] * kz, rd = sLz[kZPlane + t] * kz, rf = sLz[2 * kZPlane + t] * kz;
-        const T c35 = sC[4 * kSPlane + u];
-        a = sC[2 * kSPlane + u] * rb + c35 * rd;
-        b = sC[5 * kSPlane + u] * rf;
-        c = sC[kSPlane + u] * rb + sC[3 * kSPlane + u] * rd;
+        const T rb = sLz[hs] * kz, rd = sLz[kZPlane + hs] * kz, rf = sLz[2 * kZPlane + hs] * kz;
+        const T c35 = sC[4 * kSPlane + hf];
+        a = sC[2 * kSPlane + hf] * rb + c35 * rd;
+        b = sC[5 * kSPlane + hf] * rf;
+        c = sC[kSPlane + hf] * rb + sC[3 * kSPlane + hf] * rd;
         d = c35 * rf;
       }
-      sQz[t] = a;
-      sQz[kZPlane + t] = b;
-      sQz[2 * kZPlane + t] = c;
-      sQz[3 * kZPlane + t] = d;
+      sLz[hs] = a;
+      sLz[kZPlane + hs] = b;
+      sLz[2 * kZPlane + hs] = c;
+      sQz[hs] = d;
     }
     __syncthreads();
     if (valid) {
-      const StagedX<T> q0{sQx, i0, j0}, q2{sQx + kXPlane, i0, j0}, q4{sQx + 2 * kXPlane, i0, j0},
-          q6{sQx + 3 * kXPlane, i0, j0};
-      const StagedZ<T> q1{sQz, i0, j0}, q3{sQz + kZPlane, i0, j0}, q5{sQz + 2 * kZPlane, i0, j0},
-          q7{sQz + 3 * kZPlane, i0, j0};
+      const StagedX<T> q0{sLx, i0, j0}, q2{sLx + kXPlane, i0, j0}, q4{sLx + 2 * kXPlane, i0, j0}, q6{sQx, i0, j0};
+      const StagedZ<T> q1{sLz, i0, j0}, q3{sLz + kZPlane, i0, j0}, q5{sLz + 2 * kZPlane, i0, j0}, q7{sQz, i0, j0};
       const T avx = dxb_t<NN>(g, q0, i, j) + dzb_t<NN>(g, q1, i, j) + dxf_t<NN>(g, q2, i, j) + dzf_t<NN>(g, q3, i, j);
       const T avz = dxb_t<NN>(g, q4, i, j) + dzb_t<NN>(g, q5, i, j) + dxf_t<NN>(g, q6, i, j) + dzf_t<NN>(g, q7, i, j);
-      const int64_t o = so + oc;
+      const int64_t o = (int64_t)s * PL + oc;
       lv[VX * NSP + o] = avx;
       lv[VZ * NSP + o] = avz;
       if (inside) {
-        const T kx = sK[sc], kz = sK[kSPlane + sc];
-        StressQ<T> r;  // the stress update's sources at the cell (stress_q's PML form)
-        r.a = sLx[cx] * kx;
-        r.b = sLz[cz] * kz;
-        r.c = sLx[kXPlane + cx] * kx;
-        r.d = sLz[kZPlane + cz] * kz;
-        r.e = sLx[2 * kXPlane + cx] * kx;
-        r.f = sLz[2 * kZPlane + cz] * kz;
-        const T* vx = sV;
-        const T* vz = sV + kSPlane;
+        const T* vx = B + oV;
+        const T* vz = B + oV + kSPlane;
         const T dxb_vx = dxb<NN>(g, vx, sc), dxb_vz = dxb<NN>(g, vz, sc);
         const T dzb_vx = dzb<NN>(g, vx, sc, kSW), dzb_vz = dzb<NN>(g, vz, sc, kSW);
         const T dxf_vx = dxf<NN>(g, vx, sc), dxf_vz = dxf<NN>(g, vz, sc);
@@ -1183,7 +1320,7 @@ __global__ void __launch_bounds__(kTileThreads)
         g55 += r.e * dxf_vz + r.f * dzf_vx;
       }
     }
-    __syncthreads();  // the next shot's copies overwrite the staged planes
+    __syncthreads();  // this buffer is refilled by the copies of the shot after next
   }
   if (inside) {
     gc[C11 * PL + oc] += g11;
@@ -1389,11 +1526,14 @@ ECarve ecarve(const adfwi_elastic_plan* p, bool grad, int K) {
     c.snap_scale = take(full ? 0 : (int64_t)nseg * nstate * ns * 4);
     c.hv = take((int64_t)K * 2 * ns * pl);  // velocity totals at the start of each step
     c.ht = take((int64_t)K * 3 * ns * pl);  // stress totals after each step's free surface
-    c.lst = take((int64_t)(p->d.pml ? 10 : 3) * ns * pl);
+    // lambda of the split stresses (6) and of the split velocities (4, twice: read one, write the other)
+    c.lst = take((int64_t)(p->d.pml ? 14 : 3) * ns * pl);
     c.lt = take(3 * ns * pl);
     c.lv = take(2 * ns * pl);
     c.lv2 = take(2 * ns * pl);
-    c.qsrc = take(8 * ns * pl);  // adjoint sources of the step transposes (8 planes per shot)
+    // adjoint sources of the absorbing-layer step transposes (8 planes per shot; the PML kernels
+    // form theirs in shared memory)
+    c.qsrc = take(p->d.pml ? 0 : 8 * ns * pl);
     c.gc = take(8 * pl * egroups(p));
   }
   c.total = o;
@@ -1642,13 +1782,13 @@ int ebackward(const adfwi_elastic_plan* p, const void* wavelet, const void* grec
   T* gcp = reinterpret_cast<T*>(ws + c.gc);
   T* qsrc = reinterpret_cast<T*>(ws + c.qsrc);
   const T* gr = static_cast<const T*>(grec);
-  const int nsf = p->d.pml ? 10 : 3;
+  const int nsf = p->d.pml ? 14 : 3;
   ADFWI_CUDA_TRY(cudaMemsetAsync(lst, 0, nsf * NSP * sizeof(T), s));
   ADFWI_CUDA_TRY(cudaMemsetAsync(lt, 0, 3 * NSP * sizeof(T), s));
   ADFWI_CUDA_TRY(cudaMemsetAsync(lv, 0, 2 * NSP * sizeof(T), s));
   const int egr = egroups(p), eg = eshots_per_group(p);
   ADFWI_CUDA_TRY(cudaMemsetAsync(gcp, 0, (int64_t)egr * 8 * PL * sizeof(T), s));
-  {
+  if (!p->d.pml) {
     // the source planes are read with their halos by the transposed stencils
     int rc0 = zero_frames<T>(qsrc, (int64_t)8 * ns, p->L, s);
     if (rc0) return rc0;
@@ -1663,7 +1803,7 @@ int ebackward(const adfwi_elastic_plan* p, const void* wavelet, const void* grec
   const dim3 gcs = cells_grid(p, ns), gcg = cells_grid(p, egroups(p)), b(el::kTileThreads);
   const dim3 gcm = cells_grid(p, (ns + el::kCellShots - 1) / el::kCellShots);
   // shared memory of the staged gradient kernels (above the 48 KB default in double precision)
-  const int smem_t = el::kAdjTPlanes * el::kSPlane * (int)sizeof(T);
+  const int smem_t = el::kAdjTElems * (int)sizeof(T);
   const int smem_vp = el::kAdjVPmlElems * (int)sizeof(T);
   const int smem_va = el::adj_v_planes<false>() * el::kSPlane * (int)sizeof(T);
   ADFWI_CUDA_TRY(cudaFuncSetAttribute(el::adj_t_pml<T, NN>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_t));
@@ -1672,6 +1812,7 @@ int ebackward(const adfwi_elastic_plan* p, const void* wavelet, const void* grec
   const dim3 gcol((unsigned)((p->nxp + 127) / 128), ns);
   const dim3 ginj((unsigned)std::max(1, (p->ncells + 127) / 128), ns);
   const int nseg = full ? 1 : (nt + K - 1) / K;
+  int flip = 0;  // which copy of the split velocities' lambda the next reverse step reads
   for (int seg = nseg - 1; seg >= 0; --seg) {
     const int t0 = full ? 0 : seg * K;
     const int t1 = full ? nt : std::min(nt, t0 + K);
@@ -1699,9 +1840,11 @@ int ebackward(const adfwi_elastic_plan* p, const void* wavelet, const void* grec
         // one stream of programmatically serialised launches per reverse step; lt is
         // overwritten by adj_t_pml before the stress-record gradients are added to it
         if (gr) ADFWI_LAUNCH(kAux, s, (void)launch_pdl_kernel(el::adj_inject<T>, ginj, dim3(128), 0, s, g, it, gr, lt, lv, 1));
-        ADFWI_LAUNCH(kElAdjStep, s, (void)launch_pdl_kernel(el::adj_vfs_tq_pml<T>, gcm, b, 0, s, g, cf, lv, lst + 6 * NSP, qsrc));
+        T* lvs_in = lst + (6 + 4 * flip) * NSP;
+        T* lvs_out = lst + (10 - 4 * flip) * NSP;
+        flip ^= 1;
         ADFWI_LAUNCH(kElAdjStep, s, (void)launch_pdl_kernel(el::adj_t_pml<T, NN>, gcg, b, (size_t)smem_t, s, g, cf,
-                                                            lst + 6 * NSP, qsrc, lt, th, gcp, eg));
+                                                            (const T*)lv, (const T*)lvs_in, lvs_out, lt, th, gcp, eg));
         if (gr) ADFWI_LAUNCH(kAux, s, (void)launch_pdl_kernel(el::adj_inject<T>, ginj, dim3(128), 0, s, g, it, gr, lt, lv, 2));
         ADFWI_LAUNCH(kElAdjStep, s, (void)launch_pdl_kernel(el::adj_tfs_pml<T>, gcm, b, 0, s, g, cf, (const T*)lt, lst));
         ADFWI_LAUNCH(kElAdjStep, s, (void)launch_pdl_kernel(el::adj_v_pml<T, NN>, gcg, b, (size_t)smem_vp, s, g, cf,

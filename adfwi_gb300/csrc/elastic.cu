@@ -953,36 +953,6 @@ __global__ void __launch_bounds__(kTileThreads, sizeof(T) == 4 ? 5 : 2)
   }
 }
 
-// (B2) lambda of the split stresses: S * lambda + lambda of the totals after the stress
-// free-surface adjoint (the stress update's adjoint sources are formed by adj_v_pml).
-template <typename T>
-__global__ void adj_tfs_pml(Geo<T> g, const T* __restrict__ cf, const T* __restrict__ lt, T* __restrict__ lts) {
-  griddep_wait();  // launched with programmatic serialisation in the PML time loops
-  griddep_launch_dependents();
-  EL_CELL_SHOTS
-  T sx = T(1), sz = T(1);
-  if (in_I(g, i, j)) {
-    const Pml<T> p = pml_at(g, cf, occ, PL);
-    sx = p.xn * (T(1) / p.xd);  // the adjoint needs no bit-exact rounding
-    sz = p.zn * (T(1) / p.zd);
-  }
-#pragma unroll
-  for (int q = 0; q < kCellShots; ++q) {
-    const int s = s_lo + q;
-    if (s >= g.ns) break;
-    const int64_t o = (int64_t)s * PL + occ;
-    T azz, axz;
-    tfs_adjoint(g, lt + TZZ * NSP, lt + TXZ * NSP, i, o, azz, axz);
-    const T axx = lt[TXX * NSP + o];
-    lts[TXX_X * NSP + o] = sx * lts[TXX_X * NSP + o] + axx;
-    lts[TXX_Z * NSP + o] = sz * lts[TXX_Z * NSP + o] + axx;
-    lts[TZZ_X * NSP + o] = sx * lts[TZZ_X * NSP + o] + azz;
-    lts[TZZ_Z * NSP + o] = sz * lts[TZZ_Z * NSP + o] + azz;
-    lts[TXZ_X * NSP + o] = sx * lts[TXZ_X * NSP + o] + axz;
-    lts[TXZ_Z * NSP + o] = sz * lts[TXZ_Z * NSP + o] + axz;
-  }
-}
-
 // Coefficient-weighted adjoint sources of the stress update at cell (ii, jj):
 // q[0..5] = lambda of txx_x, txx_z, tzz_x, tzz_z, txz_x, txz_z times their d(update)/d(C D v).
 template <typename T>
@@ -1137,36 +1107,41 @@ __global__ void __launch_bounds__(kTileThreads)
   }
 }
 
-// (B1a, PML) lambda of the velocity totals at the start of the step (overwrite) and the C
-// gradients, with the stress update's adjoint sources formed in shared memory. Per block the
-// tile's cell coefficients C11 .. C55 (full planes, with the halo) are staged once and the PML
-// factors dt/dx / pml_xd (compact x plane) and dt/dz / pml_zd (compact z plane; zero outside I)
-// formed once. Per shot the lambda of the six split stresses (x parts on compact x planes, z
-// parts on compact z planes) and vx, vz of the forward history (full planes) are staged into
-// one of two buffers -- the next shot's copies are in flight while a shot is evaluated. Each
-// thread then forms the eight sources q (sx_b, sx_zb, sx_f, sx_zf, sz_b, sz_zb, sz_f, sz_zf:
-// coefficient-weighted lambda, zero outside I) of its own cell (whose weighted lambda it keeps
-// for the gradients) and of at most one halo cell, three of each four over the lambda they are
-// formed from; the transposes and gradients follow. 47.0 KB of shared memory in single
+// (B2 + B1a, PML) per shot group: the split stresses' lambda after the step (the stress
+// free-surface adjoint, then S * lambda + lambda of the totals; read from lts_in, written to
+// lts_out, so that no block reads a halo cell another block has already advanced), lambda of the
+// velocity totals at the start of the step (overwrite) and the C gradients, with the stress
+// update's adjoint sources formed in shared memory. Per block the tile's cell coefficients
+// C11 .. C55 (full planes, with the halo) are staged once and the factors S_x and dt/dx / pml_xd
+// (compact x planes), S_z and dt/dz / pml_zd (compact z planes; S = 1 and the source factors zero
+// outside I) formed once. Per shot the lambda of the six split stresses (x parts on compact x
+// planes, z parts on compact z planes), the lambda of the stress totals and vx, vz of the
+// forward history (full planes) are staged into one of two buffers -- the next shot's copies
+// are in flight while a shot is evaluated. Each thread then advances the lambda of its own cell
+// (stored for the next step; its weighted lambda kept for the gradients) and of at most one
+// halo cell and forms their eight sources q (sx_b, sx_zb, sx_f, sx_zf, sz_b, sz_zb, sz_f, sz_zf:
+// coefficient-weighted lambda, zero outside I), three of each four over the lambda they are
+// formed from; the transposes and gradients follow. 63.5 KB of shared memory in single
 // precision.
-constexpr int kAdjVShot = 3 * kXPlane + 3 * kZPlane + 2 * kSPlane;  // one shot's staged planes
-constexpr int kAdjVPmlElems = 6 * kSPlane + 2 * kXPlane + 2 * kZPlane + 2 * kAdjVShot;  // C, factors, q; buffers
+constexpr int kAdjVShot = 3 * kXPlane + 3 * kZPlane + 5 * kSPlane;  // one shot's staged planes
+constexpr int kAdjVPmlElems = 6 * kSPlane + 3 * kXPlane + 3 * kZPlane + 2 * kAdjVShot;  // C, factors, q; buffers
 template <typename T, int NN>
-__global__ void __launch_bounds__(kTileThreads, sizeof(T) == 4 ? 4 : 2)
-    adj_v_pml(Geo<T> g, const T* __restrict__ cf, const T* __restrict__ lts, T* __restrict__ lv,
-              const T* __restrict__ v_hist, T* __restrict__ gpart, int eg) {
+__global__ void __launch_bounds__(kTileThreads, sizeof(T) == 4 ? 3 : 1)
+    adj_v_pml(Geo<T> g, const T* __restrict__ cf, const T* __restrict__ lt, const T* __restrict__ lts_in,
+              T* __restrict__ lts_out, T* __restrict__ lv, const T* __restrict__ v_hist, T* __restrict__ gpart,
+              int eg) {
   griddep_wait();  // launched with programmatic serialisation in the PML time loops
   griddep_launch_dependents();
   extern __shared__ __align__(16) unsigned char el_smem[];
   T* sC = reinterpret_cast<T*>(el_smem);  // 6 full planes
-  T* sKx = sC + 6 * kSPlane;              // dt/dx / pml_xd (x plane)
-  T* sKz = sKx + kXPlane;                 // dt/dz / pml_zd (z plane)
-  T* sQx = sKz + kZPlane;                 // the fourth x source q6 (x plane)
+  T* sKx = sC + 6 * kSPlane;              // S_x, dt/dx / pml_xd (x planes)
+  T* sKz = sKx + 2 * kXPlane;             // S_z, dt/dz / pml_zd (z planes)
+  T* sQx = sKz + 2 * kZPlane;             // the fourth x source q6 (x plane)
   T* sQz = sQx + kXPlane;                 // the fourth z source q7 (z plane)
   T* sB = sQz + kZPlane;                  // two shot buffers
   // a shot buffer: lambda txx_x, tzz_x, txz_x (x planes; then q0, q2, q4), lambda txx_z, tzz_z,
-  // txz_z (z planes; then q1, q3, q5), vx, vz (full planes)
-  constexpr int oLz = 3 * kXPlane, oV = oLz + 3 * kZPlane;
+  // txz_z (z planes; then q1, q3, q5), lambda of txx, tzz, txz, and vx, vz (full planes)
+  constexpr int oLz = 3 * kXPlane, oA = oLz + 3 * kZPlane, oV = oA + 3 * kSPlane;
   const int tiles_x = (g.L.nxp + kTileX - 1) / kTileX;
   const int i0 = ((int)blockIdx.x / tiles_x) * kTileZ, j0 = ((int)blockIdx.x % tiles_x) * kTileX;
   const int ty = (int)threadIdx.x / kTileX, tx = (int)threadIdx.x % kTileX;
@@ -1187,10 +1162,15 @@ __global__ void __launch_bounds__(kTileThreads, sizeof(T) == 4 ? 4 : 2)
     hr = r6 < 3 ? r6 - 3 : r6 + kTileZ - 3;
     hc = t - r6 * kTileX;
   }
+  const int hi = i0 + hr, hj = j0 + hc;
+  const bool hvalid = hi >= 0 && hi < g.L.nzp && hj >= 0 && hj < g.L.nxp;
   const int hs = hx ? hr * kSW + hc + 4 : (hr + 3) * kTileX + hc;  // in its compact plane
   const int hf = (hr + 3) * kSW + hc + 4;                            // in a full plane
   EL_SHOT_GROUP
   T* gc = gbase;
+  const T* lxx = lt + TXX * NSP;
+  const T* lzz = lt + TZZ * NSP;
+  const T* lxz = lt + TXZ * NSP;
 #pragma unroll
   for (int k = 0; k < 6; ++k) stage(sC + k * kSPlane, cf + (C11 + k) * PL, g.L, i0, j0, 3, 4);
   cp_async_commit();
@@ -1200,23 +1180,45 @@ __global__ void __launch_bounds__(kTileThreads, sizeof(T) == 4 ? 4 : 2)
     // z differences
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-      stage_x(B + k * kXPlane, lts + (2 * k) * NSP + so, g.L, i0, j0);
-      stage_z(B + oLz + k * kZPlane, lts + (2 * k + 1) * NSP + so, g.L, i0, j0);
+      stage_x(B + k * kXPlane, lts_in + (2 * k) * NSP + so, g.L, i0, j0);
+      stage_z(B + oLz + k * kZPlane, lts_in + (2 * k + 1) * NSP + so, g.L, i0, j0);
     }
+    stage(B + oA, lxx + so, g.L, i0, j0, 3, 4);
+    stage(B + oA + kSPlane, lzz + so, g.L, i0, j0, 3, 4);
+    stage(B + oA + 2 * kSPlane, lxz + so, g.L, i0, j0, 3, 4);
     stage(B + oV, v_hist + VX * NSP + so, g.L, i0, j0, 3, 4);
     stage(B + oV + kSPlane, v_hist + VZ * NSP + so, g.L, i0, j0, 3, 4);
     cp_async_commit();
   };
   if (s_beg < s_end) issue(s_beg, sB);
+  // the factors, formed as the per-cell adjoint forms them, while the first copies land
   for (int t = threadIdx.x; t < kXPlane; t += kTileThreads) {
     const int ii = i0 + t / kSW, jj = j0 - 4 + t % kSW;
-    sKx[t] = in_I(g, ii, jj) ? g.dt_dx / (T(1) + g.hdt * cf[BCX * PL + g.L.off(ii, jj)]) : T(0);
+    T sx = T(1), kx = T(0);
+    if (in_I(g, ii, jj)) {
+      const int64_t c0 = g.L.off(ii, jj);
+      const Pml<T> p = pml_at(g, cf, c0, PL);
+      sx = p.xn * (T(1) / p.xd);
+      kx = g.dt_dx / (T(1) + g.hdt * cf[BCX * PL + c0]);
+    }
+    sKx[t] = sx;
+    sKx[kXPlane + t] = kx;
   }
   for (int t = threadIdx.x; t < kZPlane; t += kTileThreads) {
     const int ii = i0 - 3 + t / kTileX, jj = j0 + t % kTileX;
-    sKz[t] = in_I(g, ii, jj) ? g.dt_dz / (T(1) + g.hdt * cf[BCZ * PL + g.L.off(ii, jj)]) : T(0);
+    T sz = T(1), kz = T(0);
+    if (in_I(g, ii, jj)) {
+      const int64_t c0 = g.L.off(ii, jj);
+      const Pml<T> p = pml_at(g, cf, c0, PL);
+      sz = p.zn * (T(1) / p.zd);
+      kz = g.dt_dz / (T(1) + g.hdt * cf[BCZ * PL + c0]);
+    }
+    sKz[t] = sz;
+    sKz[kZPlane + t] = kz;
   }
   // (the barrier after the first shot's copies orders these writes before their reads)
+  // rows whose totals' lambda the stress free-surface adjoint combines across cells
+  const int fs_lo = g.fsurf ? g.h - 3 : 1 << 30, fs_hi = g.fsurf ? g.h : -1;
   T g11 = T(0), g13 = T(0), g15 = T(0), g33 = T(0), g35 = T(0), g55 = T(0);
   for (int s = s_beg; s < s_end; ++s) {
     T* B = sB + ((s - s_beg) & 1) * kAdjVShot;
@@ -1227,18 +1229,42 @@ __global__ void __launch_bounds__(kTileThreads, sizeof(T) == 4 ? 4 : 2)
       cp_async_wait_group<0>();
     }
     __syncthreads();
+    const int64_t so = (int64_t)s * PL;
     T* sLx = B;
     T* sLz = B + oLz;
-    // own cell: the stress update's sources at the cell (stress_q's PML form), then q
+    const T* sA = B + oA;
+    // own cell: lambda after the step (stored), the stress update's sources at the cell
+    // (stress_q's PML form), then q
     StressQ<T> r;
     {
-      const T kx = sKx[cx], kz = sKz[cz];
-      r.a = sLx[cx] * kx;
-      r.c = sLx[kXPlane + cx] * kx;
-      r.e = sLx[2 * kXPlane + cx] * kx;
-      r.b = sLz[cz] * kz;
-      r.d = sLz[kZPlane + cz] * kz;
-      r.f = sLz[2 * kZPlane + cz] * kz;
+      T lxx_x = sLx[cx], lzz_x = sLx[kXPlane + cx], lxz_x = sLx[2 * kXPlane + cx];
+      T lxx_z = sLz[cz], lzz_z = sLz[kZPlane + cz], lxz_z = sLz[2 * kZPlane + cz];
+      if (valid) {
+        const int64_t o = so + oc;
+        const T axx = sA[sc];
+        T azz = sA[kSPlane + sc], axz = sA[2 * kSPlane + sc];
+        if (i >= fs_lo && i <= fs_hi) tfs_adjoint(g, lzz, lxz, i, o, azz, axz);
+        const T sx = sKx[cx], sz = sKz[cz];
+        lxx_x = sx * lxx_x + axx;
+        lxx_z = sz * lxx_z + axx;
+        lzz_x = sx * lzz_x + azz;
+        lzz_z = sz * lzz_z + azz;
+        lxz_x = sx * lxz_x + axz;
+        lxz_z = sz * lxz_z + axz;
+        lts_out[TXX_X * NSP + o] = lxx_x;
+        lts_out[TXX_Z * NSP + o] = lxx_z;
+        lts_out[TZZ_X * NSP + o] = lzz_x;
+        lts_out[TZZ_Z * NSP + o] = lzz_z;
+        lts_out[TXZ_X * NSP + o] = lxz_x;
+        lts_out[TXZ_Z * NSP + o] = lxz_z;
+      }
+      const T kx = sKx[kXPlane + cx], kz = sKz[kZPlane + cz];
+      r.a = lxx_x * kx;
+      r.c = lzz_x * kx;
+      r.e = lxz_x * kx;
+      r.b = lxx_z * kz;
+      r.d = lzz_z * kz;
+      r.f = lxz_z * kz;
       const T c11 = sC[sc], c13 = sC[kSPlane + sc], c15 = sC[2 * kSPlane + sc];
       const T c33 = sC[3 * kSPlane + sc], c35 = sC[4 * kSPlane + sc], c55 = sC[5 * kSPlane + sc];
       T a = T(0), b = T(0), c = T(0), d = T(0);
@@ -1264,37 +1290,43 @@ __global__ void __launch_bounds__(kTileThreads, sizeof(T) == 4 ? 4 : 2)
       sLz[2 * kZPlane + cz] = c;
       sQz[cz] = d;
     }
-    // halo cell: its sources
-    if (hx) {
-      const T kx = sKx[hs];
-      T a = T(0), b = T(0), c = T(0), d = T(0);
-      if (kx != T(0)) {
-        const T ra = sLx[hs] * kx, rc = sLx[kXPlane + hs] * kx, re = sLx[2 * kXPlane + hs] * kx;
-        const T c15 = sC[2 * kSPlane + hf];
-        a = sC[hf] * ra + sC[kSPlane + hf] * rc;
-        b = c15 * re;
-        c = c15 * ra + sC[4 * kSPlane + hf] * rc;
-        d = sC[5 * kSPlane + hf] * re;
+    // halo cell: lambda after the step (not stored: another block owns the cell), its sources
+    {
+      T* hl = hx ? sLx + hs : sLz + hs;
+      const int HP = hx ? kXPlane : kZPlane;
+      const T* hK = hx ? sKx + hs : sKz + hs;
+      T l0 = hl[0], l1 = hl[HP], l2 = hl[2 * HP];  // lambda of the txx, tzz, txz part
+      if (hvalid) {
+        const T axx = sA[hf];
+        T azz = sA[kSPlane + hf], axz = sA[2 * kSPlane + hf];
+        if (hi >= fs_lo && hi <= fs_hi) tfs_adjoint(g, lzz, lxz, hi, so + g.L.off(hi, hj), azz, axz);
+        const T sh = hK[0];
+        l0 = sh * l0 + axx;
+        l1 = sh * l1 + azz;
+        l2 = sh * l2 + axz;
       }
-      sLx[hs] = a;
-      sLx[kXPlane + hs] = b;
-      sLx[2 * kXPlane + hs] = c;
-      sQx[hs] = d;
-    } else {
-      const T kz = sKz[hs];
+      const T k = hK[HP];
       T a = T(0), b = T(0), c = T(0), d = T(0);
-      if (kz != T(0)) {
-        const T rb = sLz[hs] * kz, rd = sLz[kZPlane + hs] * kz, rf = sLz[2 * kZPlane + hs] * kz;
-        const T c35 = sC[4 * kSPlane + hf];
-        a = sC[2 * kSPlane + hf] * rb + c35 * rd;
-        b = sC[5 * kSPlane + hf] * rf;
-        c = sC[kSPlane + hf] * rb + sC[3 * kSPlane + hf] * rd;
-        d = c35 * rf;
+      if (k != T(0)) {
+        const T r0 = l0 * k, r1 = l1 * k, r2 = l2 * k;
+        if (hx) {  // ra, rc, re
+          const T c15 = sC[2 * kSPlane + hf];
+          a = sC[hf] * r0 + sC[kSPlane + hf] * r1;
+          b = c15 * r2;
+          c = c15 * r0 + sC[4 * kSPlane + hf] * r1;
+          d = sC[5 * kSPlane + hf] * r2;
+        } else {  // rb, rd, rf
+          const T c35 = sC[4 * kSPlane + hf];
+          a = sC[2 * kSPlane + hf] * r0 + c35 * r1;
+          b = sC[5 * kSPlane + hf] * r2;
+          c = sC[kSPlane + hf] * r0 + sC[3 * kSPlane + hf] * r1;
+          d = c35 * r2;
+        }
       }
-      sLz[hs] = a;
-      sLz[kZPlane + hs] = b;
-      sLz[2 * kZPlane + hs] = c;
-      sQz[hs] = d;
+      hl[0] = a;
+      hl[HP] = b;
+      hl[2 * HP] = c;
+      (hx ? sQx : sQz)[hs] = d;
     }
     __syncthreads();
     if (valid) {
@@ -1302,7 +1334,7 @@ __global__ void __launch_bounds__(kTileThreads, sizeof(T) == 4 ? 4 : 2)
       const StagedZ<T> q1{sLz, i0, j0}, q3{sLz + kZPlane, i0, j0}, q5{sLz + 2 * kZPlane, i0, j0}, q7{sQz, i0, j0};
       const T avx = dxb_t<NN>(g, q0, i, j) + dzb_t<NN>(g, q1, i, j) + dxf_t<NN>(g, q2, i, j) + dzf_t<NN>(g, q3, i, j);
       const T avz = dxb_t<NN>(g, q4, i, j) + dzb_t<NN>(g, q5, i, j) + dxf_t<NN>(g, q6, i, j) + dzf_t<NN>(g, q7, i, j);
-      const int64_t o = (int64_t)s * PL + oc;
+      const int64_t o = so + oc;
       lv[VX * NSP + o] = avx;
       lv[VZ * NSP + o] = avz;
       if (inside) {
@@ -1526,8 +1558,9 @@ ECarve ecarve(const adfwi_elastic_plan* p, bool grad, int K) {
     c.snap_scale = take(full ? 0 : (int64_t)nseg * nstate * ns * 4);
     c.hv = take((int64_t)K * 2 * ns * pl);  // velocity totals at the start of each step
     c.ht = take((int64_t)K * 3 * ns * pl);  // stress totals after each step's free surface
-    // lambda of the split stresses (6) and of the split velocities (4, twice: read one, write the other)
-    c.lst = take((int64_t)(p->d.pml ? 14 : 3) * ns * pl);
+    // lambda of the split stresses (6) and of the split velocities (4), twice each (a reverse
+    // step reads one copy and writes the other)
+    c.lst = take((int64_t)(p->d.pml ? 20 : 3) * ns * pl);
     c.lt = take(3 * ns * pl);
     c.lv = take(2 * ns * pl);
     c.lv2 = take(2 * ns * pl);
@@ -1782,7 +1815,7 @@ int ebackward(const adfwi_elastic_plan* p, const void* wavelet, const void* grec
   T* gcp = reinterpret_cast<T*>(ws + c.gc);
   T* qsrc = reinterpret_cast<T*>(ws + c.qsrc);
   const T* gr = static_cast<const T*>(grec);
-  const int nsf = p->d.pml ? 14 : 3;
+  const int nsf = p->d.pml ? 20 : 3;
   ADFWI_CUDA_TRY(cudaMemsetAsync(lst, 0, nsf * NSP * sizeof(T), s));
   ADFWI_CUDA_TRY(cudaMemsetAsync(lt, 0, 3 * NSP * sizeof(T), s));
   ADFWI_CUDA_TRY(cudaMemsetAsync(lv, 0, 2 * NSP * sizeof(T), s));
@@ -1840,15 +1873,19 @@ int ebackward(const adfwi_elastic_plan* p, const void* wavelet, const void* grec
         // one stream of programmatically serialised launches per reverse step; lt is
         // overwritten by adj_t_pml before the stress-record gradients are added to it
         if (gr) ADFWI_LAUNCH(kAux, s, (void)launch_pdl_kernel(el::adj_inject<T>, ginj, dim3(128), 0, s, g, it, gr, lt, lv, 1));
-        T* lvs_in = lst + (6 + 4 * flip) * NSP;
-        T* lvs_out = lst + (10 - 4 * flip) * NSP;
+        // lambda of the split stresses: planes 0-5 / 6-11 of lst, of the split velocities 12-15 /
+        // 16-19; each reverse step reads one copy and writes the other
+        const int f = flip;
         flip ^= 1;
+        T* lvs_in = lst + (12 + 4 * f) * NSP;
+        T* lvs_out = lst + (16 - 4 * f) * NSP;
+        T* lts_in = lst + (6 * f) * NSP;
+        T* lts_out = lst + (6 - 6 * f) * NSP;
         ADFWI_LAUNCH(kElAdjStep, s, (void)launch_pdl_kernel(el::adj_t_pml<T, NN>, gcg, b, (size_t)smem_t, s, g, cf,
                                                             (const T*)lv, (const T*)lvs_in, lvs_out, lt, th, gcp, eg));
         if (gr) ADFWI_LAUNCH(kAux, s, (void)launch_pdl_kernel(el::adj_inject<T>, ginj, dim3(128), 0, s, g, it, gr, lt, lv, 2));
-        ADFWI_LAUNCH(kElAdjStep, s, (void)launch_pdl_kernel(el::adj_tfs_pml<T>, gcm, b, 0, s, g, cf, (const T*)lt, lst));
         ADFWI_LAUNCH(kElAdjStep, s, (void)launch_pdl_kernel(el::adj_v_pml<T, NN>, gcg, b, (size_t)smem_vp, s, g, cf,
-                                                            (const T*)lst, lv, vh, gcp, eg));
+                                                            (const T*)lt, (const T*)lts_in, lts_out, lv, vh, gcp, eg));
       } else {
         if (gr) ADFWI_LAUNCH(kAux, s, (el::adj_inject<T><<<ginj, 128, 0, s>>>(g, it, gr, lst, lv, 3)));
         ADFWI_LAUNCH(kElAdjStep, s, (el::adj_vfs_abl<T><<<gcs, b, 0, s>>>(g, cf, lv, lv2, nullptr)));

@@ -783,8 +783,11 @@ template <int N>
 __device__ __forceinline__ void cp_async_wait_group() {
   asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
+#ifndef ADFWI_EL_ADJT_MINB
+#define ADFWI_EL_ADJT_MINB 5
+#endif
 template <typename T, int NN>
-__global__ void __launch_bounds__(kTileThreads, sizeof(T) == 4 ? 5 : 2)
+__global__ void __launch_bounds__(kTileThreads, sizeof(T) == 4 ? ADFWI_EL_ADJT_MINB : 2)
     adj_t_pml(Geo<T> g, const T* __restrict__ cf, const T* __restrict__ lv, const T* __restrict__ lvs_in,
               T* __restrict__ lvs_out, T* __restrict__ lt, const T* __restrict__ tt_hist, T* __restrict__ gpart,
               int eg) {

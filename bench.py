@@ -325,7 +325,7 @@ def fp64_error(args, dev, memory_fraction):
         model.vp.data.copy_(torch.as_tensor(vp_init, device=dev))
         loss, rec = prop.forward_l2(obs)
         loss.backward()
-        res[dtype] = (rec["p"].detach().double(), model.vp.grad.detach().double(), float(loss),
+        res[dtype] = (rec["p"].detach().double(), model.vp.grad.detach().double(), float(loss.detach()),
                       prop.plan()[1].snapshot_every)
         del model, prop, rec, obs
         torch.cuda.empty_cache()

@@ -154,7 +154,7 @@ def test_checkpointed_gradient_is_bit_identical_to_the_full_history():
         loss, rec = prop.forward_l2(obs, silent_rel=1e-3, normalise_obs=True)
         loss.backward()
         assert prop.plan()[1].snapshot_every == (300 if K == 0 else K)
-        res[K] = (float(loss), rec["p"].detach().clone(), model.vp.grad.detach().clone())
+        res[K] = (float(loss.detach()), rec["p"].detach().clone(), model.vp.grad.detach().clone())
     for K in (40, 75):
         assert res[K][0] == res[0][0]
         assert torch.equal(res[K][1], res[0][1]) and torch.equal(res[K][2], res[0][2])

@@ -48,7 +48,8 @@ def test_fused_misfit_is_the_autograd_gradient():
     s2 = syn.clone().requires_grad_(True)
     loss = l2_misfit(s2, obs, 1e-3)
     (2.0 * loss).backward()
-    assert abs(float(loss.detach()) - float(ref)) <= 1e-12 * float(ref)
+    r = float(ref.detach())
+    assert abs(float(loss.detach()) - r) <= 1e-12 * r
     assert float((s2.grad - 2.0 * s.grad).norm() / (2.0 * s.grad).norm()) <= 1e-12
 
 
